@@ -1,0 +1,66 @@
+/*
+ * spws device-resident API.
+ *
+ * The TACO entry points in taco_abi.h take host arrays and return malloc'd
+ * host arrays, like the reference. Callers that keep operands on the GPU
+ * (benchmarks, the batched and served forms) use these calls instead: inputs
+ * and outputs are device arrays owned by the library's stream-ordered pool.
+ * This API has no counterpart in the reference, whose kernels are CPU-only.
+ */
+#ifndef SPWS_DEVICE_H
+#define SPWS_DEVICE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A CSR matrix whose arrays live in device memory. */
+typedef struct spws_csr_dev {
+  int32_t nrows;
+  int32_t ncols;
+  int64_t nnz;
+  int32_t* pos;  /* nrows + 1 */
+  int32_t* crd;  /* nnz */
+  double* vals;  /* nnz */
+} spws_csr_dev;
+
+/* How products are summed into an output entry.
+ *  SPWS_ACCUM_ATOMIC: products are added with FP64 atomics in the order the
+ *    GPU issues them (fastest path; order not fixed).
+ */
+enum { SPWS_ACCUM_ATOMIC = 0 };
+
+typedef struct spws_spgemm_stats {
+  int64_t products;      /* scalar products a_ij * b_jk (flops = 2 * products) */
+  int64_t nnz;           /* output nonzeros */
+  float ms_setup;        /* row analysis + chunk table + scheduling order */
+  float ms_symbolic;     /* symbolic pass (per-row output counts) */
+  float ms_scan;         /* counts -> C.pos */
+  float ms_numeric;      /* numeric pass (accumulate + write crd/vals) */
+  float ms_total;        /* all of the above, device time */
+  int32_t chunk_width;   /* columns per dense accumulator chunk */
+  int32_t n_chunks;      /* chunks covering B's columns */
+} spws_spgemm_stats;
+
+/* Copy a host CSR into library-owned device memory. */
+int spws_csr_upload(const int32_t* pos, const int32_t* crd, const double* vals, int32_t nrows, int32_t ncols,
+                    spws_csr_dev* out);
+/* Copy a device CSR back into caller-provided host arrays (sizes from `m`). */
+int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double* vals);
+/* Release a device CSR allocated by the library (upload or spgemm). */
+int spws_csr_release(spws_csr_dev* m);
+
+/* C = A * B on the current device; C's arrays are allocated by the library.
+ * `stats` may be NULL. Synchronises once internally (to size C). */
+int spws_spgemm_csr_device(const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C, int accum_mode,
+                           spws_spgemm_stats* stats);
+
+/* Block until the library's stream on the current device is idle. */
+int spws_device_sync(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

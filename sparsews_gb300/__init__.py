@@ -1,0 +1,148 @@
+"""spws-gb300: the sparse-workspace kernels of SparseWS as GB300 (sm_103a) CUDA.
+
+Python front end over ``libspws.so`` (the C ABI of include/spws/*.h). The
+library is built in-tree by ``sparsews_gb300.build`` (nvcc, sm_103a); nothing
+here computes on the CPU: if the library is missing the calls raise.
+
+High-level helpers take and return numpy CSR triples ``(pos, crd, vals)``:
+
+* ``spgemm(A, B)``: C = A*B through the reference-compatible C entry point
+  ``spws_csr_csr_hash_compute`` (host arrays in, malloc'd host arrays out).
+* ``DeviceCsr`` / ``spgemm_device``: the device-resident API
+  (``spws_csr_upload``, ``spws_spgemm_csr_device``, ...).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import taco
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libspws.so")
+
+_lib = None
+
+
+class SpwsError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"spws status {status}: {msg}")
+        self.status = status
+
+
+class CsrDev(C.Structure):
+    _fields_ = [("nrows", C.c_int32), ("ncols", C.c_int32), ("nnz", C.c_int64),
+                ("pos", C.c_void_p), ("crd", C.c_void_p), ("vals", C.c_void_p)]
+
+
+class SpgemmStats(C.Structure):
+    _fields_ = [("products", C.c_int64), ("nnz", C.c_int64), ("ms_setup", C.c_float), ("ms_symbolic", C.c_float),
+                ("ms_scan", C.c_float), ("ms_numeric", C.c_float), ("ms_total", C.c_float),
+                ("chunk_width", C.c_int32), ("n_chunks", C.c_int32)]
+
+
+def lib():
+    """Load libspws.so (raises if it has not been built: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with sparsews_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    P = C.POINTER(taco.TacoTensor)
+    sig = {
+        "spws_status_string": ([C.c_int], C.c_char_p),
+        "spws_last_error": ([], C.c_char_p),
+        "spws_version": ([], C.c_char_p),
+        "spws_free": ([C.c_void_p], None),
+        "spws_device_sync": ([], C.c_int),
+        "spws_csr_csr_hash_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_csr_csr_taco_compute": ([P, P, P], C.c_int),
+        "CSR_CSR_hash": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "CSR_CSR_taco": ([P, P, P, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "spws_csr_upload": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CsrDev)], C.c_int),
+        "spws_csr_download": ([C.POINTER(CsrDev), C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+        "spws_csr_release": ([C.POINTER(CsrDev)], C.c_int),
+        "spws_spgemm_csr_device": ([C.POINTER(CsrDev), C.POINTER(CsrDev), C.POINTER(CsrDev), C.c_int,
+                                    C.POINTER(SpgemmStats)], C.c_int),
+    }
+    for name, (argt, rest) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = argt
+        f.restype = rest
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != 0:
+        L = lib()
+        raise SpwsError(status, L.spws_last_error().decode())
+    return status
+
+
+def _free_fn():
+    return lib().spws_free
+
+
+def spgemm(A, B, method="hash"):
+    """C = A*B for numpy CSR tuples (pos, crd, vals, nrows, ncols) through the
+    TACO C entry point. Returns (pos, crd, vals)."""
+    L = lib()
+    ap, ac, av, an, am = A
+    bp, bc, bv, bn, bm = B
+    At = taco.csr(ap, ac, av, an, am)
+    Bt = taco.csr(bp, bc, bv, bn, bm)
+    Ct = taco.init_dc(an, bm)
+    if method == "hash":
+        check(L.spws_csr_csr_hash_compute(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
+    elif method == "taco":
+        check(L.spws_csr_csr_taco_compute(Ct.ptr(), At.ptr(), Bt.ptr()))
+    else:
+        raise ValueError(method)
+    return taco.take_csr(Ct, an, L.spws_free)
+
+
+class DeviceCsr:
+    """A CSR matrix in library-owned device memory."""
+
+    def __init__(self, m=None):
+        self.m = m if m is not None else CsrDev()
+
+    @classmethod
+    def upload(cls, pos, crd, vals, nrows, ncols):
+        L = lib()
+        pos = np.ascontiguousarray(pos, np.int32)
+        crd = np.ascontiguousarray(crd, np.int32)
+        vals = np.ascontiguousarray(vals, np.float64)
+        d = cls()
+        check(L.spws_csr_upload(pos.ctypes.data, crd.ctypes.data, vals.ctypes.data, nrows, ncols, C.byref(d.m)))
+        return d
+
+    def download(self):
+        L = lib()
+        pos = np.empty(self.m.nrows + 1, np.int32)
+        crd = np.empty(max(self.m.nnz, 1), np.int32)
+        vals = np.empty(max(self.m.nnz, 1), np.float64)
+        check(L.spws_csr_download(C.byref(self.m), pos.ctypes.data, crd.ctypes.data, vals.ctypes.data))
+        return pos, crd[: self.m.nnz], vals[: self.m.nnz]
+
+    def release(self):
+        if self.m.pos:
+            lib().spws_csr_release(C.byref(self.m))
+            self.m = CsrDev()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def spgemm_device(A, B, accum_mode=0):
+    """C = A*B for DeviceCsr operands; returns (DeviceCsr C, SpgemmStats)."""
+    L = lib()
+    Cd = DeviceCsr()
+    st = SpgemmStats()
+    check(L.spws_spgemm_csr_device(C.byref(A.m), C.byref(B.m), C.byref(Cd.m), accum_mode, C.byref(st)))
+    return Cd, st

@@ -1,0 +1,160 @@
+// Per-device state, stream-ordered allocation, error strings and device-side
+// validation of CSR operands (so that no kernel ever indexes out of bounds on
+// malformed input: every row's positions and columns are checked first).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "spws_internal.h"
+#include "validate.h"
+
+namespace spws {
+
+static thread_local std::string g_err;
+void set_error(const std::string& msg) { g_err = msg; }
+void clear_error() { g_err.clear(); }
+
+static std::mutex g_dev_mu;
+static DeviceState g_dev[64];
+
+int device_state(DeviceState** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    set_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+    return SPWS_ERR_NO_DEVICE;
+  }
+  if (dev < 0 || dev >= 64) {
+    set_error("device ordinal out of range");
+    return SPWS_ERR_NO_DEVICE;
+  }
+  std::lock_guard<std::mutex> g(g_dev_mu);
+  DeviceState& d = g_dev[dev];
+  if (!d.init) {
+    d.device = dev;
+    SPWS_CUDA(cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev));
+    int optin = 0;
+    SPWS_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    d.smem_optin = (size_t)optin;
+    SPWS_CUDA(cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking));
+    // keep freed blocks in the pool: repeated calls reuse them
+    cudaMemPool_t pool;
+    SPWS_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t thresh = UINT64_MAX;
+    SPWS_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thresh));
+    d.init = true;
+  }
+  *out = &d;
+  return SPWS_OK;
+}
+
+int dalloc(void** p, size_t bytes, cudaStream_t s) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    set_error("device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+    *p = nullptr;
+    return SPWS_ERR_NOMEM;
+  }
+  return SPWS_OK;
+}
+
+void dfree(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+namespace {
+
+// Thread per row: 0 <= pos[i] <= pos[i+1] <= nnz, columns in [0, ncols) and
+// strictly increasing within the row. Any violation sets *bad.
+__global__ void k_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int32_t* __restrict__ pos,
+                               const int32_t* __restrict__ crd, int* __restrict__ bad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t s = pos[i], e = pos[i + 1];
+  if (s < 0 || e < s || (int64_t)e > nnz) {
+    atomicExch(bad, 1);
+    return;
+  }
+  int prev = -1;
+  for (int32_t p = s; p < e; p++) {
+    const int k = crd[p];
+    if (k <= prev || k >= ncols) {
+      atomicExch(bad, 1);
+      return;
+    }
+    prev = k;
+  }
+}
+
+}  // namespace
+
+int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
+                        const char* what, cudaStream_t s) {
+  if (nrows < 0 || ncols < 0 || nnz < 0 || nnz > INT32_MAX) {
+    set_error(std::string(what) + ": negative or oversized dimensions");
+    return SPWS_ERR_INVALID;
+  }
+  int32_t ends[2] = {0, 0};
+  SPWS_CUDA(cudaMemcpyAsync(&ends[0], pos, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&ends[1], pos + nrows, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  int* bad = nullptr;
+  SPWS_TRY(dalloc((void**)&bad, sizeof(int), s));
+  SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  if (nrows > 0) {
+    k_validate_csr<<<(unsigned)((nrows + 255) / 256), 256, 0, s>>>(nrows, nnz, ncols, pos, crd, bad);
+    SPWS_CUDA(cudaGetLastError());
+  }
+  int hbad = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  dfree(bad, s);
+  if (ends[0] != 0 || (int64_t)ends[1] != nnz) {
+    set_error(std::string(what) + ": pos[0] must be 0 and pos[nrows] must equal nnz");
+    return SPWS_ERR_INVALID;
+  }
+  if (hbad) {
+    set_error(std::string(what) + ": positions not monotone, or columns out of range / not strictly increasing");
+    return SPWS_ERR_INVALID;
+  }
+  return SPWS_OK;
+}
+
+}  // namespace spws
+
+extern "C" {
+
+const char* spws_status_string(int status) {
+  switch (status) {
+    case SPWS_OK: return "ok";
+    case SPWS_ERR_INVALID: return "invalid argument";
+    case SPWS_ERR_NOMEM: return "out of memory";
+    case SPWS_ERR_CUDA: return "CUDA error";
+    case SPWS_ERR_CAPACITY: return "capacity exceeded";
+    case SPWS_ERR_TIMEOUT: return "device wait timed out";
+    case SPWS_ERR_NO_DEVICE: return "no CUDA device";
+    case SPWS_ERR_BUSY: return "admission refused";
+    default: return "unknown status";
+  }
+}
+
+const char* spws_last_error(void) { return spws::g_err.c_str(); }
+
+const char* spws_version(void) { return "spws-gb300 0.1 (sm_103a)"; }
+
+void spws_free(void* p) { free(p); }
+
+int spws_device_sync(void) {
+  spws::DeviceState* ds = nullptr;
+  SPWS_TRY(spws::device_state(&ds));
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
+  return SPWS_OK;
+}
+
+}  // extern "C"

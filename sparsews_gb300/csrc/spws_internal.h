@@ -1,0 +1,75 @@
+// Internal declarations shared by the host C-ABI layer and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/spws/taco_abi.h"
+#include "../../include/spws/spws_device.h"
+
+namespace spws {
+
+// Thread-local error message; set by the failing call, read by spws_last_error().
+void set_error(const std::string& msg);
+void clear_error();
+
+// Wraps a CUDA call: on failure records the message and returns SPWS_ERR_CUDA
+// (or SPWS_ERR_NOMEM for allocation failures) from the enclosing function.
+#define SPWS_CUDA(call)                                                                 \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      ::spws::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));            \
+      (void)cudaGetLastError();                                                         \
+      return e_ == cudaErrorMemoryAllocation ? SPWS_ERR_NOMEM : SPWS_ERR_CUDA;          \
+    }                                                                                   \
+  } while (0)
+
+#define SPWS_TRY(expr)            \
+  do {                            \
+    int rc_ = (expr);             \
+    if (rc_ != SPWS_OK) return rc_; \
+  } while (0)
+
+// Per-device state: a stream-ordered memory pool that keeps freed blocks for
+// reuse, so repeated calls do not go back to the driver.
+struct DeviceState {
+  int device = -1;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;  // the library's default stream on this device
+  bool init = false;
+};
+int device_state(DeviceState** out);  // current device's state, created on first use
+
+// Stream-ordered allocation helpers (cudaMallocAsync on the given stream).
+int dalloc(void** p, size_t bytes, cudaStream_t s);
+void dfree(void* p, cudaStream_t s);
+
+// ---- SpGEMM (row-wise, column-chunked dense workspace) ----
+struct SpgemmOpts {
+  int accum_mode = SPWS_ACCUM_ATOMIC;
+};
+
+// Device CSR view used by the kernels (pointers on the device).
+struct CsrView {
+  int32_t nrows = 0, ncols = 0;
+  int64_t nnz = 0;
+  const int32_t* pos = nullptr;
+  const int32_t* crd = nullptr;
+  const double* vals = nullptr;
+};
+
+// Full pipeline on `stream`: C = A*B. Allocates C's arrays with dalloc.
+// `transpose_key` is reserved (0).
+int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const SpgemmOpts& opt,
+                   spws_spgemm_stats* stats, cudaStream_t stream);
+
+// Exclusive scan of `n` int32 counts into `out[0..n]` (out[n] = total), with
+// the total also returned through `total_dev` (int64, device) so callers can
+// detect overflow of int32 positions.
+int scan_counts_i32(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev, cudaStream_t s);
+
+}  // namespace spws

@@ -1,0 +1,11 @@
+// Device-side operand validation (see device.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace spws {
+// Checks a device CSR: pos[0] == 0, pos[nrows] == nnz, positions monotone,
+// columns in [0, ncols) and strictly increasing per row. Synchronises `s`.
+int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
+                        const char* what, cudaStream_t s);
+}  // namespace spws

@@ -1,0 +1,136 @@
+"""GPU parity of the row-wise SpGEMM (CSR x CSR) against the oracle and the
+reference's golden vectors, through the C ABI."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from _check import abs_csr, assert_csr_close
+from sparsews_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def csr(z, p):
+    n, m = (int(x) for x in z[p + "_shape"])
+    return z[p + "_pos"], z[p + "_crd"], z[p + "_vals"], n, m
+
+
+def scale_of(A, B):
+    return oracle.spgemm("taco", abs_csr(A), abs_csr(B))[2]
+
+
+@pytest.mark.parametrize("name", sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLD, "spgemm_*.npz"))
+                                        if "spgemm_t_" not in f))
+@pytest.mark.parametrize("method", ["hash", "taco"])
+def test_golden(spws_lib, name, method):
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    A, B = csr(z, "A"), csr(z, "B")
+    got = sp.spgemm(A, B, method=method)
+    ref = (z["pos"], z["crd"], z[method + "_vals"])
+    assert_csr_close(got, ref, z["absprod_vals"], name)
+
+
+@pytest.mark.parametrize("case", ["er", "rmat", "band", "poisson"])
+def test_against_oracle(spws_lib, case):
+    import sparsews_gb300 as sp
+    A = {"er": lambda: gen.er(3000, 10, seed=41),
+         "rmat": lambda: gen.rmat(12, 8, seed=42),
+         "band": lambda: gen.band(50000, 8, 0.5, seed=43),
+         "poisson": lambda: gen.poisson_rows(20000, 8.0, seed=44)}[case]()
+    got = sp.spgemm(A, A)
+    ref = oracle.spgemm("taco", A, A)
+    assert_csr_close(got, ref, scale_of(A, A), case)
+
+
+def test_wide_columns_many_chunks(spws_lib):
+    """Columns spread over many dense-workspace chunks (ncols >> chunk width)."""
+    import sparsews_gb300 as sp
+    rng = np.random.default_rng(45)
+    n, m = 300, 200000
+    A = gen.poisson_rows(n, 5.0, seed=46)
+    A = (A[0], A[1] % n, A[2], n, n)
+    # B: n x m with scattered columns
+    cnt = rng.poisson(30, n)
+    rows = np.repeat(np.arange(n), cnt)
+    cols = rng.integers(0, m, len(rows))
+    key = np.unique(rows.astype(np.int64) * m + cols)
+    rows, cols = key // m, (key % m).astype(np.int32)
+    pos = np.zeros(n + 1, np.int64)
+    np.add.at(pos, rows + 1, 1)
+    B = (np.cumsum(pos).astype(np.int32), cols, rng.uniform(-1, 1, len(cols)), n, m)
+    A = (A[0], np.sort(A[1].reshape(-1)) if False else A[1], A[2], n, n)
+    # rows of A must stay sorted after the modulo: rebuild
+    rr = np.repeat(np.arange(n), np.diff(A[0]))
+    key = np.unique(rr.astype(np.int64) * n + A[1])
+    rr, cc = key // n, (key % n).astype(np.int32)
+    pa = np.zeros(n + 1, np.int64)
+    np.add.at(pa, rr + 1, 1)
+    A = (np.cumsum(pa).astype(np.int32), cc, rng.uniform(-1, 1, len(cc)), n, n)
+    got = sp.spgemm(A, B)
+    ref = oracle.spgemm("taco", A, B)
+    assert_csr_close(got, ref, scale_of(A, B), "wide")
+
+
+def test_empty_operands(spws_lib):
+    import sparsews_gb300 as sp
+    Z = (np.zeros(6, np.int32), np.zeros(0, np.int32), np.zeros(0), 5, 7)
+    B = gen.er(7, 3, seed=47)
+    B = (B[0], B[1], B[2], 7, 7)
+    p, c, v = sp.spgemm(Z, B)
+    assert np.array_equal(p, np.zeros(6, np.int32)) and len(c) == 0
+    E = (np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), 0, 7)
+    p, c, v = sp.spgemm(E, B)
+    assert len(p) == 1 and p[0] == 0
+
+
+def test_invalid_input_is_rejected(spws_lib):
+    """Out-of-range or unsorted columns are refused before any kernel runs."""
+    import sparsews_gb300 as sp
+    A = gen.er(50, 4, seed=48)
+    bad = (A[0], A[1].copy(), A[2], 50, 50)
+    bad[1][5] = 50  # out of range
+    with pytest.raises(sp.SpwsError) as e:
+        sp.spgemm(bad, A)
+    assert e.value.status == 1
+    bad = (A[0], A[1].copy(), A[2], 50, 50)
+    bad[1][[0, 1]] = bad[1][[1, 0]]  # unsorted row
+    with pytest.raises(sp.SpwsError):
+        sp.spgemm(A, bad)
+    # shape mismatch
+    with pytest.raises(sp.SpwsError):
+        sp.spgemm(A, (A[0][:41], A[1][:A[0][40]], A[2][:A[0][40]], 40, 50))
+
+
+def test_device_api_and_stats(spws_lib):
+    import sparsews_gb300 as sp
+    A = gen.rmat(11, 8, seed=49)
+    dA = sp.DeviceCsr.upload(*A)
+    dC, st = sp.spgemm_device(dA, dA)
+    got = dC.download()
+    ref = oracle.spgemm("taco", A, A)
+    assert_csr_close(got, ref, scale_of(A, A), "device")
+    assert st.products == int(np.diff(A[0])[A[1]].sum())
+    assert st.nnz == len(ref[1])
+    assert st.ms_total > 0
+    dC.release()
+    dA.release()
+
+
+def test_timing_wrapper_frees_like_reference(spws_lib):
+    import ctypes as C
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import taco
+    L = sp.lib()
+    A = gen.er(400, 6, seed=50)
+    At = taco.csr(*A)
+    Ct = taco.init_dc(400, 400)
+    t = L.CSR_CSR_hash(At.ptr(), At.ptr(), Ct.ptr(), 1024, 1, 3, True, False)
+    assert t > 0
+    got = taco.take_csr(Ct, 400, L.spws_free)  # the last repeat's output is left for the caller
+    ref = oracle.spgemm("taco", A, A)
+    assert_csr_close(got, ref, scale_of(A, A), "wrapper")
