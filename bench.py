@@ -1,0 +1,408 @@
+#!/usr/bin/env python3
+"""Benchmark: row-wise SpGEMM C = A*A on the R-MAT workload (2^18 x 2^18,
+16*2^18 edge draws with a=0.57 b=0.19 c=0.19 d=0.05, duplicates removed, FP64
+values U[-1,1], seeded synthetic data), reported as GFLOP/s (flops = 2 x scalar
+products) and as a fraction of the HBM roofline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl spws|reference]
+                    [--workload rmat|er|band]
+
+--impl spws (default): one step = one full SpGEMM (row analysis, symbolic pass,
+scan, numeric pass, output allocation) with A resident in HBM; L2 is flushed
+between timed steps. `e2e` repeats the step through the reference-compatible C
+entry point spws_csr_csr_hash_compute with host (page-locked) operands and
+malloc'd host outputs, copies included.
+
+--impl reference: the reference's CPU algorithm (the oracle's C restatement of
+benchmark/Parallel/CSR_CSR_hash_sequential.h, or the reference headers
+themselves where they were built) on a bounded row sample of the same
+workload, on all host cores (one thread per core, rows split between them).
+
+Under torchrun (N > 1) every rank runs the full product on its own GPU
+(independent replicas, no collective on the data path: weak scaling); rank 0
+prints one JSON line with the whole-job throughput over the slowest rank.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT]
+
+RMAT = dict(scale=18, deg=16, a=0.57, b=0.19, c=0.19, seed=42)
+L2_FLUSH_BYTES = 512 << 20  # > 2x the 126 MB L2
+
+
+def make_workload(name):
+    from sparsews_gb300 import gen
+    if name == "rmat":
+        A = gen.rmat(RMAT["scale"], RMAT["deg"], RMAT["a"], RMAT["b"], RMAT["c"], seed=RMAT["seed"])
+        cfg = {"workload": "rmat_spgemm_AxA", "n": 1 << RMAT["scale"], "edge_draws_per_row": RMAT["deg"],
+               "rmat_abc": [RMAT["a"], RMAT["b"], RMAT["c"]], "seed": RMAT["seed"]}
+    elif name == "er":
+        A = gen.er(10000, 10, seed=42)
+        cfg = {"workload": "er_spgemm_AxA", "n": 10000, "per_row": 10, "seed": 42}
+    elif name == "band":
+        A = gen.band(1 << 20, 8, 0.5, seed=42)
+        cfg = {"workload": "band_spgemm_AxA", "n": 1 << 20, "half_bandwidth": 8, "fill": 0.5, "seed": 42}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    products = int(np.diff(A[0]).astype(np.int64)[A[1]].sum())
+    cfg.update({"nnz_A": int(len(A[1])), "products": products, "value_dtype": "f64", "index_dtype": "int32"})
+    return A, cfg
+
+
+def gustavson_bytes(nA, nnzA, products, nC, nnzC):
+    """Algorithmic bytes of one SpGEMM under the Gustavson traffic model:
+    read A (pos + crd + vals), one B entry (crd + val) per product, write C."""
+    return 4 * (nA + 1) + 12 * nnzA + 12 * products + 4 * (nC + 1) + 12 * nnzC
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload):
+    """DRAM bytes per k_numeric launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"k_numeric_{workload}.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+# ------------------------------------------------------------------ CPU arm
+def cpu_sample_rows(A, target_products, seed=7):
+    """A fixed random sample of rows of A whose products total ~target."""
+    pos = A[0].astype(np.int64)
+    prod_per_entry = np.diff(pos)[A[1]]
+    cs = np.concatenate([[0], np.cumsum(prod_per_entry)])
+    rowp = cs[pos[1:]] - cs[pos[:-1]]
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(len(rowp))
+    cum = np.cumsum(rowp[order])
+    k = int(np.searchsorted(cum, target_products)) + 1
+    rows = np.sort(order[:k])
+    return rows, int(rowp[rows].sum())
+
+
+def sub_rows(A, rows):
+    pos, crd, vals, n, m = A
+    lens = np.diff(pos.astype(np.int64))[rows]
+    npos = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    idx = np.concatenate([np.arange(pos[r], pos[r + 1]) for r in rows]) if len(rows) else np.zeros(0, np.int64)
+    return npos, crd[idx], vals[idx], len(rows), m
+
+
+def run_cpu(A, rows, threads, kind):
+    """Runs the reference algorithm on the sampled rows split over `threads`
+    threads (the C code releases the GIL); returns (seconds, products)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    parts = np.array_split(rows, threads)
+    subs = [sub_rows(A, p) for p in parts]
+    w_cap = oracle.w_cap_default(len(A[1]))  # bench_hash_row_noT.cpp:45
+    out = [None] * threads
+
+    def work(t):
+        out[t] = oracle.spgemm("hash", subs[t], A, w_cap=w_cap, kind=kind)
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    t0 = time.perf_counter()
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    return time.perf_counter() - t0
+
+
+def cpu_kind():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    if os.path.exists(oracle.REF_SO):
+        return "reference"
+    oracle.build_port()
+    return "port"
+
+
+def cpu_baseline(A, target_products, threads):
+    kind = cpu_kind()
+    rows, prods = cpu_sample_rows(A, target_products)
+    secs = run_cpu(A, rows, threads, "ref" if kind == "reference" else "port")
+    return {"value": 2 * prods / secs / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": kind,
+            "sample": f"{len(rows)} random rows of A (seed 7) times the full A: {prods} products, {secs:.2f} s"}
+
+
+# ------------------------------------------------------------------ dist
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        return ws, rank, local, dist
+    return 1, 0, local, None
+
+
+def reduce_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ arms
+def bench_reference(args, ws, rank, dist):
+    if rank != 0:
+        return
+    A, cfg = make_workload(args.workload)
+    threads = os.cpu_count() or 1
+    kind = cpu_kind()
+    per_step = args.cpu_step_products
+    rows, prods = cpu_sample_rows(A, per_step)
+    for _ in range(args.warmup):
+        run_cpu(A, rows, threads, "ref" if kind == "reference" else "port")
+    times = [run_cpu(A, rows, threads, "ref" if kind == "reference" else "port") for _ in range(args.steps)]
+    secs = sum(times) / len(times)
+    val = 2 * prods / secs / 1e9
+    line = {"impl": "reference", "metric": "spgemm_gflops", "value": val, "unit": "GFLOP/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded R-MAT)",
+            "config": cfg,
+            "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": threads, "kind": kind,
+                             "sample": f"{len(rows)} random rows of A (seed 7) times the full A per step: {prods} products"},
+            "e2e": {"value": val, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def bench_spws(args, ws, rank, local, dist):
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import build, taco
+    build.build()
+    L = sp.lib()
+    L.spws_launch_count.restype = C.c_ulonglong
+    L.spws_flush_l2.argtypes = [C.c_size_t]
+    L.spws_host_pin.argtypes = [C.c_void_p, C.c_size_t]
+    L.spws_host_unpin.argtypes = [C.c_void_p]
+    L.spws_set_device.argtypes = [C.c_int]
+    sp.check(L.spws_set_device(local))
+
+    A, cfg = make_workload(args.workload)
+    nA = A[3]
+    dA = sp.DeviceCsr.upload(*A)
+
+    def step():
+        dC, st = sp.spgemm_device(dA, dA)
+        nnz = st.nnz
+        dC.release()
+        return st, nnz
+
+    for _ in range(args.warmup):
+        step()
+    sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+    barrier(dist)
+    sp.check(L.spws_device_sync())
+
+    walls, stats = [], []
+    l0 = L.spws_launch_count()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))  # between timed steps, outside the timed window
+            t0 = time.perf_counter()
+            st, nnzC = step()
+            t1 = time.perf_counter()
+            walls.append(t1 - t0)
+            stats.append(st)
+    launches = (L.spws_launch_count() - l0) // args.steps
+    # flush launches are cudaMemset, not kernels of this library
+    wall = sum(walls) / len(walls)
+    wall_max = reduce_max(dist, wall)
+    products = stats[0].products
+    flops_job = 2.0 * products * ws
+    value = flops_job / wall_max / 1e9
+
+    ms_num = sum(s.ms_numeric for s in stats) / len(stats)
+    ms_sym = sum(s.ms_symbolic for s in stats) / len(stats)
+    ms_dev = sum(s.ms_total for s in stats) / len(stats)
+    alg_bytes = gustavson_bytes(nA, len(A[1]), products, nA, nnzC)
+    peak, peak_src = measured_peaks()
+    achieved = alg_bytes / (ms_num * 1e-3) / 1e9
+    dev_flops = 2.0 * products / (ms_dev * 1e-3) / 1e9
+
+    # ---- e2e through the reference-compatible C entry point, host buffers ----
+    pos = np.ascontiguousarray(A[0], np.int32)
+    crd = np.ascontiguousarray(A[1], np.int32)
+    vals = np.ascontiguousarray(A[2], np.float64)
+    pinned = []
+    for arr in (pos, crd, vals):
+        if L.spws_host_pin(arr.ctypes.data, arr.nbytes) == 0:
+            pinned.append(arr)
+    At = taco.csr(pos, crd, vals, nA, A[4])
+    e2e_walls = []
+    h2d = 2 * (pos.nbytes + crd.nbytes + vals.nbytes)  # A and B are both copied in
+    d2h = 0
+    for it in range(max(1, args.e2e_steps) + 1):
+        Ct = taco.init_dc(nA, A[4])
+        barrier(dist)
+        t0 = time.perf_counter()
+        sp.check(L.spws_csr_csr_hash_compute(Ct.ptr(), At.ptr(), At.ptr(), 0))
+        t1 = time.perf_counter()
+        nnz = int(Ct.t.vals_size)
+        d2h = 4 * (nA + 1) + 12 * nnz
+        for p in (Ct.t.indices[1][0], Ct.t.indices[1][1]):
+            L.spws_free(C.cast(p, C.c_void_p))
+        L.spws_free(C.cast(Ct.t.vals, C.c_void_p))
+        if it > 0:  # first call is a warm-up (host allocator, page faults)
+            e2e_walls.append(t1 - t0)
+    for arr in pinned:
+        L.spws_host_unpin(arr.ctypes.data)
+    e2e_wall = reduce_max(dist, sum(e2e_walls) / len(e2e_walls))
+    e2e_value = flops_job / e2e_wall / 1e9
+
+    if rank != 0:
+        return
+    cpu = None
+    if ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(A, args.cpu_products, 1)
+    line = {
+        "metric": "spgemm_gflops",
+        "value": value,
+        "unit": "GFLOP/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": wall_max * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded R-MAT generator, numpy PCG64 seed 42)",
+        "config": {**cfg, "parallelism": f"replicas{ws}", "l2": "flushed between timed steps (512 MiB write)",
+                   "accumulate": "fp64 shared-memory atomics"},
+        "device_ms_per_step": ms_dev,
+        "device_gflops": dev_flops,
+        "phase_ms": {"symbolic": ms_sym, "numeric": ms_num,
+                     "setup": sum(s.ms_setup for s in stats) / len(stats),
+                     "scan": sum(s.ms_scan for s in stats) / len(stats)},
+        "nnz_C": nnzC,
+        "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "traffic": profiled_traffic(args.workload)},
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_wall * 1e3, "path": "spws_csr_csr_hash_compute (taco_tensor_t, host arrays)"},
+        "gpu_launches": int(launches * args.steps),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="spws", choices=["spws", "reference"])
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-products", type=int, default=60_000_000, help="products in the CPU-baseline sample")
+    ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
+                    help="products per step of the reference arm (all cores)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local, dist = dist_init()
+    if args.impl == "reference":
+        bench_reference(args, ws, rank, dist)
+    else:
+        bench_spws(args, ws, rank, local, dist)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -10,6 +10,7 @@
 #ifndef SPWS_DEVICE_H
 #define SPWS_DEVICE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -57,8 +58,21 @@ int spws_csr_release(spws_csr_dev* m);
 int spws_spgemm_csr_device(const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C, int accum_mode,
                            spws_spgemm_stats* stats);
 
+/* Make `device` current for the calling thread (cudaSetDevice). */
+int spws_set_device(int device);
+
 /* Block until the library's stream on the current device is idle. */
 int spws_device_sync(void);
+
+/* Number of kernels this library has launched so far in this process. */
+unsigned long long spws_launch_count(void);
+
+/* Overwrite `bytes` of scratch device memory (evicts the L2 between timed runs). */
+int spws_flush_l2(size_t bytes);
+
+/* Page-lock / unlock a host range so copies to and from it run at DMA speed. */
+int spws_host_pin(void* p, size_t bytes);
+int spws_host_unpin(void* p);
 
 #ifdef __cplusplus
 }

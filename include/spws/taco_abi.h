@@ -190,6 +190,12 @@ int spws_coo_csf_dcsr_dcsr_bucket_compute(taco_tensor_t* A, taco_tensor_t* B, ta
 double COO_CSF_DCSR_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D, int32_t w_cap,
                                 int32_t warmup, int32_t repeat, bool bench, bool print);
 
+/* Replaces `void COO_CSF_DCSR_DCSR_coord(A, B, C, D, w_cap, print=false)` of
+ * benchmark/MTTKRP/COO_CSF_DCSR_DCSR_coord_index_chase_flex.h:382 (coordinate
+ * workspace); errors through spws_last_error(). */
+void COO_CSF_DCSR_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D, int32_t w_cap,
+                             bool print);
+
 /* ------------------------------------------------------------------------ */
 /* TTM A(k,j,l) = sum_i B(k,i,j) * C(i,l): B in CSF (k,i,j), C in DCSR,        */
 /* A is sorted 3-D COO.                                                         */
@@ -209,6 +215,10 @@ int spws_coo_csf_dcsr_bucket_compute(taco_tensor_t* A, taco_tensor_t* B, taco_te
 /* Replaces `double COO_CSF_DCSR_bucket(...)` of benchmark/TTM/COO_CSF_DCSR_bucket_il.h:411. */
 double COO_CSF_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
                            int32_t repeat, bool bench, bool print);
+
+/* Replaces `void COO_CSF_DCSR_coord(A, B, C, w_cap, print=false)` of
+ * benchmark/TTM/COO_CSF_DCSR_coord_il.h:395; errors through spws_last_error(). */
+void COO_CSF_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print);
 
 #ifdef __cplusplus
 }

@@ -60,6 +60,26 @@ def lib():
         "spws_csr_csr_taco_compute": ([P, P, P], C.c_int),
         "CSR_CSR_hash": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
         "CSR_CSR_taco": ([P, P, P, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "spws_csr_csr_coord_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_dcsc_dcsr_hash_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_dcsc_dcsr_bucket_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_dcsc_dcsr_coord_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_csc_csr_t_hash_compute": ([P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+        "DCSC_DCSR_hash": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "DCSC_DCSR_bucket": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "DCSC_DCSR_coord": ([P, P, P, C.c_int32, C.c_bool], None),
+        "CSC_CSR_T_hash": ([P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_double),
+        "spws_coo_csf_dcsr_dcsr_hash_compute": ([P, P, P, P, C.c_int32], C.c_int),
+        "spws_coo_csf_dcsr_dcsr_bucket_compute": ([P, P, P, P, C.c_int32], C.c_int),
+        "spws_coo_csf_dcsr_hash_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_coo_csf_dcsr_bucket_compute": ([P, P, P, C.c_int32], C.c_int),
+        "COO_CSF_DCSR_DCSR_hash": ([P, P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "COO_CSF_DCSR_hash": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "spws_set_device": ([C.c_int], C.c_int),
+        "spws_launch_count": ([], C.c_ulonglong),
+        "spws_flush_l2": ([C.c_size_t], C.c_int),
+        "spws_host_pin": ([C.c_void_p, C.c_size_t], C.c_int),
+        "spws_host_unpin": ([C.c_void_p], C.c_int),
         "spws_csr_upload": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CsrDev)], C.c_int),
         "spws_csr_download": ([C.POINTER(CsrDev), C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "spws_csr_release": ([C.POINTER(CsrDev)], C.c_int),
@@ -98,9 +118,77 @@ def spgemm(A, B, method="hash"):
         check(L.spws_csr_csr_hash_compute(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
     elif method == "taco":
         check(L.spws_csr_csr_taco_compute(Ct.ptr(), At.ptr(), Bt.ptr()))
+    elif method == "coord":
+        check(L.spws_csr_csr_coord_compute(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
     else:
         raise ValueError(method)
     return taco.take_csr(Ct, an, L.spws_free)
+
+
+def _csr_transpose_np(pos, crd, vals, nrow, ncol):
+    pos = np.asarray(pos, np.int64)
+    rows = np.repeat(np.arange(nrow, dtype=np.int64), np.diff(pos))
+    order = np.lexsort((rows, np.asarray(crd, np.int64)))
+    tpos = np.zeros(ncol + 1, np.int64)
+    np.add.at(tpos, np.asarray(crd, np.int64) + 1, 1)
+    return np.cumsum(tpos).astype(np.int32), rows[order].astype(np.int32), np.asarray(vals)[order]
+
+
+def spgemm_outer(A, B, method="hash"):
+    """Outer-product C = A*B with A passed as DCSC and B as DCSR (the reference's
+    DCSC_DCSR_* entry points). method: 'hash', 'bucket' or 'coord'."""
+    L = lib()
+    ap, ac, av, an, am = A
+    bp, bc, bv, bn, bm = B
+    tp, tc, tv = _csr_transpose_np(ap, ac, av, an, am)
+    At = taco.dcsc(tp, tc, tv, an, am)
+    Bt = taco.dcsr(bp, bc, bv, bn, bm)
+    Ct = taco.init_dc(an, bm)
+    fn = {"hash": L.spws_dcsc_dcsr_hash_compute, "bucket": L.spws_dcsc_dcsr_bucket_compute,
+          "coord": L.spws_dcsc_dcsr_coord_compute}[method]
+    check(fn(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
+    return taco.take_csr(Ct, an, L.spws_free)
+
+
+def spgemm_t(A, B):
+    """C^T = (A*B)^T with A passed as CSC and B as CSR (CSC_CSR_T_hash).
+    Returns ((pos, crd, vals) of C^T, collisions)."""
+    L = lib()
+    ap, ac, av, an, am = A
+    bp, bc, bv, bn, bm = B
+    tp, tc, tv = _csr_transpose_np(ap, ac, av, an, am)
+    At = taco.csc(tp, tc, tv, an, am)
+    Bt = taco.csr(bp, bc, bv, bn, bm)
+    Ct = taco.init_dc(bm, an)
+    coll = C.c_int32(0)
+    check(L.spws_csc_csr_t_hash_compute(Ct.ptr(), At.ptr(), Bt.ptr(), 0, C.byref(coll)))
+    return taco.take_csr(Ct, bm, L.spws_free), int(coll.value)
+
+
+def mttkrp(Bcoo, dims, Cf, Df, method="bucket"):
+    """A(i,j) = sum_{k,l} B(k,l,i) C(k,j) D(l,j) through the TACO C entry point.
+    Bcoo: (c0, c1, c2, vals) in CSF level order (k, l, i) with dims; Cf, Df:
+    CSR tuples of the factors (passed as DCSR). Returns ([i, j], vals)."""
+    L = lib()
+    B = taco.csf3_from_coo(*Bcoo, dims)
+    Ct = taco.dcsr(*Cf)
+    Dt = taco.dcsr(*Df)
+    A = taco.init_coo((dims[2], Cf[4]))
+    fn = L.spws_coo_csf_dcsr_dcsr_hash_compute if method == "hash" else L.spws_coo_csf_dcsr_dcsr_bucket_compute
+    check(fn(A.ptr(), B.ptr(), Ct.ptr(), Dt.ptr(), 0))
+    return taco.take_coo(A, 2, L.spws_free)
+
+
+def ttm(Bcoo, dims, Cf, method="bucket"):
+    """A(k,j,l) = sum_i B(k,i,j) C(i,l) through the TACO C entry point.
+    Bcoo in CSF level order (k, i, j). Returns ([k, j, l], vals)."""
+    L = lib()
+    B = taco.csf3_from_coo(*Bcoo, dims)
+    Ct = taco.dcsr(*Cf)
+    A = taco.init_coo((dims[0], dims[2], Cf[4]))
+    fn = L.spws_coo_csf_dcsr_hash_compute if method == "hash" else L.spws_coo_csf_dcsr_bucket_compute
+    check(fn(A.ptr(), B.ptr(), Ct.ptr(), 0))
+    return taco.take_coo(A, 3, L.spws_free)
 
 
 class DeviceCsr:

@@ -8,11 +8,12 @@
 #include <cstring>
 #include <string>
 
+#include "abi_util.h"
 #include "spws_internal.h"
 #include "validate.h"
 
 namespace spws {
-namespace {
+namespace abi {
 
 // ---- host-side structural checks (content is validated on the device) ----
 
@@ -47,17 +48,6 @@ int check_out_dc(taco_tensor_t* C, const char* what) {
   }
   return SPWS_OK;
 }
-
-// Owns device copies of one CSR operand.
-struct DevCsr {
-  spws_csr_dev m{};
-  cudaStream_t s = nullptr;
-  ~DevCsr() {
-    dfree(m.pos, s);
-    dfree(m.crd, s);
-    dfree(m.vals, s);
-  }
-};
 
 int upload(const int32_t* pos, const int32_t* crd, const double* vals, int32_t nrows, int32_t ncols, int64_t nnz,
            const char* what, DevCsr* out, cudaStream_t s) {
@@ -165,28 +155,12 @@ void free_csr_out(taco_tensor_t* C) {
   C->indices[1][1] = nullptr;
 }
 
-// The reference timing wrappers (e.g. CSR_CSR_hash_sequential.h:355-382):
-// `warmup` untimed calls, then `repeat` timed calls; with bench=true every
-// output but the last is freed. Returns seconds per repeat, or -1 on error.
-template <typename F>
-double timed(taco_tensor_t* C, int32_t warmup, int32_t repeat, bool bench, F&& call) {
-  for (int i = 0; i < warmup; i++) {
-    if (call() != SPWS_OK) return -1.0;
-    if (bench) free_csr_out(C);
-  }
-  const double t0 = now_s();
-  for (int i = 0; i < repeat; i++) {
-    if (call() != SPWS_OK) return -1.0;
-    if (bench && i != repeat - 1) free_csr_out(C);
-  }
-  const double t1 = now_s();
-  return repeat > 0 ? (t1 - t0) / repeat : 0.0;
-}
 
-}  // namespace
+}  // namespace abi
 }  // namespace spws
 
 using namespace spws;
+using namespace spws::abi;
 
 extern "C" {
 
@@ -202,13 +176,15 @@ int spws_csr_csr_taco_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t*
 double CSR_CSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
                     int32_t repeat, bool bench, bool print) {
   (void)print;
-  return timed(C, warmup, repeat, bench, [&] { return spws_csr_csr_hash_compute(C, A, B, w_cap); });
+  return timed(warmup, repeat, bench, [&] { return spws_csr_csr_hash_compute(C, A, B, w_cap); },
+               [&] { free_csr_out(C); });
 }
 
 double CSR_CSR_taco(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t warmup, int32_t repeat, bool bench,
                     bool print) {
   (void)print;
-  return timed(C, warmup, repeat, bench, [&] { return spws_csr_csr_taco_compute(C, A, B); });
+  return timed(warmup, repeat, bench, [&] { return spws_csr_csr_taco_compute(C, A, B); },
+               [&] { free_csr_out(C); });
 }
 
 // ---- device-resident API ----

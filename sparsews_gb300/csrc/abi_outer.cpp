@@ -1,0 +1,225 @@
+// C-ABI entry points of the outer-product (DCSC x DCSR), coordinate-workspace
+// and transposed-output SpGEMMs. Operands are brought to CSR on the device
+// (convert.cu) and run through the row-wise pipeline or the coordinate
+// workspace; results are identical in structure to the reference's and summed
+// over j like its loops.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "abi_util.h"
+#include "convert.h"
+#include "spws_internal.h"
+
+namespace spws {
+namespace abi {
+namespace {
+
+// Host structural checks of a compressed-outer ("CC") matrix
+// (utils/dataloader.h:504-537): indices[0][0] = {0, nq}, indices[0][1] the nq
+// outer coordinates, indices[1][0] fiber positions (nq+1), indices[1][1] crd.
+int check_cc(const taco_tensor_t* t, const char* what, int outer_mode, int32_t* nq, int64_t* nnz) {
+  if (!t || t->order != 2 || !t->dimensions || !t->indices || !t->indices[0] || !t->indices[0][0] ||
+      !t->indices[1] || !t->indices[1][0]) {
+    set_error(std::string(what) + ": expected an order-2 tensor with two compressed levels");
+    return SPWS_ERR_INVALID;
+  }
+  if (t->mode_ordering && t->mode_ordering[0] != outer_mode) {
+    set_error(std::string(what) + ": unexpected mode ordering");
+    return SPWS_ERR_INVALID;
+  }
+  if (t->indices[0][0][0] != 0) {
+    set_error(std::string(what) + ": outer level positions must start at 0");
+    return SPWS_ERR_INVALID;
+  }
+  *nq = t->indices[0][0][1];
+  if (*nq < 0 || (*nq > 0 && !t->indices[0][1])) {
+    set_error(std::string(what) + ": missing outer coordinates");
+    return SPWS_ERR_INVALID;
+  }
+  *nnz = t->indices[1][0][*nq];
+  if (*nnz < 0 || (*nnz > 0 && (!t->indices[1][1] || !t->vals))) {
+    set_error(std::string(what) + ": missing crd/vals arrays");
+    return SPWS_ERR_INVALID;
+  }
+  return SPWS_OK;
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  ~DevBuf() { dfree(p, s); }
+};
+
+template <typename T>
+int up(const T* h, size_t n, DevBuf* b, cudaStream_t s) {
+  b->s = s;
+  SPWS_TRY(dalloc(&b->p, sizeof(T) * (n ? n : 1), s));
+  if (n) SPWS_CUDA(cudaMemcpyAsync(b->p, h, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+  return SPWS_OK;
+}
+
+// Uploads a CC matrix, validates it on the device and converts it to CSR.
+// outer_mode 1 = DCSC (outer level over columns), 0 = DCSR.
+int cc_to_dev_csr(const taco_tensor_t* t, const char* what, int outer_mode, DevCsr* out, cudaStream_t s) {
+  int32_t nq;
+  int64_t nnz;
+  SPWS_TRY(check_cc(t, what, outer_mode, &nq, &nnz));
+  const int32_t nrows = t->dimensions[0], ncols = t->dimensions[1];
+  if (nrows < 0 || ncols < 0) {
+    set_error(std::string(what) + ": negative dimension");
+    return SPWS_ERR_INVALID;
+  }
+  const int32_t outer_dim = outer_mode == 1 ? ncols : nrows;
+  const int32_t inner_dim = outer_mode == 1 ? nrows : ncols;
+  DevBuf oc, pos, ic, vals;
+  SPWS_TRY(up(t->indices[0][1], (size_t)nq, &oc, s));
+  SPWS_TRY(up(t->indices[1][0], (size_t)nq + 1, &pos, s));
+  SPWS_TRY(up(t->indices[1][1], (size_t)nnz, &ic, s));
+  SPWS_TRY(up(t->vals, (size_t)nnz, &vals, s));
+  SPWS_TRY(validate_cc_device((int32_t*)oc.p, (int32_t*)pos.p, (int32_t*)ic.p, nq, outer_dim, inner_dim, nnz, what,
+                              s));
+  out->s = s;
+  if (outer_mode == 1)
+    return dcsc_to_csr((int32_t*)oc.p, (int32_t*)pos.p, (int32_t*)ic.p, (double*)vals.p, nq, nrows, ncols, nnz,
+                       &out->m, s);
+  return dcsr_to_csr((int32_t*)oc.p, (int32_t*)pos.p, (int32_t*)ic.p, (double*)vals.p, nq, nrows, ncols, nnz, &out->m,
+                     s);
+}
+
+enum class Engine { Rowwise, Coord };
+
+int run_into(taco_tensor_t* C, const CsrView& A, const CsrView& B, Engine eng, spws_spgemm_stats* st,
+             cudaStream_t s) {
+  spws_csr_dev r{};
+  int rc;
+  if (eng == Engine::Coord) {
+    rc = spgemm_coord(A, B, &r, st, s);
+  } else {
+    SpgemmOpts opt;
+    rc = spgemm_rowwise(A, B, &r, opt, st, s);
+  }
+  if (rc == SPWS_OK) rc = download_into(C, r, s);
+  release(&r, s);
+  return rc;
+}
+
+// Outer product C = A*B with A in DCSC and B in DCSR.
+int dcsc_dcsr(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, Engine eng) {
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  SPWS_TRY(check_out_dc(C, "C"));
+  cudaStream_t s = ds->stream;
+  DevCsr dA, dB;
+  SPWS_TRY(cc_to_dev_csr(A, "A", 1, &dA, s));
+  SPWS_TRY(cc_to_dev_csr(B, "B", 0, &dB, s));
+  if (dA.m.ncols != dB.m.nrows || C->dimensions[0] != dA.m.nrows) {
+    set_error("shape mismatch: A is n x m, B must be m x k and C n x k");
+    return SPWS_ERR_INVALID;
+  }
+  return run_into(C, view(dA.m), view(dB.m), eng, nullptr, s);
+}
+
+}  // namespace
+}  // namespace abi
+}  // namespace spws
+
+using namespace spws;
+using namespace spws::abi;
+
+extern "C" {
+
+int spws_dcsc_dcsr_hash_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  (void)w_cap;
+  return dcsc_dcsr(C, A, B, Engine::Rowwise);
+}
+
+int spws_dcsc_dcsr_bucket_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  (void)w_cap;
+  return dcsc_dcsr(C, A, B, Engine::Rowwise);
+}
+
+int spws_dcsc_dcsr_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  (void)w_cap;
+  return dcsc_dcsr(C, A, B, Engine::Coord);
+}
+
+double DCSC_DCSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                      int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_dcsc_dcsr_hash_compute(C, A, B, w_cap); },
+               [&] { free_csr_out(C); });
+}
+
+double DCSC_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                        int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_dcsc_dcsr_bucket_compute(C, A, B, w_cap); },
+               [&] { free_csr_out(C); });
+}
+
+void DCSC_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print) {
+  (void)print;
+  spws_dcsc_dcsr_coord_compute(C, A, B, w_cap);
+}
+
+int spws_csr_csr_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  (void)w_cap;
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  int32_t an, am, bn, bm;
+  int64_t annz, bnnz;
+  SPWS_TRY(check_dc(A, "A", 0, &an, &am, &annz));
+  SPWS_TRY(check_dc(B, "B", 0, &bn, &bm, &bnnz));
+  SPWS_TRY(check_out_dc(C, "C"));
+  if (am != bn) {
+    set_error("A's column count must equal B's row count");
+    return SPWS_ERR_INVALID;
+  }
+  cudaStream_t s = ds->stream;
+  DevCsr dA, dB;
+  SPWS_TRY(upload(A->indices[1][0], A->indices[1][1], A->vals, an, am, annz, "A", &dA, s));
+  SPWS_TRY(upload(B->indices[1][0], B->indices[1][1], B->vals, bn, bm, bnnz, "B", &dB, s));
+  return run_into(C, view(dA.m), view(dB.m), Engine::Coord, nullptr, s);
+}
+
+// C = (A*B)^T with A in CSC (dense outer level over j) and B in CSR, computed
+// as B^T * A^T row by row: the rows of the result are indexed by k, the key
+// the reference swaps in (evaluate/CSC_CSR_T_hash_record.h:275,278). The
+// CSC arrays of A are the CSR arrays of A^T; B^T is built on the device.
+int spws_csc_csr_t_hash_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap,
+                                int32_t* collisions) {
+  (void)w_cap;
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  int32_t aj, ai, bn, bm;
+  int64_t annz, bnnz;
+  SPWS_TRY(check_dc(A, "A", 1, &aj, &ai, &annz));  // outer = columns j, inner = rows i
+  SPWS_TRY(check_dc(B, "B", 0, &bn, &bm, &bnnz));
+  SPWS_TRY(check_out_dc(C, "C"));
+  if (aj != bn || C->dimensions[0] != bm) {
+    set_error("shape mismatch: A is i x j (CSC), B j x k, C must have k rows");
+    return SPWS_ERR_INVALID;
+  }
+  cudaStream_t s = ds->stream;
+  DevCsr dAt, dB, dBt;
+  SPWS_TRY(upload(A->indices[1][0], A->indices[1][1], A->vals, aj, ai, annz, "A", &dAt, s));
+  SPWS_TRY(upload(B->indices[1][0], B->indices[1][1], B->vals, bn, bm, bnnz, "B", &dB, s));
+  dBt.s = s;
+  SPWS_TRY(csr_transpose(view(dB.m), &dBt.m, s));
+  spws_spgemm_stats st{};
+  SPWS_TRY(run_into(C, view(dBt.m), view(dAt.m), Engine::Rowwise, &st, s));
+  if (collisions) *collisions = (int32_t)(st.products - st.nnz);
+  return SPWS_OK;
+}
+
+double CSC_CSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t* collisions) {
+  const double t0 = now_s();
+  if (spws_csc_csr_t_hash_compute(C, A, B, w_cap, collisions) != SPWS_OK) return -1.0;
+  return now_s() - t0;
+}
+
+}  // extern "C"

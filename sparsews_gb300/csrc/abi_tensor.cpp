@@ -1,0 +1,280 @@
+// C-ABI entry points of MTTKRP and TTM (hash, bucket and coordinate names of
+// the reference all map to the bucket kernel of tensor.cu; they return the
+// same sorted COO).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "abi_util.h"
+#include "convert.h"
+#include "spws_internal.h"
+#include "tensor.h"
+#include "validate.h"
+
+namespace spws {
+namespace abi {
+namespace {
+
+struct Buf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  ~Buf() { dfree(p, s); }
+};
+
+template <typename T>
+int up(const T* h, size_t n, Buf* b, cudaStream_t s) {
+  b->s = s;
+  SPWS_TRY(dalloc(&b->p, sizeof(T) * (n ? n : 1), s));
+  if (n) SPWS_CUDA(cudaMemcpyAsync(b->p, h, sizeof(T) * n, cudaMemcpyHostToDevice, s));
+  return SPWS_OK;
+}
+
+// CSF of order 3 as read_tns_csf builds it (utils/dataloader.h:636-724).
+struct CsfUp {
+  Buf roots, pos1, crd1, pos2, crd2, vals;
+  Csf3Dev d;
+};
+
+int upload_csf(const taco_tensor_t* t, CsfUp* u, cudaStream_t s) {
+  if (!t || t->order != 3 || !t->dimensions || !t->indices || !t->indices[0] || !t->indices[1] || !t->indices[2] ||
+      !t->indices[0][0] || !t->indices[1][0] || !t->indices[2][0]) {
+    set_error("B: expected an order-3 CSF tensor");
+    return SPWS_ERR_INVALID;
+  }
+  Csf3Dev& d = u->d;
+  d.d0 = t->dimensions[0];
+  d.d1 = t->dimensions[1];
+  d.d2 = t->dimensions[2];
+  if (d.d0 < 0 || d.d1 < 0 || d.d2 < 0 || t->indices[0][0][0] != 0) {
+    set_error("B: bad dimensions or root positions");
+    return SPWS_ERR_INVALID;
+  }
+  d.nk = t->indices[0][0][1];
+  if (d.nk < 0 || (d.nk > 0 && !t->indices[0][1])) {
+    set_error("B: missing root coordinates");
+    return SPWS_ERR_INVALID;
+  }
+  d.nf = t->indices[1][0][d.nk];
+  if (d.nf < 0 || (d.nf > 0 && !t->indices[1][1])) {
+    set_error("B: missing level-1 coordinates");
+    return SPWS_ERR_INVALID;
+  }
+  d.nnz = t->indices[2][0][d.nf];
+  if (d.nnz < 0 || (d.nnz > 0 && (!t->indices[2][1] || !t->vals))) {
+    set_error("B: missing leaf coordinates or values");
+    return SPWS_ERR_INVALID;
+  }
+  SPWS_TRY(up(t->indices[0][1], (size_t)d.nk, &u->roots, s));
+  SPWS_TRY(up(t->indices[1][0], (size_t)d.nk + 1, &u->pos1, s));
+  SPWS_TRY(up(t->indices[1][1], (size_t)d.nf, &u->crd1, s));
+  SPWS_TRY(up(t->indices[2][0], (size_t)d.nf + 1, &u->pos2, s));
+  SPWS_TRY(up(t->indices[2][1], (size_t)d.nnz, &u->crd2, s));
+  SPWS_TRY(up(t->vals, (size_t)d.nnz, &u->vals, s));
+  d.roots = (int32_t*)u->roots.p;
+  d.pos1 = (int32_t*)u->pos1.p;
+  d.crd1 = (int32_t*)u->crd1.p;
+  d.pos2 = (int32_t*)u->pos2.p;
+  d.crd2 = (int32_t*)u->crd2.p;
+  d.vals = (double*)u->vals.p;
+  // roots + level 1 form a compressed-outer matrix; level 2 is a CSR over fibers
+  SPWS_TRY(validate_cc_device(d.roots, d.pos1, d.crd1, d.nk, d.d0, d.d1, d.nf, "B levels 0-1", s));
+  SPWS_TRY(validate_csr_device(d.pos2, d.crd2, d.nf, d.d2, d.nnz, "B level 2", s));
+  return SPWS_OK;
+}
+
+// DCSR factor (CC_to_taco_tensor with ordering {0,1}) -> dense rows + mask.
+int upload_factor(const taco_tensor_t* t, const char* what, FactorDense* out, cudaStream_t s) {
+  if (!t || t->order != 2 || !t->dimensions || !t->indices || !t->indices[0] || !t->indices[0][0] ||
+      !t->indices[1] || !t->indices[1][0] || t->indices[0][0][0] != 0) {
+    set_error(std::string(what) + ": expected a DCSR matrix");
+    return SPWS_ERR_INVALID;
+  }
+  DcsrDev f;
+  f.nrows = t->dimensions[0];
+  f.ncols = t->dimensions[1];
+  f.nq = t->indices[0][0][1];
+  if (f.nrows < 0 || f.ncols < 0 || f.nq < 0 || (f.nq > 0 && !t->indices[0][1])) {
+    set_error(std::string(what) + ": bad DCSR sizes");
+    return SPWS_ERR_INVALID;
+  }
+  f.nnz = t->indices[1][0][f.nq];
+  if (f.nnz < 0 || (f.nnz > 0 && (!t->indices[1][1] || !t->vals))) {
+    set_error(std::string(what) + ": missing crd/vals");
+    return SPWS_ERR_INVALID;
+  }
+  Buf oc, pos, ic, vals;
+  SPWS_TRY(up(t->indices[0][1], (size_t)f.nq, &oc, s));
+  SPWS_TRY(up(t->indices[1][0], (size_t)f.nq + 1, &pos, s));
+  SPWS_TRY(up(t->indices[1][1], (size_t)f.nnz, &ic, s));
+  SPWS_TRY(up(t->vals, (size_t)f.nnz, &vals, s));
+  f.oc = (int32_t*)oc.p;
+  f.pos = (int32_t*)pos.p;
+  f.ic = (int32_t*)ic.p;
+  f.vals = (double*)vals.p;
+  SPWS_TRY(validate_cc_device(f.oc, f.pos, f.ic, f.nq, f.nrows, f.ncols, f.nnz, what, s));
+  return densify_factor(f, out, s);
+}
+
+int check_out_coo(taco_tensor_t* A, int order) {
+  if (!A || !A->indices) {
+    set_error("A: output must be initialised like init_taco_tensor_COO");
+    return SPWS_ERR_INVALID;
+  }
+  for (int m = 1; m <= order; m++)
+    if (!A->indices[m]) {
+      set_error("A: output must be initialised like init_taco_tensor_COO");
+      return SPWS_ERR_INVALID;
+    }
+  return SPWS_OK;
+}
+
+// Device COO -> malloc'd host arrays in A->indices[m+1][0] and A->vals.
+int download_coo(taco_tensor_t* A, CooOut& o, int order, cudaStream_t s) {
+  const size_t n = (size_t)o.n;
+  int32_t* c[3] = {nullptr, nullptr, nullptr};
+  double* v = (double*)malloc(sizeof(double) * std::max<size_t>(n, 1));
+  bool ok = v != nullptr;
+  for (int d = 0; d < order; d++) {
+    c[d] = (int32_t*)malloc(sizeof(int32_t) * std::max<size_t>(n, 1));
+    ok = ok && c[d];
+  }
+  cudaError_t e = cudaSuccess;
+  if (ok && n) {
+    for (int d = 0; d < order && e == cudaSuccess; d++)
+      e = cudaMemcpyAsync(c[d], o.crd[d], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v, o.vals, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  for (int d = 0; d < 3; d++) dfree(o.crd[d], s);
+  dfree(o.vals, s);
+  if (!ok || e != cudaSuccess) {
+    (void)cudaGetLastError();
+    free(v);
+    for (int d = 0; d < order; d++) free(c[d]);
+    set_error(ok ? std::string("copying the output failed: ") + cudaGetErrorString(e)
+                 : std::string("host allocation of the output failed"));
+    return ok ? SPWS_ERR_CUDA : SPWS_ERR_NOMEM;
+  }
+  for (int d = 0; d < order; d++) A->indices[d + 1][0] = c[d];
+  A->vals = v;
+  A->vals_size = (int32_t)o.n;
+  return SPWS_OK;
+}
+
+int mttkrp(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* Cf, taco_tensor_t* Df) {
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  cudaStream_t s = ds->stream;
+  SPWS_TRY(check_out_coo(A, 2));
+  CsfUp b;
+  SPWS_TRY(upload_csf(B, &b, s));
+  FactorDense c, d;
+  int rc = upload_factor(Cf, "C", &c, s);
+  if (rc == SPWS_OK) rc = upload_factor(Df, "D", &d, s);
+  CooOut o;
+  if (rc == SPWS_OK) rc = tensor_bucket(0, b.d, c, &d, &o, s);
+  free_factor(&c, s);
+  free_factor(&d, s);
+  if (rc == SPWS_OK) rc = download_coo(A, o, 2, s);
+  return rc;
+}
+
+int ttm(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* Cf) {
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  cudaStream_t s = ds->stream;
+  SPWS_TRY(check_out_coo(A, 3));
+  CsfUp b;
+  SPWS_TRY(upload_csf(B, &b, s));
+  FactorDense c;
+  int rc = upload_factor(Cf, "C", &c, s);
+  CooOut o;
+  if (rc == SPWS_OK) rc = tensor_bucket(1, b.d, c, nullptr, &o, s);
+  free_factor(&c, s);
+  if (rc == SPWS_OK) rc = download_coo(A, o, 3, s);
+  return rc;
+}
+
+void free_coo_out(taco_tensor_t* A, int order) {
+  free(A->vals);
+  A->vals = nullptr;
+  for (int d = 1; d <= order; d++) {
+    free(A->indices[d][0]);
+    A->indices[d][0] = nullptr;
+  }
+}
+
+}  // namespace
+}  // namespace abi
+}  // namespace spws
+
+using namespace spws;
+using namespace spws::abi;
+
+extern "C" {
+
+int spws_coo_csf_dcsr_dcsr_hash_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D,
+                                        int32_t w_cap) {
+  (void)w_cap;
+  return mttkrp(A, B, C, D);
+}
+
+int spws_coo_csf_dcsr_dcsr_bucket_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D,
+                                          int32_t w_cap) {
+  (void)w_cap;
+  return mttkrp(A, B, C, D);
+}
+
+double COO_CSF_DCSR_DCSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D, int32_t w_cap,
+                              int32_t warmup, int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_coo_csf_dcsr_dcsr_hash_compute(A, B, C, D, w_cap); },
+               [&] { free_coo_out(A, 2); });
+}
+
+double COO_CSF_DCSR_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D, int32_t w_cap,
+                                int32_t warmup, int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_coo_csf_dcsr_dcsr_bucket_compute(A, B, C, D, w_cap); },
+               [&] { free_coo_out(A, 2); });
+}
+
+void COO_CSF_DCSR_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D, int32_t w_cap,
+                             bool print) {
+  (void)print;
+  spws_coo_csf_dcsr_dcsr_bucket_compute(A, B, C, D, w_cap);
+}
+
+int spws_coo_csf_dcsr_hash_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap) {
+  (void)w_cap;
+  return ttm(A, B, C);
+}
+
+int spws_coo_csf_dcsr_bucket_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap) {
+  (void)w_cap;
+  return ttm(A, B, C);
+}
+
+double COO_CSF_DCSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                         int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_coo_csf_dcsr_hash_compute(A, B, C, w_cap); },
+               [&] { free_coo_out(A, 3); });
+}
+
+double COO_CSF_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                           int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_coo_csf_dcsr_bucket_compute(A, B, C, w_cap); },
+               [&] { free_coo_out(A, 3); });
+}
+
+void COO_CSF_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print) {
+  (void)print;
+  spws_coo_csf_dcsr_bucket_compute(A, B, C, w_cap);
+}
+
+}  // extern "C"

@@ -1,0 +1,242 @@
+// Format conversions between the TACO level formats the reference's entry
+// points take (utils/dataloader.h: DC_to_taco_tensor, CC_to_taco_tensor and
+// CSF) and the CSR the row-wise kernels consume, plus their device-side
+// validation. All conversions run on the device; sorts are the stable radix
+// sort of sort.cu, so entries keep their order within a row.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <string>
+
+#include "convert.h"
+#include "sort.h"
+#include "spws_internal.h"
+
+namespace spws {
+namespace {
+
+int bits_for(unsigned long long max_key_exclusive) {
+  int b = 0;
+  while (b < 64 && (1ull << b) < max_key_exclusive) b++;
+  return b;
+}
+
+// Compressed-outer validation: the outer coordinate list strictly increasing
+// in [0, outer_dim), the fiber positions monotone inside [0, nnz], and each
+// fiber's inner coordinates strictly increasing in [0, inner_dim).
+__global__ void k_validate_cc(int32_t nq, int32_t outer_dim, int32_t inner_dim, int64_t nnz,
+                              const int32_t* __restrict__ oc, const int32_t* __restrict__ pos,
+                              const int32_t* __restrict__ ic, int* __restrict__ bad) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const int32_t o = oc[q];
+  if (o < 0 || o >= outer_dim || (q > 0 && oc[q - 1] >= o)) {
+    atomicExch(bad, 1);
+    return;
+  }
+  const int32_t s = pos[q], e = pos[q + 1];
+  if (s < 0 || e < s || (int64_t)e > nnz) {
+    atomicExch(bad, 1);
+    return;
+  }
+  int prev = -1;
+  for (int32_t p = s; p < e; p++) {
+    const int k = ic[p];
+    if (k <= prev || k >= inner_dim) {
+      atomicExch(bad, 1);
+      return;
+    }
+    prev = k;
+  }
+}
+
+// keys[p] = row(p) * ncols + col(p) for a compressed-outer matrix whose outer
+// coordinates are columns (DCSC): row = inner crd, col = outer coordinate.
+__global__ void k_cc_transposed_keys(int32_t nq, const int32_t* __restrict__ oc, const int32_t* __restrict__ pos,
+                                     const int32_t* __restrict__ ic, const double* __restrict__ vals, int32_t ncols,
+                                     unsigned long long* __restrict__ keys, unsigned long long* __restrict__ pay) {
+  const int lane = threadIdx.x & 31;
+  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= nq) return;
+  const int32_t col = oc[q];
+  for (int32_t p = pos[q] + lane; p < pos[q + 1]; p += 32) {
+    keys[p] = (unsigned long long)ic[p] * (unsigned long long)ncols + (unsigned long long)col;
+    pay[p] = __double_as_longlong(vals[p]);
+  }
+}
+
+// keys[p] = col(p) * nrows + row(p) for a CSR (its transpose order).
+__global__ void k_csr_transposed_keys(int32_t nrows, const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+                                      const double* __restrict__ vals, unsigned long long* __restrict__ keys,
+                                      unsigned long long* __restrict__ pay) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= nrows) return;
+  for (int32_t p = pos[i] + lane; p < pos[i + 1]; p += 32) {
+    keys[p] = (unsigned long long)crd[p] * (unsigned long long)nrows + (unsigned long long)i;
+    pay[p] = __double_as_longlong(vals[p]);
+  }
+}
+
+// Sorted (major * minor_dim + minor) keys -> CSR crd/vals and major counts.
+__global__ void k_keys_to_csr(int64_t n, const unsigned long long* __restrict__ keys,
+                              const unsigned long long* __restrict__ pay, int32_t minor_dim, int32_t* __restrict__ crd,
+                              double* __restrict__ vals, int32_t* __restrict__ counts) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const unsigned long long k = keys[p];
+  const int32_t major = (int32_t)(k / (unsigned long long)minor_dim);
+  crd[p] = (int32_t)(k % (unsigned long long)minor_dim);
+  vals[p] = __longlong_as_double((long long)pay[p]);
+  atomicAdd(&counts[major], 1);
+}
+
+// counts[outer coordinate] = fiber length, for expanding a compressed outer level.
+__global__ void k_cc_counts(int32_t nq, const int32_t* __restrict__ oc, const int32_t* __restrict__ pos,
+                            int32_t* __restrict__ counts) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  counts[oc[q]] = pos[q + 1] - pos[q];
+}
+
+int keys_to_csr(int64_t nnz, unsigned long long* keys, unsigned long long* pay, unsigned long long* ktmp,
+                unsigned long long* ptmp, int key_bits, int32_t nmajor, int32_t nminor, spws_csr_dev* out,
+                cudaStream_t s) {
+  bool in_tmp = false;
+  SPWS_TRY(radix_sort_pairs(keys, pay, ktmp, ptmp, nnz, key_bits, &in_tmp, s));
+  const unsigned long long* k = in_tmp ? ktmp : keys;
+  const unsigned long long* v = in_tmp ? ptmp : pay;
+  int32_t* counts = nullptr;
+  SPWS_TRY(dalloc((void**)&counts, sizeof(int32_t) * std::max<int64_t>(nmajor, 1), s));
+  SPWS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * std::max<int64_t>(nmajor, 1), s));
+  if (nnz > 0) {
+    k_keys_to_csr<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, k, v, nminor, out->crd, out->vals, counts);
+    count_launch(1);
+  }
+  long long* tot = nullptr;
+  SPWS_TRY(dalloc((void**)&tot, sizeof(long long), s));
+  SPWS_TRY(scan_counts_i32(counts, out->pos, nmajor, tot, s));
+  SPWS_CUDA(cudaGetLastError());
+  dfree(tot, s);
+  dfree(counts, s);
+  return SPWS_OK;
+}
+
+}  // namespace
+
+int validate_cc_device(const int32_t* oc, const int32_t* pos, const int32_t* ic, int32_t nq, int32_t outer_dim,
+                       int32_t inner_dim, int64_t nnz, const char* what, cudaStream_t s) {
+  if (nq < 0 || nq > outer_dim || nnz < 0 || nnz > INT32_MAX || outer_dim < 0 || inner_dim < 0) {
+    set_error(std::string(what) + ": bad compressed level sizes");
+    return SPWS_ERR_INVALID;
+  }
+  int32_t ends[2] = {0, 0};
+  SPWS_CUDA(cudaMemcpyAsync(&ends[0], pos, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&ends[1], pos + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  int* bad = nullptr;
+  SPWS_TRY(dalloc((void**)&bad, sizeof(int), s));
+  SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  if (nq > 0) {
+    k_validate_cc<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(nq, outer_dim, inner_dim, nnz, oc, pos, ic, bad);
+    count_launch(1);
+    SPWS_CUDA(cudaGetLastError());
+  }
+  int hbad = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  dfree(bad, s);
+  if (ends[0] != 0 || (int64_t)ends[1] != nnz) {
+    set_error(std::string(what) + ": fiber positions must start at 0 and end at nnz");
+    return SPWS_ERR_INVALID;
+  }
+  if (hbad) {
+    set_error(std::string(what) + ": coordinates out of range or not strictly increasing");
+    return SPWS_ERR_INVALID;
+  }
+  return SPWS_OK;
+}
+
+int dcsc_to_csr(const int32_t* oc, const int32_t* pos, const int32_t* ic, const double* vals, int32_t nq, int32_t nrows,
+                int32_t ncols, int64_t nnz, spws_csr_dev* out, cudaStream_t s) {
+  out->nrows = nrows;
+  out->ncols = ncols;
+  out->nnz = nnz;
+  SPWS_TRY(dalloc((void**)&out->pos, sizeof(int32_t) * ((size_t)nrows + 1), s));
+  SPWS_TRY(dalloc((void**)&out->crd, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max<int64_t>(nnz, 1), s));
+  unsigned long long *k = nullptr, *p = nullptr, *kt = nullptr, *pt = nullptr;
+  const size_t b = sizeof(unsigned long long) * (size_t)std::max<int64_t>(nnz, 1);
+  SPWS_TRY(dalloc((void**)&k, b, s));
+  SPWS_TRY(dalloc((void**)&p, b, s));
+  SPWS_TRY(dalloc((void**)&kt, b, s));
+  SPWS_TRY(dalloc((void**)&pt, b, s));
+  if (nq > 0) {
+    k_cc_transposed_keys<<<(unsigned)((nq + 7) / 8), 256, 0, s>>>(nq, oc, pos, ic, vals, ncols, k, p);
+    count_launch(1);
+  }
+  const int bits = bits_for((unsigned long long)std::max(nrows, 1) * (unsigned long long)std::max(ncols, 1));
+  int rc = keys_to_csr(nnz, k, p, kt, pt, bits, nrows, ncols, out, s);
+  dfree(k, s);
+  dfree(p, s);
+  dfree(kt, s);
+  dfree(pt, s);
+  return rc;
+}
+
+int dcsr_to_csr(const int32_t* oc, const int32_t* pos, const int32_t* ic, const double* vals, int32_t nq, int32_t nrows,
+                int32_t ncols, int64_t nnz, spws_csr_dev* out, cudaStream_t s) {
+  out->nrows = nrows;
+  out->ncols = ncols;
+  out->nnz = nnz;
+  SPWS_TRY(dalloc((void**)&out->pos, sizeof(int32_t) * ((size_t)nrows + 1), s));
+  SPWS_TRY(dalloc((void**)&out->crd, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max<int64_t>(nnz, 1), s));
+  if (nnz > 0) {
+    SPWS_CUDA(cudaMemcpyAsync(out->crd, ic, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToDevice, s));
+    SPWS_CUDA(cudaMemcpyAsync(out->vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyDeviceToDevice, s));
+  }
+  int32_t* counts = nullptr;
+  SPWS_TRY(dalloc((void**)&counts, sizeof(int32_t) * std::max<int64_t>(nrows, 1), s));
+  SPWS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * std::max<int64_t>(nrows, 1), s));
+  if (nq > 0) {
+    k_cc_counts<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(nq, oc, pos, counts);
+    count_launch(1);
+  }
+  long long* tot = nullptr;
+  SPWS_TRY(dalloc((void**)&tot, sizeof(long long), s));
+  SPWS_TRY(scan_counts_i32(counts, out->pos, nrows, tot, s));
+  SPWS_CUDA(cudaGetLastError());
+  dfree(tot, s);
+  dfree(counts, s);
+  return SPWS_OK;
+}
+
+int csr_transpose(const CsrView& m, spws_csr_dev* out, cudaStream_t s) {
+  out->nrows = m.ncols;
+  out->ncols = m.nrows;
+  out->nnz = m.nnz;
+  const int64_t nnz = m.nnz;
+  SPWS_TRY(dalloc((void**)&out->pos, sizeof(int32_t) * ((size_t)m.ncols + 1), s));
+  SPWS_TRY(dalloc((void**)&out->crd, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max<int64_t>(nnz, 1), s));
+  unsigned long long *k = nullptr, *p = nullptr, *kt = nullptr, *pt = nullptr;
+  const size_t b = sizeof(unsigned long long) * (size_t)std::max<int64_t>(nnz, 1);
+  SPWS_TRY(dalloc((void**)&k, b, s));
+  SPWS_TRY(dalloc((void**)&p, b, s));
+  SPWS_TRY(dalloc((void**)&kt, b, s));
+  SPWS_TRY(dalloc((void**)&pt, b, s));
+  if (m.nrows > 0) {
+    k_csr_transposed_keys<<<(unsigned)((m.nrows + 7) / 8), 256, 0, s>>>(m.nrows, m.pos, m.crd, m.vals, k, p);
+    count_launch(1);
+  }
+  const int bits = bits_for((unsigned long long)std::max(m.nrows, 1) * (unsigned long long)std::max(m.ncols, 1));
+  int rc = keys_to_csr(nnz, k, p, kt, pt, bits, m.ncols, m.nrows, out, s);
+  dfree(k, s);
+  dfree(p, s);
+  dfree(kt, s);
+  dfree(pt, s);
+  return rc;
+}
+
+}  // namespace spws

@@ -14,6 +14,8 @@
 namespace spws {
 
 static thread_local std::string g_err;
+static unsigned long long g_launches = 0;  // kernels this library has launched (all threads)
+void count_launch(int n) { __atomic_fetch_add(&g_launches, (unsigned long long)n, __ATOMIC_RELAXED); }
 void set_error(const std::string& msg) { g_err = msg; }
 void clear_error() { g_err.clear(); }
 
@@ -71,26 +73,24 @@ void dfree(void* p, cudaStream_t s) {
 
 namespace {
 
-// Thread per row: 0 <= pos[i] <= pos[i+1] <= nnz, columns in [0, ncols) and
+// Warp per row: 0 <= pos[i] <= pos[i+1] <= nnz, columns in [0, ncols) and
 // strictly increasing within the row. Any violation sets *bad.
 __global__ void k_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int32_t* __restrict__ pos,
                                const int32_t* __restrict__ crd, int* __restrict__ bad) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= n) return;
   const int32_t s = pos[i], e = pos[i + 1];
   if (s < 0 || e < s || (int64_t)e > nnz) {
-    atomicExch(bad, 1);
+    if (lane == 0) atomicExch(bad, 1);
     return;
   }
-  int prev = -1;
-  for (int32_t p = s; p < e; p++) {
+  bool ok = true;
+  for (int32_t p = s + lane; p < e; p += 32) {
     const int k = crd[p];
-    if (k <= prev || k >= ncols) {
-      atomicExch(bad, 1);
-      return;
-    }
-    prev = k;
+    ok &= k >= 0 && k < ncols && (p == s || crd[p - 1] < k);
   }
+  if (!__all_sync(0xffffffffu, ok) && lane == 0) atomicExch(bad, 1);
 }
 
 }  // namespace
@@ -108,7 +108,8 @@ int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, i
   SPWS_TRY(dalloc((void**)&bad, sizeof(int), s));
   SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (nrows > 0) {
-    k_validate_csr<<<(unsigned)((nrows + 255) / 256), 256, 0, s>>>(nrows, nnz, ncols, pos, crd, bad);
+    k_validate_csr<<<(unsigned)((nrows + 7) / 8), 256, 0, s>>>(nrows, nnz, ncols, pos, crd, bad);
+    count_launch(1);
     SPWS_CUDA(cudaGetLastError());
   }
   int hbad = 0;
@@ -150,6 +151,31 @@ const char* spws_version(void) { return "spws-gb300 0.1 (sm_103a)"; }
 
 void spws_free(void* p) { free(p); }
 
+unsigned long long spws_launch_count(void) { return __atomic_load_n(&spws::g_launches, __ATOMIC_RELAXED); }
+
+int spws_flush_l2(size_t bytes) {
+  spws::DeviceState* ds = nullptr;
+  SPWS_TRY(spws::device_state(&ds));
+  void* p = nullptr;
+  SPWS_TRY(spws::dalloc(&p, bytes, ds->stream));
+  SPWS_CUDA(cudaMemsetAsync(p, 0x5a, bytes, ds->stream));
+  spws::dfree(p, ds->stream);
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
+  return SPWS_OK;
+}
+
+int spws_host_pin(void* p, size_t bytes) {
+  if (!p || !bytes) return SPWS_OK;
+  SPWS_CUDA(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+  return SPWS_OK;
+}
+
+int spws_host_unpin(void* p) {
+  if (!p) return SPWS_OK;
+  SPWS_CUDA(cudaHostUnregister(p));
+  return SPWS_OK;
+}
+
 int spws_device_sync(void) {
   spws::DeviceState* ds = nullptr;
   SPWS_TRY(spws::device_state(&ds));
@@ -158,3 +184,8 @@ int spws_device_sync(void) {
 }
 
 }  // extern "C"
+
+extern "C" int spws_set_device(int device) {
+  SPWS_CUDA(cudaSetDevice(device));
+  return SPWS_OK;
+}

@@ -111,6 +111,7 @@ int scan_counts_i32(const int32_t* counts, int32_t* out, int64_t n, long long* t
   k_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile);
   k_scan_tile_sums<<<1, kScanThreads, 0, s>>>(tile, ntiles, total_dev);
   k_tile_scan<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile, out, total_dev);
+  count_launch(3);
   SPWS_CUDA(cudaGetLastError());
   dfree(tile, s);
   return SPWS_OK;

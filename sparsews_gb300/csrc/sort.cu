@@ -1,0 +1,235 @@
+// Stable LSD radix sort of (uint64 key, 64-bit payload) pairs on the device,
+// and a 64-bit exclusive scan. Used by the coordinate workspace (sort of the
+// expanded (row, col) products, the GPU form of the reference's qsort of its
+// coordinate buffer: DCSC_DCSR_coord_index_chase_flex.h:34-45) and by the
+// format conversions (transposes).
+//
+// One pass per 8-bit digit: per-tile histograms (tile = 4096 items), a scan
+// of the histograms in digit-major order, and a scatter that ranks the items
+// of each 256-item round with warp ballots (a multisplit) so equal digits keep
+// their input order; passes are therefore stable and the sort is stable.
+#include <cuda_runtime.h>
+
+#include "sort.h"
+#include "spws_internal.h"
+
+namespace spws {
+namespace {
+
+constexpr int kRadixBits = 8;
+constexpr int kBins = 1 << kRadixBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kRounds = 16;
+constexpr int kTile = kSortThreads * kRounds;  // 4096
+static_assert(kBins == kSortThreads, "one bin per thread");
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long* __restrict__ keys, int64_t n,
+                                                             int shift, int64_t ntiles, int* __restrict__ hist) {
+  __shared__ int h[kBins];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+#pragma unroll 4
+  for (int r = 0; r < kRounds; r++) {
+    const int64_t idx = base + (int64_t)r * kSortThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(int)((keys[idx] >> shift) & (kBins - 1))], 1);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long* __restrict__ kin,
+                                                                const unsigned long long* __restrict__ vin,
+                                                                unsigned long long* __restrict__ kout,
+                                                                unsigned long long* __restrict__ vout, int64_t n,
+                                                                int shift, int64_t ntiles,
+                                                                const long long* __restrict__ offs) {
+  __shared__ long long base[kBins];
+  __shared__ int wcnt[kSortWarps][kBins];
+  __shared__ int rcnt[kBins];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  base[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+#pragma unroll
+  for (int w = 0; w < kSortWarps; w++) wcnt[w][threadIdx.x] = 0;
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t tile0 = (int64_t)blockIdx.x * kTile;
+  for (int r = 0; r < kRounds; r++) {
+    const int64_t idx = tile0 + (int64_t)r * kSortThreads + threadIdx.x;
+    const bool valid = idx < n;
+    unsigned long long k = 0, v = 0;
+    int d = 0;
+    if (valid) {
+      k = kin[idx];
+      v = vin[idx];
+      d = (int)((k >> shift) & (kBins - 1));
+    }
+    // lanes of this warp holding the same digit
+    unsigned eq = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < kRadixBits; b++) {
+      const bool bit = (d >> b) & 1;
+      const unsigned m = __ballot_sync(0xffffffffu, bit);
+      eq &= bit ? m : ~m;
+    }
+    const int rank = __popc(eq & lt);
+    if (valid && rank == 0) wcnt[warp][d] = __popc(eq);
+    __syncthreads();
+    {  // thread t owns digit t: prefix over warps
+      int run = 0;
+#pragma unroll
+      for (int w = 0; w < kSortWarps; w++) {
+        const int c = wcnt[w][threadIdx.x];
+        wcnt[w][threadIdx.x] = run;
+        run += c;
+      }
+      rcnt[threadIdx.x] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      const long long p = base[d] + wcnt[warp][d] + rank;
+      kout[p] = k;
+      vout[p] = v;
+    }
+    __syncthreads();
+    base[threadIdx.x] += rcnt[threadIdx.x];
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++) wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
+  }
+}
+
+// ---- 64-bit exclusive scan of int32 counts (n may exceed 2^31 in sum) ----
+constexpr int kScanT = 256;
+constexpr int kScanPer = 8;
+constexpr int kScanTile = kScanT * kScanPer;
+
+__device__ __forceinline__ long long warp_incl(long long v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    long long y = __shfl_up_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) >= o) v += y;
+  }
+  return v;
+}
+
+__device__ __forceinline__ long long block_incl(long long v, long long* total) {
+  __shared__ long long ws[kScanT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_incl(v);
+  if (lane == 31) ws[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = lane < kScanT / 32 ? ws[lane] : 0;
+    w = warp_incl(w);
+    if (lane < kScanT / 32) ws[lane] = w;
+  }
+  __syncthreads();
+  if (warp > 0) v += ws[warp - 1];
+  *total = ws[kScanT / 32 - 1];
+  __syncthreads();
+  return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kScanT) k_sum_tiles(const T* __restrict__ in, int64_t n, long long* __restrict__ ts) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  long long s = 0;
+  for (int q = 0; q < kScanPer; q++) {
+    const int64_t idx = base + (int64_t)q * kScanT + threadIdx.x;
+    if (idx < n) s += (long long)in[idx];
+  }
+  long long t;
+  block_incl(s, &t);
+  if (threadIdx.x == 0) ts[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(kScanT) k_scan_sums(long long* __restrict__ ts, int64_t nt, long long* __restrict__ total) {
+  long long carry = 0;
+  for (int64_t b = 0; b < nt; b += kScanT) {
+    const int64_t idx = b + threadIdx.x;
+    const long long v = idx < nt ? ts[idx] : 0;
+    long long t;
+    const long long inc = block_incl(v, &t);
+    if (idx < nt) ts[idx] = carry + inc - v;
+    carry += t;
+  }
+  if (threadIdx.x == 0 && total) *total = carry;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kScanT) k_scan_tiles(const T* __restrict__ in, int64_t n, const long long* __restrict__ ts,
+                                                       long long* __restrict__ out) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
+  long long v[kScanPer];
+  long long s = 0;
+  for (int q = 0; q < kScanPer; q++) {
+    const int64_t idx = base + q;
+    v[q] = idx < n ? (long long)in[idx] : 0;
+    s += v[q];
+  }
+  long long t;
+  const long long inc = block_incl(s, &t);
+  long long run = ts[blockIdx.x] + inc - s;
+  for (int q = 0; q < kScanPer; q++) {
+    const int64_t idx = base + q;
+    if (idx < n) out[idx] = run;
+    run += v[q];
+  }
+}
+
+template <typename T>
+int scan64_impl(const T* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s) {
+  const int64_t nt = (n + kScanTile - 1) / kScanTile;
+  if (nt == 0) {
+    if (total_dev) SPWS_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(long long), s));
+    return SPWS_OK;
+  }
+  long long* ts = nullptr;
+  SPWS_TRY(dalloc((void**)&ts, sizeof(long long) * nt, s));
+  k_sum_tiles<T><<<(unsigned)nt, kScanT, 0, s>>>(in, n, ts);
+  k_scan_sums<<<1, kScanT, 0, s>>>(ts, nt, total_dev);
+  k_scan_tiles<T><<<(unsigned)nt, kScanT, 0, s>>>(in, n, ts, out);
+  count_launch(3);
+  SPWS_CUDA(cudaGetLastError());
+  dfree(ts, s);
+  return SPWS_OK;
+}
+
+}  // namespace
+
+int scan_i32_to_i64(const int32_t* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s) {
+  return scan64_impl<int32_t>(in, out, n, total_dev, s);
+}
+
+int scan_i64(const long long* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s) {
+  return scan64_impl<long long>(in, out, n, total_dev, s);
+}
+
+int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigned long long* keys_tmp,
+                     unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s) {
+  *result_in_tmp = false;
+  if (n <= 1 || key_bits <= 0) return SPWS_OK;
+  const int64_t ntiles = (n + kTile - 1) / kTile;
+  int* hist = nullptr;
+  long long* offs = nullptr;
+  SPWS_TRY(dalloc((void**)&hist, sizeof(int) * kBins * ntiles, s));
+  SPWS_TRY(dalloc((void**)&offs, sizeof(long long) * kBins * ntiles, s));
+  unsigned long long *ka = keys, *va = vals, *kb = keys_tmp, *vb = vals_tmp;
+  for (int shift = 0; shift < key_bits; shift += kRadixBits) {
+    k_radix_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, hist);
+    SPWS_TRY(scan_i32_to_i64(hist, offs, (int64_t)kBins * ntiles, nullptr, s));
+    k_radix_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, offs);
+    count_launch(2);
+    SPWS_CUDA(cudaGetLastError());
+    std::swap(ka, kb);
+    std::swap(va, vb);
+    *result_in_tmp = !*result_in_tmp;
+  }
+  dfree(hist, s);
+  dfree(offs, s);
+  return SPWS_OK;
+}
+
+}  // namespace spws

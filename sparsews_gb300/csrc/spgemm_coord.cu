@@ -1,0 +1,249 @@
+// Coordinate workspace SpGEMM (the reference's
+// benchmark/DCSC_DCSR/DCSC_DCSR_coord_index_chase_flex.h and the
+// seperate/CSR_CSR_4.h prototype): append every product (i, k, a*b) as a
+// coordinate triple, sort the triples by (i, k), and reduce runs of equal
+// coordinates. On the GPU the append is a parallel expansion into a buffer
+// sized exactly by the product count, the sort is the stable device radix
+// sort of 64-bit keys (i_local * ncols + k), and the reduce walks each run in
+// sorted order with one thread. Stability keeps every run in expansion order
+// (ascending j), so each output value is the left-to-right sum over j, the
+// order of the reference's sequential loop.
+//
+// Rows are processed in chunks whose product count fits a fixed buffer
+// budget, so memory is bounded whatever the output size.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <vector>
+
+#include "common.cuh"
+#include "sort.h"
+#include "spws_internal.h"
+
+namespace spws {
+namespace {
+
+constexpr int64_t kChunkProducts = int64_t(1) << 27;  // 134M products = 4.3 GB of pairs + ping-pong
+
+__global__ void k_row_products(int32_t nA, const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
+                               const int32_t* __restrict__ Bp, long long* __restrict__ prods) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nA) return;
+  long long p = 0;
+  for (int32_t q = Ap[w] + lane; q < Ap[w + 1]; q += 32) {
+    const int32_t j = Aj[q];
+    p += Bp[j + 1] - Bp[j];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+  if (lane == 0) prods[w] = p;
+}
+
+// Warp per row of the chunk: writes the row's products in (j, k) order at
+// its offset in the chunk buffer.
+__global__ void k_expand(int32_t r0, int32_t r1, const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
+                         const double* __restrict__ Av, const int32_t* __restrict__ Bp,
+                         const int32_t* __restrict__ Bk, const double* __restrict__ Bv, int32_t ncols,
+                         const long long* __restrict__ poff, unsigned long long* __restrict__ keys,
+                         unsigned long long* __restrict__ vals) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t i = r0 + w;
+  if (i >= r1) return;
+  long long out = poff[i] - poff[r0];
+  const unsigned long long rowkey = (unsigned long long)(i - r0) * (unsigned long long)ncols;
+  for (int32_t qb = Ap[i]; qb < Ap[i + 1]; qb += 32) {
+    Slice sl{0, 0, 0.0};
+    const int32_t q = qb + lane;
+    if (q < Ap[i + 1]) {
+      const int32_t j = Aj[q];
+      sl.s = Bp[j];
+      sl.len = Bp[j + 1] - sl.s;
+      sl.a = Av[q];
+    }
+    const int total = warp_expand_indexed(sl, [&](int f, int32_t p, double a) {
+      keys[out + f] = rowkey + (unsigned long long)Bk[p];
+      vals[out + f] = __double_as_longlong(__dmul_rn(a, Bv[p]));
+    });
+    out += total;
+  }
+}
+
+__global__ void k_heads(int64_t n, const unsigned long long* __restrict__ keys, int32_t* __restrict__ head) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  head[p] = (p == 0 || keys[p] != keys[p - 1]) ? 1 : 0;
+}
+
+__global__ void k_run_starts(int64_t n, const int32_t* __restrict__ head, const long long* __restrict__ hpos,
+                             long long* __restrict__ starts) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  if (head[p]) starts[hpos[p]] = p;
+}
+
+// One thread per run: sum the run left to right, emit (row, col, value).
+__global__ void k_reduce_runs(int64_t nruns, int64_t n, const long long* __restrict__ starts,
+                              const unsigned long long* __restrict__ keys, const unsigned long long* __restrict__ vals,
+                              int32_t ncols, int32_t r0, int32_t* __restrict__ out_crd, double* __restrict__ out_val,
+                              int32_t* __restrict__ rowcnt) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nruns) return;
+  const long long s = starts[r];
+  const long long e = r + 1 < nruns ? starts[r + 1] : n;
+  double v = __longlong_as_double((long long)vals[s]);
+  for (long long q = s + 1; q < e; q++) v = __dadd_rn(v, __longlong_as_double((long long)vals[q]));
+  const unsigned long long k = keys[s];
+  out_crd[r] = (int32_t)(k % (unsigned long long)ncols);
+  out_val[r] = v;
+  atomicAdd(&rowcnt[r0 + (int32_t)(k / (unsigned long long)ncols)], 1);
+}
+
+int bits_for(unsigned long long max_key_exclusive) {
+  int b = 0;
+  while (b < 64 && (1ull << b) < max_key_exclusive) b++;
+  return b;
+}
+
+}  // namespace
+
+int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgemm_stats* stats, cudaStream_t s) {
+  const int32_t nA = A.nrows, ncols = B.ncols;
+  C->nrows = nA;
+  C->ncols = ncols;
+  C->nnz = 0;
+  C->pos = nullptr;
+  C->crd = nullptr;
+  C->vals = nullptr;
+  cudaEvent_t e0, e1;
+  SPWS_CUDA(cudaEventCreate(&e0));
+  SPWS_CUDA(cudaEventCreate(&e1));
+  SPWS_CUDA(cudaEventRecord(e0, s));
+  SPWS_TRY(dalloc((void**)&C->pos, sizeof(int32_t) * ((size_t)nA + 1), s));
+
+  long long* prods = nullptr;
+  long long* poff = nullptr;
+  int32_t* rowcnt = nullptr;
+  long long* tot = nullptr;
+  SPWS_TRY(dalloc((void**)&prods, sizeof(long long) * (size_t)std::max(nA, 1), s));
+  SPWS_TRY(dalloc((void**)&poff, sizeof(long long) * ((size_t)nA + 1), s));
+  SPWS_TRY(dalloc((void**)&rowcnt, sizeof(int32_t) * (size_t)std::max(nA, 1), s));
+  SPWS_TRY(dalloc((void**)&tot, sizeof(long long), s));
+  SPWS_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int32_t) * (size_t)std::max(nA, 1), s));
+  if (nA > 0) {
+    k_row_products<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A.pos, A.crd, B.pos, prods);
+    count_launch(1);
+  }
+  SPWS_TRY(scan_i64(prods, poff, nA, tot, s));
+  SPWS_CUDA(cudaMemcpyAsync(poff + nA, tot, sizeof(long long), cudaMemcpyDeviceToDevice, s));
+  std::vector<long long> hoff((size_t)nA + 1);
+  SPWS_CUDA(cudaMemcpyAsync(hoff.data(), poff, sizeof(long long) * ((size_t)nA + 1), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  const long long total_products = hoff[nA];
+
+  // chunk boundaries: consecutive rows whose products fit the budget (a row
+  // larger than the budget forms a chunk of its own)
+  std::vector<int32_t> cuts{0};
+  while (cuts.back() < nA) {
+    const int32_t r0 = cuts.back();
+    const long long lim = hoff[r0] + kChunkProducts;
+    int32_t r1 = (int32_t)(std::upper_bound(hoff.begin() + r0 + 1, hoff.end(), lim) - hoff.begin()) - 1;
+    if (r1 <= r0) r1 = r0 + 1;
+    cuts.push_back(std::min(r1, nA));
+  }
+  long long max_chunk = 0;
+  for (size_t c = 0; c + 1 < cuts.size(); c++) max_chunk = std::max(max_chunk, hoff[cuts[c + 1]] - hoff[cuts[c]]);
+  const size_t cap = (size_t)std::max<long long>(max_chunk, 1);
+
+  unsigned long long *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr;
+  int32_t* head = nullptr;
+  long long *hpos = nullptr, *starts = nullptr;
+  SPWS_TRY(dalloc((void**)&k0, sizeof(unsigned long long) * cap, s));
+  SPWS_TRY(dalloc((void**)&v0, sizeof(unsigned long long) * cap, s));
+  SPWS_TRY(dalloc((void**)&k1, sizeof(unsigned long long) * cap, s));
+  SPWS_TRY(dalloc((void**)&v1, sizeof(unsigned long long) * cap, s));
+  SPWS_TRY(dalloc((void**)&head, sizeof(int32_t) * cap, s));
+  SPWS_TRY(dalloc((void**)&hpos, sizeof(long long) * cap, s));
+  SPWS_TRY(dalloc((void**)&starts, sizeof(long long) * cap, s));
+
+  struct Part {
+    int32_t* crd;
+    double* val;
+    long long n;
+  };
+  std::vector<Part> parts;
+  long long nnz = 0;
+  int rc = SPWS_OK;
+  for (size_t c = 0; c + 1 < cuts.size() && rc == SPWS_OK; c++) {
+    const int32_t r0 = cuts[c], r1 = cuts[c + 1];
+    const long long n = hoff[r1] - hoff[r0];
+    if (n == 0) continue;
+    k_expand<<<(unsigned)((r1 - r0 + 7) / 8), 256, 0, s>>>(r0, r1, A.pos, A.crd, A.vals, B.pos, B.crd, B.vals, ncols,
+                                                            poff, k0, v0);
+    count_launch(1);
+    bool in_tmp = false;
+    const int bits = bits_for((unsigned long long)(r1 - r0) * (unsigned long long)std::max(ncols, 1));
+    if ((rc = radix_sort_pairs(k0, v0, k1, v1, n, bits, &in_tmp, s)) != SPWS_OK) break;
+    const unsigned long long* ks = in_tmp ? k1 : k0;
+    const unsigned long long* vs = in_tmp ? v1 : v0;
+    k_heads<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, ks, head);
+    count_launch(1);
+    if ((rc = scan_i32_to_i64(head, hpos, n, tot, s)) != SPWS_OK) break;
+    k_run_starts<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, head, hpos, starts);
+    count_launch(1);
+    long long nruns = 0;
+    SPWS_CUDA(cudaMemcpyAsync(&nruns, tot, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaStreamSynchronize(s));
+    Part pt{nullptr, nullptr, nruns};
+    if ((rc = dalloc((void**)&pt.crd, sizeof(int32_t) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
+    if ((rc = dalloc((void**)&pt.val, sizeof(double) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
+    k_reduce_runs<<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, n, starts, ks, vs, ncols, r0, pt.crd, pt.val,
+                                                                  rowcnt);
+    count_launch(1);
+    SPWS_CUDA(cudaGetLastError());
+    parts.push_back(pt);
+    nnz += nruns;
+  }
+  dfree(k0, s); dfree(v0, s); dfree(k1, s); dfree(v1, s);
+  dfree(head, s); dfree(hpos, s); dfree(starts, s);
+  if (rc == SPWS_OK && nnz > INT32_MAX) {
+    set_error("output has more than INT32_MAX nonzeros");
+    rc = SPWS_ERR_CAPACITY;
+  }
+  if (rc == SPWS_OK) {
+    C->nnz = nnz;
+    rc = dalloc((void**)&C->crd, sizeof(int32_t) * (size_t)std::max<long long>(nnz, 1), s);
+    if (rc == SPWS_OK) rc = dalloc((void**)&C->vals, sizeof(double) * (size_t)std::max<long long>(nnz, 1), s);
+    long long at = 0;
+    for (const Part& pt : parts) {
+      if (rc != SPWS_OK) break;
+      if (pt.n) {
+        cudaMemcpyAsync(C->crd + at, pt.crd, sizeof(int32_t) * (size_t)pt.n, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(C->vals + at, pt.val, sizeof(double) * (size_t)pt.n, cudaMemcpyDeviceToDevice, s);
+      }
+      at += pt.n;
+    }
+    if (rc == SPWS_OK) rc = scan_counts_i32(rowcnt, C->pos, nA, tot, s);
+  }
+  for (const Part& pt : parts) {
+    dfree(pt.crd, s);
+    dfree(pt.val, s);
+  }
+  SPWS_CUDA(cudaEventRecord(e1, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    *stats = spws_spgemm_stats{};
+    stats->products = total_products;
+    stats->nnz = nnz;
+    cudaEventElapsedTime(&stats->ms_total, e0, e1);
+    stats->ms_numeric = stats->ms_total;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dfree(prods, s); dfree(poff, s); dfree(rowcnt, s); dfree(tot, s);
+  return rc;
+}
+
+}  // namespace spws

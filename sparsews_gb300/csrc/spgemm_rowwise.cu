@@ -2,45 +2,53 @@
 // reference's TACO kernel (benchmark/CSR_CSR/CSR_CSR_taco.h:19-54 symbolic
 // C2_nnz assemble, :56-98 numeric) with GPU workspaces.
 //
-// Workspace: B's column space is cut into chunks of kW columns. For one row i
-// and one chunk, a CTA accumulates the products A(i,j)*B(j,k) with k in the
-// chunk into a dense FP64 array of kW entries in shared memory, and marks the
-// touched columns in a kW-bit bitmap. Scanning the bitmap in order yields the
-// row's columns already sorted, so no per-row sort is needed (the reference
-// sorts its workspace with qsort: CSR_CSR_hash_sequential.h:124-131).
+// One CTA handles one row of A at a time (rows are claimed heaviest first).
 //
-// A per-B-row chunk table (tab[j][c] = first position of row j with column
-// >= c*kW) turns "the part of B(j,:) inside chunk c" into one 8-byte load.
+// Symbolic pass: the row's products mark their columns in a bitmap over the
+// row's column span [lo, hi] (the span is read off the first and last column
+// of every B row it touches); the popcount is the row's output count
+// (the C2_nnz of CSR_CSR_taco.h:19-43).
 //
-// Pipeline (all on one stream, one host sync to size C):
-//   k_row_info      products per row (upper bound of the row's nnz), the
-//                   chunk range the row touches, a cost bucket
-//   k_chunk_table   tab[][] for B
-//   k_order_*       rows ordered by cost bucket, heaviest first
-//   k_symbolic      per-row output counts (bitmap popcounts)   -> C2_nnz
-//   scan            counts -> C.pos
-//   k_numeric       accumulate + write sorted crd/vals at C.pos[i]
+// Numeric pass: the bitmap is rebuilt, prefix-counted per 32-bit word, and the
+// output columns are written straight to C.crd in order (the bitmap is the
+// sorted column list, so no sort is needed; the reference qsorts:
+// CSR_CSR_hash_sequential.h:124-131). A column's rank in the bitmap is its
+// position in the row, so products are accumulated into a dense FP64 window
+// indexed by rank: windows of kAcc consecutive ranks, one after the other,
+// each written to C.vals with coalesced stores. Rows whose output fits one
+// window read every product once for the bitmap and once for the values.
+//
+// Inside a CTA the row's j's are taken in batches of kThreads; the products
+// of a batch form one flat stream split evenly over all threads (a thread
+// finds the B row of its product by walking the batch's prefix sums), so no
+// warp waits at a barrier for another that drew a long B row.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <climits>
 
+#include "common.cuh"
 #include "spws_internal.h"
 
 namespace spws {
 namespace {
 
-constexpr int kW = 8192;              // columns per chunk
-constexpr int kWords = kW / 32;       // bitmap words per chunk
-constexpr int kThreads = 256;         // threads per CTA in the symbolic/numeric passes
+constexpr int kThreads = 512;                 // threads per CTA (symbolic and numeric)
 constexpr int kWarps = kThreads / 32;
-constexpr int kBuckets = 66;          // cost buckets: 0 = no products, b = 1 + floor(log2(P))
-static_assert(kWords == kThreads, "one bitmap word per thread in the extraction");
+constexpr int kSpanBits = 1 << 18;            // columns one bitmap covers
+constexpr int kSpanWords = kSpanBits / 32;    // 8192
+constexpr int kGroupWords = 2048;             // words per 32-bit prefix base (65536 bits)
+constexpr int kGroups = kSpanWords / kGroupWords;
+constexpr int kAcc = 6144;                    // ranks per numeric window (48 KB of FP64)
+constexpr int kBuckets = 66;                  // cost buckets: 0 = no products, b = 1 + floor(log2(P))
+constexpr int kLightBucket = 9;               // rows with bucket <= 9 (fewer than 512 products) go to k_light
+constexpr int kLightMax = 512;                // staging entries per warp in k_light
+constexpr int kLightWarps = 8;                // warps per CTA in k_light
 
 struct RowInfo {
-  long long products;  // sum over j in A(i,:) of nnz(B(j,:))
-  int32_t cfirst;      // first chunk with products (or 0)
-  int32_t clast;       // last chunk with products (or -1)
+  long long products;  // sum over j in A(i,:) of nnz(B(j,:)) (upper bound of the row's nnz)
+  int32_t lo;          // smallest column the row can produce
+  int32_t hi;          // largest column the row can produce (-1 if none)
 };
 
 __device__ __forceinline__ int cost_bucket(long long p) { return p <= 0 ? 0 : 64 - __clzll(p); }
@@ -48,7 +56,8 @@ __device__ __forceinline__ int cost_bucket(long long p) { return p <= 0 ? 0 : 64
 // Warp per row of A: products, column span, cost bucket.
 __global__ void k_row_info(int32_t nA, const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
                            const int32_t* __restrict__ Bp, const int32_t* __restrict__ Bk, RowInfo* __restrict__ info,
-                           int* __restrict__ hist, unsigned long long* __restrict__ total_products) {
+                           int* __restrict__ hist, unsigned long long* __restrict__ total_products,
+                           int* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= nA) return;
@@ -73,41 +82,22 @@ __global__ void k_row_info(int32_t nA, const int32_t* __restrict__ Ap, const int
   if (lane == 0) {
     RowInfo r;
     r.products = p;
-    r.cfirst = p > 0 ? lo / kW : 0;
-    r.clast = p > 0 ? hi / kW : -1;
+    r.lo = p > 0 ? lo : 0;
+    r.hi = p > 0 ? hi : -1;
     info[i] = r;
     atomicAdd(&hist[cost_bucket(p)], 1);
     atomicAdd(total_products, (unsigned long long)p);
+    if (p > INT_MAX) atomicExch(err, 2);  // per-row product streams are indexed in 32 bits
   }
 }
 
-// Warp per row of B: tab[j*(nc+1) + c] = first position in row j whose column
-// is >= c*kW (row end if none). Every slot is written exactly once.
-__global__ void k_chunk_table(int32_t nB, int32_t nc, const int32_t* __restrict__ Bp, const int32_t* __restrict__ Bk,
-                              int32_t* __restrict__ tab) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (warp >= nB) return;
-  const int32_t j = (int32_t)warp;
-  const int32_t s = Bp[j], e = Bp[j + 1];
-  int32_t* t = tab + (int64_t)j * (nc + 1);
-  for (int32_t p = s + lane; p < e; p += 32) {
-    const int q = Bk[p] / kW;
-    const int qprev = p == s ? -1 : Bk[p - 1] / kW;
-    for (int c = qprev + 1; c <= q; c++) t[c] = p;
-  }
-  if (lane == 0) {
-    const int qlast = e > s ? Bk[e - 1] / kW : -1;
-    for (int c = qlast + 1; c <= nc; c++) t[c] = e;
-  }
-}
-
-// Single CTA: bucket offsets in descending cost order (bucket 0 excluded),
-// and the number of rows with products.
-__global__ void k_order_offsets(const int* __restrict__ hist, int* __restrict__ cursor, int* __restrict__ nwork) {
+// Single thread: bucket offsets in descending cost order (bucket 0 excluded).
+__global__ void k_order_offsets(const int* __restrict__ hist, int* __restrict__ cursor, int* __restrict__ nwork,
+                                int* __restrict__ nheavy) {
   if (threadIdx.x == 0) {
     int run = 0;
     for (int b = kBuckets - 1; b >= 1; b--) {
+      if (b == kLightBucket) *nheavy = run;
       cursor[b] = run;
       run += hist[b];
     }
@@ -122,90 +112,53 @@ __global__ void k_order_scatter(int32_t nA, const RowInfo* __restrict__ info, in
   if (i >= nA) return;
   const int b = cost_bucket(info[i].products);
   if (b == 0) return;
-  const int slot = atomicAdd(&cursor[b], 1);
-  order[slot] = (int32_t)i;
+  order[atomicAdd(&cursor[b], 1)] = (int32_t)i;
 }
 
-// Loads one j per lane for the batch starting at A position q0 and returns its
-// slice [s, s+len) of chunk c plus the A value.
-struct Slice {
-  int32_t s;
-  int32_t len;
-  double a;
+struct PassArgs {
+  const int32_t* Ap;
+  const int32_t* Aj;
+  const double* Av;
+  const int32_t* Bp;
+  const int32_t* Bk;
+  const double* Bv;
+  const RowInfo* info;
+  const int32_t* order;
+  const int* nwork;   // rows with products; order[0, nheavy) go to the CTA kernels,
+  const int* nheavy;  // order[nheavy, nwork) to k_light
+  int* counter;
+  int* light_counter;
+  int32_t* rowcnt;     // symbolic output
+  const int32_t* Cp;   // numeric input
+  int32_t* Ck;         // numeric output
+  double* Cv;          // numeric output
+  int* err;            // set on internal inconsistency
 };
 
-__device__ __forceinline__ Slice load_slice(int32_t q, int32_t qend, const int32_t* __restrict__ Aj,
-                                            const double* __restrict__ Av, const int32_t* __restrict__ tab,
-                                            int32_t nc1, int32_t c, bool want_val) {
-  Slice r{0, 0, 0.0};
-  if (q < qend) {
-    const int32_t j = __ldg(Aj + q);
-    const int32_t* tj = tab + (int64_t)j * nc1 + c;
-    r.s = __ldg(tj);
-    r.len = __ldg(tj + 1) - r.s;
-    if (want_val) r.a = __ldg(Av + q);
-  }
-  return r;
-}
+// Shared staging of one batch of j's: the B-row slice each thread loaded and
+// the exclusive prefix of slice lengths.
+struct Batch {
+  int32_t s[kThreads];
+  int32_t excl[kThreads + 1];
+  double a[kThreads];
+};
 
-// Expands the lanes' slices into a flat stream of entries and calls
-// f(position in B, owner's A value) for each, 32 entries per round.
-template <typename F>
-__device__ __forceinline__ void warp_expand(const Slice& sl, F&& f) {
-  const int lane = threadIdx.x & 31;
-  int incl = sl.len;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
-  }
-  const int total = __shfl_sync(0xffffffffu, incl, 31);
-  const int excl = incl - sl.len;
-  for (int base = 0; base < total; base += 32) {
-    const int fidx = base + lane;
-    // largest lane L with excl[L] <= fidx (it has a nonempty slice)
-    int owner = 0;
-#pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
-      const int cand = owner + step;
-      const int ex = __shfl_sync(0xffffffffu, excl, cand & 31);
-      if (cand < 32 && ex <= fidx) owner = cand;
-    }
-    const int o_excl = __shfl_sync(0xffffffffu, excl, owner);
-    const int o_s = __shfl_sync(0xffffffffu, sl.s, owner);
-    const double o_a = __shfl_sync(0xffffffffu, sl.a, owner);
-    if (fidx < total) f(o_s + (fidx - o_excl), o_a);
-  }
-}
-
-__device__ __forceinline__ int block_sum_int(int v, int* red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  int t = 0;
-#pragma unroll
-  for (int w = 0; w < kWarps; w++) t += red[w];
-  __syncthreads();
-  return t;
-}
-
-// Exclusive block scan of one int per thread; *total receives the block sum.
-__device__ __forceinline__ int block_excl_scan_int(int v, int* red, int* total) {
+// Block exclusive scan of one int per thread. Returns the exclusive prefix;
+// *total gets the block sum. Two barriers.
+__device__ __forceinline__ int block_excl_scan(int v, int* wsum, int* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int incl = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += y;
   }
-  if (lane == 31) red[warp] = incl;
+  if (lane == 31) wsum[warp] = incl;
   __syncthreads();
   int before = 0, t = 0;
 #pragma unroll
   for (int w = 0; w < kWarps; w++) {
-    const int x = red[w];
+    const int x = wsum[w];
     before += w < warp ? x : 0;
     t += x;
   }
@@ -214,124 +167,325 @@ __device__ __forceinline__ int block_excl_scan_int(int v, int* red, int* total) 
   return before + incl - v;
 }
 
-struct PassArgs {
-  int32_t nc1;  // chunks + 1 (row stride of tab)
-  const int32_t* Ap;
-  const int32_t* Aj;
-  const double* Av;
-  const int32_t* Bk;
-  const double* Bv;
-  const int32_t* tab;
-  const RowInfo* info;
-  const int32_t* order;
-  const int* nwork;
-  int* counter;
-  int32_t* rowcnt;     // symbolic output
-  const int32_t* Cp;   // numeric input
-  int32_t* Ck;         // numeric output
-  double* Cv;          // numeric output
-  int* err;            // set on internal inconsistency
-};
+__device__ __forceinline__ int32_t span_end(int32_t wlo) {
+  return (int32_t)min((long long)wlo + kSpanBits, (long long)INT_MAX);
+}
+
+// Loads batch [qb, qb + kThreads) of row i's A entries into `b`: the B-row
+// slice limited to columns in [clo, chi) when `clip` is set (found by binary
+// search in the sorted B row), else the whole B row. Returns the batch total;
+// `b.excl` holds the prefix. Ends with a barrier.
+__device__ __forceinline__ int load_batch(const PassArgs& a, int32_t qb, int32_t q1, bool want_a, bool clip,
+                                          int32_t clo, int32_t chi, Batch& b, int* wsum) {
+  const int32_t q = qb + threadIdx.x;
+  int32_t s = 0, len = 0;
+  double av = 0.0;
+  if (q < q1) {
+    const int32_t j = __ldg(a.Aj + q);
+    s = __ldg(a.Bp + j);
+    int32_t e = __ldg(a.Bp + j + 1);
+    if (clip && e > s) {
+      int32_t lo = s, hi = e;  // first position with column >= clo
+      while (lo < hi) {
+        const int32_t m = (lo + hi) >> 1;
+        if (__ldg(a.Bk + m) < clo) lo = m + 1; else hi = m;
+      }
+      const int32_t s2 = lo;
+      hi = e;  // first position with column >= chi
+      while (lo < hi) {
+        const int32_t m = (lo + hi) >> 1;
+        if (__ldg(a.Bk + m) < chi) lo = m + 1; else hi = m;
+      }
+      s = s2;
+      e = lo;
+    }
+    len = e - s;
+    if (want_a) av = __ldg(a.Av + q);
+  }
+  int total;
+  const int ex = block_excl_scan(len, wsum, &total);
+  b.s[threadIdx.x] = s;
+  b.excl[threadIdx.x] = ex;
+  b.a[threadIdx.x] = av;
+  if (threadIdx.x == 0) b.excl[kThreads] = total;
+  __syncthreads();
+  return total;
+}
+
+// Calls f(position in B, A value) for the flat entries t, t+kThreads, ... of
+// the batch. The owner slice of the first entry is found by binary search,
+// later ones by walking forward.
+template <typename F>
+__device__ __forceinline__ void for_batch_entries(const Batch& b, int total, F&& f) {
+  int fidx = threadIdx.x;
+  if (fidx >= total) return;
+  int lo = 0, hi = kThreads - 1;  // largest o with excl[o] <= fidx
+  while (lo < hi) {
+    const int m = (lo + hi + 1) >> 1;
+    if (b.excl[m] <= fidx) lo = m; else hi = m - 1;
+  }
+  int o = lo;
+  for (; fidx < total; fidx += kThreads) {
+    while (b.excl[o + 1] <= fidx) o++;
+    f(b.s[o] + (fidx - b.excl[o]), b.a[o]);
+  }
+}
+
+// Marks the columns of row i inside [wlo, wlo + kSpanBits) in bm (cleared by
+// the caller). Every batch ends with a barrier.
+__device__ __forceinline__ void build_bitmap(const PassArgs& a, int32_t q0, int32_t q1, int32_t wlo, bool clip,
+                                             uint32_t* bm, Batch& b, int* wsum) {
+  for (int32_t qb = q0; qb < q1; qb += kThreads) {
+    const int total = load_batch(a, qb, q1, false, clip, wlo, clip ? span_end(wlo) : INT_MAX, b, wsum);
+    for_batch_entries(b, total, [&](int32_t p, double) {
+      const int k = __ldg(a.Bk + p) - wlo;
+      atomicOr(&bm[k >> 5], 1u << (k & 31));
+    });
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ int claim(int* counter, int* s_idx) {
+  __syncthreads();
+  if (threadIdx.x == 0) *s_idx = atomicAdd(counter, 1);
+  __syncthreads();
+  return *s_idx;
+}
+
+__device__ __forceinline__ int words_in(long long wl, int32_t hi) {
+  return (int)min((long long)kSpanWords, ((long long)hi - wl + 1 + 31) >> 5);
+}
 
 // Symbolic pass: per row, the number of distinct output columns.
-__global__ void __launch_bounds__(kThreads) k_symbolic(PassArgs a) {
-  __shared__ uint32_t bm[kWords];
-  __shared__ int red[kWarps];
+__global__ void __launch_bounds__(kThreads, 2) k_symbolic(PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* bm = reinterpret_cast<uint32_t*>(smem);  // kSpanWords
+  Batch& b = *reinterpret_cast<Batch*>(smem + sizeof(uint32_t) * kSpanWords);
+  __shared__ int wsum[kWarps];
   __shared__ int s_idx;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  bm[threadIdx.x] = 0;
-  const int nwork = *a.nwork;
+  const int nwork = *a.nheavy;
   for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_idx = atomicAdd(a.counter, 1);
-    __syncthreads();
-    const int idx = s_idx;
+    const int idx = claim(a.counter, &s_idx);
     if (idx >= nwork) break;
     const int32_t i = a.order[idx];
     const RowInfo ri = a.info[i];
     const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
+    const bool multi = (long long)ri.hi - ri.lo + 1 > kSpanBits;
     int total = 0;
-    for (int32_t c = ri.cfirst; c <= ri.clast; c++) {
-      const int32_t col0 = c * kW;
-      for (int32_t qb = q0 + warp * 32; qb < q1; qb += kThreads) {
-        const Slice sl = load_slice(qb + lane, q1, a.Aj, a.Av, a.tab, a.nc1, c, false);
-        warp_expand(sl, [&](int32_t p, double) {
-          const int k = __ldg(a.Bk + p) - col0;
-          atomicOr(&bm[k >> 5], 1u << (k & 31));
-        });
-      }
+    for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
+      const int nw = words_in(wl, ri.hi);
+      for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = 0;
       __syncthreads();
-      const int cnt = __popc(bm[threadIdx.x]);
-      bm[threadIdx.x] = 0;
-      total += block_sum_int(cnt, red);
+      build_bitmap(a, q0, q1, (int32_t)wl, multi, bm, b, wsum);
+      int c = 0;
+      for (int w = threadIdx.x; w < nw; w += kThreads) c += __popc(bm[w]);
+      int t;
+      block_excl_scan(c, wsum, &t);
+      total += t;
     }
     if (threadIdx.x == 0) a.rowcnt[i] = total;
   }
 }
 
-// Numeric pass: accumulate into the dense chunk workspace, then write the
-// chunk's entries in column order at C.pos[i] + (entries of earlier chunks).
-__global__ void __launch_bounds__(kThreads) k_numeric(PassArgs a) {
-  extern __shared__ double acc[];  // kW doubles
-  __shared__ uint32_t bm[kWords];
-  __shared__ int red[kWarps];
+// Numeric pass (see the file comment).
+__global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* acc = reinterpret_cast<double*>(smem);                             // kAcc
+  uint32_t* bm = reinterpret_cast<uint32_t*>(smem + sizeof(double) * kAcc);  // kSpanWords
+  uint16_t* wpre = reinterpret_cast<uint16_t*>(bm + kSpanWords);             // kSpanWords
+  Batch& b = *reinterpret_cast<Batch*>(reinterpret_cast<unsigned char*>(wpre + kSpanWords));
+  __shared__ uint32_t gbase[kGroups];
+  __shared__ int wsum[kWarps];
   __shared__ int s_idx;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = threadIdx.x; q < kW; q += kThreads) acc[q] = 0.0;
-  bm[threadIdx.x] = 0;
-  const int nwork = *a.nwork;
+  __shared__ int32_t s_cols[2];
+  for (int q = threadIdx.x; q < kAcc; q += kThreads) acc[q] = 0.0;
+  const int nwork = *a.nheavy;
   for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_idx = atomicAdd(a.counter, 1);
-    __syncthreads();
-    const int idx = s_idx;
+    const int idx = claim(a.counter, &s_idx);
     if (idx >= nwork) break;
     const int32_t i = a.order[idx];
     const RowInfo ri = a.info[i];
     const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
+    const bool multi = (long long)ri.hi - ri.lo + 1 > kSpanBits;
+    const int32_t row_end = a.Cp[i + 1];
     int32_t out = a.Cp[i];
-    for (int32_t c = ri.cfirst; c <= ri.clast; c++) {
-      const int32_t col0 = c * kW;
-      for (int32_t qb = q0 + warp * 32; qb < q1; qb += kThreads) {
-        const Slice sl = load_slice(qb + lane, q1, a.Aj, a.Av, a.tab, a.nc1, c, true);
-        warp_expand(sl, [&](int32_t p, double av) {
-          const int k = __ldg(a.Bk + p) - col0;
-          const double prod = __dmul_rn(av, __ldg(a.Bv + p));
-          atomicOr(&bm[k >> 5], 1u << (k & 31));
-          atomicAdd(&acc[k], prod);
-        });
+    for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
+      const int32_t wlo = (int32_t)wl;
+      const int nw = words_in(wl, ri.hi);
+      for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = 0;
+      __syncthreads();
+      build_bitmap(a, q0, q1, wlo, multi, bm, b, wsum);
+
+      // per-word prefix of set bits; thread t owns a contiguous run of words
+      const int per = (nw + kThreads - 1) / kThreads;
+      const int w0 = min(nw, (int)threadIdx.x * per), w1 = min(nw, w0 + per);
+      int c = 0;
+      for (int w = w0; w < w1; w++) c += __popc(bm[w]);
+      int nnz_w;
+      int run = block_excl_scan(c, wsum, &nnz_w);
+      for (int w = w0; w < w1; w++) {
+        if ((w & (kGroupWords - 1)) == 0) gbase[w / kGroupWords] = (uint32_t)run;
+        wpre[w] = (uint16_t)run;
+        run += __popc(bm[w]);
       }
       __syncthreads();
-      uint32_t word = bm[threadIdx.x];
-      int chunk_total;
-      int p = out + block_excl_scan_int(__popc(word), red, &chunk_total);
-      const int kbase = threadIdx.x * 32;
-      const int32_t lim = a.Cp[i + 1];
-      while (word) {
-        const int b = __ffs(word) - 1;
-        word &= word - 1;
-        if (p < lim) {  // never write past the row the symbolic pass sized
-          a.Ck[p] = col0 + kbase + b;
-          a.Cv[p] = acc[kbase + b];
-        } else {
-          atomicExch(a.err, 1);
-        }
-        acc[kbase + b] = 0.0;
-        p++;
+      if (out + nnz_w > row_end) {  // never write past the row the symbolic pass sized
+        if (threadIdx.x == 0) atomicExch(a.err, 1);
+        break;
       }
-      bm[threadIdx.x] = 0;
-      out += chunk_total;
-      __syncthreads();  // the next chunk's products must not race the resets above
+      // prefix of word w: the group's 32-bit base plus the 16-bit difference
+      auto word_prefix = [&](int w) -> int {
+        const uint32_t base = gbase[w / kGroupWords];
+        return (int)base + (int)(uint16_t)(wpre[w] - (uint16_t)base);
+      };
+      // columns, in order
+      for (int w = w0; w < w1; w++) {
+        uint32_t word = bm[w];
+        int r = word_prefix(w);
+        while (word) {
+          const int bit = __ffs(word) - 1;
+          word &= word - 1;
+          a.Ck[out + r] = wlo + w * 32 + bit;
+          r++;
+        }
+      }
+      // values, one window of kAcc ranks at a time
+      for (int r0 = 0; r0 < nnz_w; r0 += kAcc) {
+        const int r1 = min(nnz_w, r0 + kAcc);
+        const bool whole = r0 == 0 && r1 == nnz_w;
+        int32_t clo = wlo, chi = multi ? span_end(wlo) : INT_MAX;
+        if (!whole) {  // columns of ranks r0 and r1 bound the window
+          if (threadIdx.x < 2) {
+            const int target = threadIdx.x == 0 ? r0 : r1;
+            int32_t col;
+            if (target >= nnz_w) {
+              col = multi ? span_end(wlo) : INT_MAX;
+            } else {
+              int lo = 0, hi = nw - 1;  // last word whose prefix <= target
+              while (lo < hi) {
+                const int m = (lo + hi + 1) >> 1;
+                if (word_prefix(m) <= target) lo = m; else hi = m - 1;
+              }
+              int need = target - word_prefix(lo);
+              uint32_t word = bm[lo];
+              while (need-- > 0) word &= word - 1;
+              col = wlo + lo * 32 + (__ffs(word) - 1);
+            }
+            s_cols[threadIdx.x] = col;
+          }
+          __syncthreads();
+          clo = s_cols[0];
+          chi = s_cols[1];
+        }
+        const bool clip = multi || !whole;
+        for (int32_t qb = q0; qb < q1; qb += kThreads) {
+          const int total = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
+          for_batch_entries(b, total, [&](int32_t p, double av) {
+            const int k = __ldg(a.Bk + p) - wlo;
+            const int w = k >> 5;
+            const int rank = word_prefix(w) + __popc(bm[w] & ((1u << (k & 31)) - 1u));
+            atomicAdd(&acc[rank - r0], __dmul_rn(av, __ldg(a.Bv + p)));
+          });
+          __syncthreads();
+        }
+        for (int r = r0 + threadIdx.x; r < r1; r += kThreads) {
+          a.Cv[out + r] = acc[r - r0];
+          acc[r - r0] = 0.0;
+        }
+        __syncthreads();
+      }
+      out += nnz_w;
     }
-    if (threadIdx.x == 0 && out != a.Cp[i + 1]) atomicExch(a.err, 1);
+    if (threadIdx.x == 0 && out != row_end) atomicExch(a.err, 1);
   }
 }
 
-int sm_count_cached() {
-  DeviceState* ds = nullptr;
-  if (device_state(&ds) != SPWS_OK) return 1;
-  return ds->sm_count;
+
+// Light rows (fewer than 512 products): one warp per row, no CTA barriers.
+// The row's products are staged in shared memory as (column << 32 | flat
+// index) keys in the reference's visiting order (j ascending, then k), sorted
+// with a bitonic network (keys are unique, so the order of equal columns is
+// their visiting order), and each run of equal columns is summed left to
+// right: the value is the reference's sequential sum bit for bit.
+template <bool NUMERIC>
+__global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long* key = reinterpret_cast<unsigned long long*>(smem) + (size_t)warp * kLightMax;
+  double* val = reinterpret_cast<double*>(smem + sizeof(unsigned long long) * kLightMax * kLightWarps) +
+                (size_t)warp * kLightMax;
+  const int lo_idx = *a.nheavy, hi_idx = *a.nwork;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(a.light_counter, 1) + lo_idx;
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= hi_idx) break;
+    const int32_t i = a.order[idx];
+    const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
+    int n = 0;
+    for (int32_t qb = q0; qb < q1; qb += 32) {
+      Slice sl{0, 0, 0.0};
+      const int32_t q = qb + lane;
+      if (q < q1) {
+        const int32_t j = __ldg(a.Aj + q);
+        sl.s = __ldg(a.Bp + j);
+        sl.len = __ldg(a.Bp + j + 1) - sl.s;
+        if (NUMERIC) sl.a = __ldg(a.Av + q);
+      }
+      const int base = n;
+      n += warp_expand_indexed(sl, [&](int f, int32_t p, double av) {
+        const int at = base + f;  // < kLightMax: the row has fewer than 512 products
+        key[at] = ((unsigned long long)(uint32_t)__ldg(a.Bk + p) << 32) | (unsigned)at;
+        if (NUMERIC) val[at] = __dmul_rn(av, __ldg(a.Bv + p));
+      });
+    }
+    int S = 32;
+    while (S < n) S <<= 1;
+    for (int t = n + lane; t < S; t += 32) key[t] = ~0ull;
+    __syncwarp();
+    for (int k = 2; k <= S; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = lane; t < (S >> 1); t += 32) {
+          const int x = (t / j) * (j << 1) + (t % j), y = x + j;
+          const unsigned long long kx = key[x], ky = key[y];
+          if ((kx > ky) == ((x & k) == 0)) {  // values stay put: a key's low bits index them
+            key[x] = ky;
+            key[y] = kx;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    // runs of equal columns; values in the sorted (visiting) order
+    int rank = 0;
+    const int32_t out = NUMERIC ? a.Cp[i] : 0;
+    for (int b0 = 0; b0 < n; b0 += 32) {
+      const int p = b0 + lane;
+      const uint32_t col = p < n ? (uint32_t)(key[p] >> 32) : 0u;
+      const bool head = p < n && (p == 0 || (uint32_t)(key[p - 1] >> 32) != col);
+      const unsigned hm = __ballot_sync(0xffffffffu, head);
+      if (NUMERIC && head) {
+        double v = val[(int)(uint32_t)key[p]];
+        for (int q = p + 1; q < n && (uint32_t)(key[q] >> 32) == col; q++) v = __dadd_rn(v, val[(int)(uint32_t)key[q]]);
+        const int r = rank + __popc(hm & ((1u << lane) - 1u));
+        if (out + r < a.Cp[i + 1]) {  // never write past the row the symbolic pass sized
+          a.Ck[out + r] = (int32_t)col;
+          a.Cv[out + r] = v;
+        }
+      }
+      rank += __popc(hm);
+    }
+    if (!NUMERIC && lane == 0) a.rowcnt[i] = rank;
+    if (NUMERIC && lane == 0 && out + rank != a.Cp[i + 1]) atomicExch(a.err, 1);
+    __syncwarp();
+  }
 }
+
+constexpr size_t kLightSymSmem = sizeof(unsigned long long) * kLightMax * kLightWarps;
+constexpr size_t kLightNumSmem = (sizeof(unsigned long long) + sizeof(double)) * kLightMax * kLightWarps;
+constexpr size_t kSymSmem = sizeof(uint32_t) * kSpanWords + sizeof(Batch);
+constexpr size_t kNumSmem =
+    sizeof(double) * kAcc + sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords + sizeof(Batch);
 
 }  // namespace
 
@@ -339,9 +493,7 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
                    spws_spgemm_stats* stats, cudaStream_t s) {
   (void)opt;
   const int32_t nA = A.nrows;
-  const int32_t nB = B.nrows;
   const int32_t ncols = B.ncols;
-  const int32_t nc = std::max(1, (ncols + kW - 1) / kW);
   C->nrows = nA;
   C->ncols = ncols;
   C->nnz = 0;
@@ -349,7 +501,9 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
   C->crd = nullptr;
   C->vals = nullptr;
 
-  cudaEvent_t ev[5];
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  cudaEvent_t ev[6];
   for (auto& e : ev) SPWS_CUDA(cudaEventCreate(&e));
   SPWS_CUDA(cudaEventRecord(ev[0], s));
 
@@ -361,12 +515,12 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
     return SPWS_OK;
   }
 
-  // scratch: one block for the small counters, then the per-row arrays
   struct Small {
     int hist[kBuckets];
     int cursor[kBuckets];
     int nwork;
-    int counter[2];
+    int nheavy;
+    int counter[4];
     int err;
     unsigned long long products;
     long long nnz;
@@ -375,58 +529,77 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
   RowInfo* info = nullptr;
   int32_t* order = nullptr;
   int32_t* rowcnt = nullptr;
-  int32_t* tab = nullptr;
   SPWS_TRY(dalloc((void**)&sm, sizeof(Small), s));
   SPWS_TRY(dalloc((void**)&info, sizeof(RowInfo) * (size_t)nA, s));
   SPWS_TRY(dalloc((void**)&order, sizeof(int32_t) * (size_t)nA, s));
   SPWS_TRY(dalloc((void**)&rowcnt, sizeof(int32_t) * (size_t)nA, s));
-  SPWS_TRY(dalloc((void**)&tab, sizeof(int32_t) * (size_t)std::max(nB, 1) * (nc + 1), s));
   SPWS_CUDA(cudaMemsetAsync(sm, 0, sizeof(Small), s));
   SPWS_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int32_t) * (size_t)nA, s));
 
-  const int warps_per_block = 8;
-  k_row_info<<<(unsigned)((nA + warps_per_block - 1) / warps_per_block), warps_per_block * 32, 0, s>>>(
-      nA, A.pos, A.crd, B.pos, B.crd, info, sm->hist, &sm->products);
-  if (nB > 0)
-    k_chunk_table<<<(unsigned)((nB + warps_per_block - 1) / warps_per_block), warps_per_block * 32, 0, s>>>(
-        nB, nc, B.pos, B.crd, tab);
-  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork);
+  k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A.pos, A.crd, B.pos, B.crd, info, sm->hist, &sm->products,
+                                                      &sm->err);
+  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy);
   k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, sm->cursor, order);
+  count_launch(3);
   SPWS_CUDA(cudaGetLastError());
   SPWS_CUDA(cudaEventRecord(ev[1], s));
 
-  const int sms = sm_count_cached();
   PassArgs pa{};
-  pa.nc1 = nc + 1;
   pa.Ap = A.pos;
   pa.Aj = A.crd;
   pa.Av = A.vals;
+  pa.Bp = B.pos;
   pa.Bk = B.crd;
   pa.Bv = B.vals;
-  pa.tab = tab;
   pa.info = info;
   pa.order = order;
   pa.nwork = &sm->nwork;
+  pa.nheavy = &sm->nheavy;
   pa.counter = &sm->counter[0];
+  pa.light_counter = &sm->counter[2];
   pa.rowcnt = rowcnt;
   pa.err = &sm->err;
-  k_symbolic<<<sms * 8, kThreads, 0, s>>>(pa);
+  SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
+  SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
+  int per_sym = 1, per_num = 1;
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sym, k_symbolic, kThreads, kSymSmem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_num, k_numeric, kThreads, kNumSmem));
+  k_symbolic<<<ds->sm_count * std::max(per_sym, 1), kThreads, kSymSmem, s>>>(pa);
+  SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
+  SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
+  int per_ls = 1, per_ln = 1;
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ls, k_light<false>, kLightWarps * 32, kLightSymSmem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ln, k_light<true>, kLightWarps * 32, kLightNumSmem));
+  k_light<false><<<ds->sm_count * std::max(per_ls, 1), kLightWarps * 32, kLightSymSmem, s>>>(pa);
+  count_launch(2);
   SPWS_CUDA(cudaGetLastError());
   SPWS_CUDA(cudaEventRecord(ev[2], s));
 
   SPWS_TRY(scan_counts_i32(rowcnt, C->pos, nA, &sm->nnz, s));
   SPWS_CUDA(cudaEventRecord(ev[3], s));
 
-  cudaEvent_t ev_num0;
-  SPWS_CUDA(cudaEventCreate(&ev_num0));
   long long nnz = 0;
   unsigned long long products = 0;
+  int err = 0;
   SPWS_CUDA(cudaMemcpyAsync(&nnz, &sm->nnz, sizeof(nnz), cudaMemcpyDeviceToHost, s));
   SPWS_CUDA(cudaMemcpyAsync(&products, &sm->products, sizeof(products), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&err, &sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
   SPWS_CUDA(cudaStreamSynchronize(s));
+  auto cleanup = [&] {
+    for (auto& e : ev) cudaEventDestroy(e);
+    dfree(sm, s);
+    dfree(info, s);
+    dfree(order, s);
+    dfree(rowcnt, s);
+  };
+  if (err == 2) {
+    cleanup();
+    set_error("a row of A has 2^31 or more products");
+    return SPWS_ERR_CAPACITY;
+  }
   if (nnz > INT32_MAX) {
+    cleanup();
     set_error("output has more than INT32_MAX nonzeros; taco_tensor_t positions are int32");
-    dfree(sm, s); dfree(info, s); dfree(order, s); dfree(rowcnt, s); dfree(tab, s);
     return SPWS_ERR_CAPACITY;
   }
   C->nnz = nnz;
@@ -434,19 +607,17 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
   SPWS_TRY(dalloc((void**)&C->vals, sizeof(double) * (size_t)std::max<long long>(nnz, 1), s));
 
   pa.counter = &sm->counter[1];
+  pa.light_counter = &sm->counter[3];
   pa.Cp = C->pos;
   pa.Ck = C->crd;
   pa.Cv = C->vals;
-  const size_t smem = sizeof(double) * kW;
-  SPWS_CUDA(cudaEventRecord(ev_num0, s));
-  SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 1;
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_numeric, kThreads, smem));
-  k_numeric<<<sms * std::max(per_sm, 1), kThreads, smem, s>>>(pa);
-  SPWS_CUDA(cudaGetLastError());
   SPWS_CUDA(cudaEventRecord(ev[4], s));
+  k_numeric<<<ds->sm_count * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
+  k_light<true><<<ds->sm_count * std::max(per_ln, 1), kLightWarps * 32, kLightNumSmem, s>>>(pa);
+  count_launch(2);
+  SPWS_CUDA(cudaGetLastError());
+  SPWS_CUDA(cudaEventRecord(ev[5], s));
 
-  int err = 0;
   SPWS_CUDA(cudaMemcpyAsync(&err, &sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
   SPWS_CUDA(cudaStreamSynchronize(s));
   if (stats) {
@@ -455,18 +626,12 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
     cudaEventElapsedTime(&stats->ms_setup, ev[0], ev[1]);
     cudaEventElapsedTime(&stats->ms_symbolic, ev[1], ev[2]);
     cudaEventElapsedTime(&stats->ms_scan, ev[2], ev[3]);
-    cudaEventElapsedTime(&stats->ms_numeric, ev_num0, ev[4]);
+    cudaEventElapsedTime(&stats->ms_numeric, ev[4], ev[5]);
     stats->ms_total = stats->ms_setup + stats->ms_symbolic + stats->ms_scan + stats->ms_numeric;
-    stats->chunk_width = kW;
-    stats->n_chunks = nc;
+    stats->chunk_width = kAcc;
+    stats->n_chunks = (ncols + kSpanBits - 1) / kSpanBits;
   }
-  for (auto& e : ev) cudaEventDestroy(e);
-  cudaEventDestroy(ev_num0);
-  dfree(sm, s);
-  dfree(info, s);
-  dfree(order, s);
-  dfree(rowcnt, s);
-  dfree(tab, s);
+  cleanup();
   if (err) {
     set_error("numeric pass wrote a different number of entries than the symbolic pass counted");
     return SPWS_ERR_CUDA;

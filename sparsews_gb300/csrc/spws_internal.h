@@ -14,6 +14,8 @@ namespace spws {
 // Thread-local error message; set by the failing call, read by spws_last_error().
 void set_error(const std::string& msg);
 void clear_error();
+// Adds n to the count of kernels launched by this library (spws_launch_count).
+void count_launch(int n);
 
 // Wraps a CUDA call: on failure records the message and returns SPWS_ERR_CUDA
 // (or SPWS_ERR_NOMEM for allocation failures) from the enclosing function.
@@ -66,6 +68,10 @@ struct CsrView {
 // `transpose_key` is reserved (0).
 int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const SpgemmOpts& opt,
                    spws_spgemm_stats* stats, cudaStream_t stream);
+
+// Coordinate-workspace SpGEMM (expand, stable radix sort, ordered run
+// reduction): C = A*B with every value summed in ascending-j order.
+int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgemm_stats* stats, cudaStream_t stream);
 
 // Exclusive scan of `n` int32 counts into `out[0..n]` (out[n] = total), with
 // the total also returned through `total_dev` (int64, device) so callers can

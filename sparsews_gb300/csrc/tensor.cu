@@ -1,0 +1,441 @@
+// Sparse tensor kernels with the bucket workspace: MTTKRP and TTM on a CSF
+// tensor (benchmark/MTTKRP/COO_CSF_DCSR_DCSR_*.h, benchmark/TTM/COO_CSF_DCSR_*.h).
+//
+// The reference inserts one product per (leaf, output column) into a hash or
+// bucket workspace and sorts. Here the leaves are bucketed by their output
+// coordinate with the stable radix sort (MTTKRP: the leaf coordinate i; TTM:
+// the pair (k, j)), which keeps the leaves of each bucket in CSF order, i.e.
+// the order in which the reference's loops visit them. A warp then walks a
+// bucket with one lane per output column (j for MTTKRP, l for TTM) and sums
+// left to right in FP64, so a bucket handled by one warp gives the
+// reference's value bit for bit. Buckets longer than kPiece leaves are split
+// into pieces whose partial sums are added in order afterwards.
+//
+// Factor matrices arrive as DCSR (possibly with missing entries, the
+// reference's co-iteration C(k,:) & D(l,:)); they are expanded to dense rows
+// plus a presence bitmask, and a product is formed only where every factor
+// entry it needs is present, as in the co-iteration.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <string>
+
+#include "convert.h"
+#include "sort.h"
+#include "spws_internal.h"
+#include "tensor.h"
+
+namespace spws {
+namespace {
+
+constexpr int kPiece = 2048;  // leaves per warp work item
+constexpr int kJpl = 8;       // output columns per lane per pass (256 per warp)
+constexpr int kTileR = 32 * kJpl;
+
+int bits_for(unsigned long long max_key_exclusive) {
+  int b = 0;
+  while (b < 64 && (1ull << b) < max_key_exclusive) b++;
+  return b;
+}
+
+__global__ void k_densify(int32_t nq, const int32_t* __restrict__ oc, const int32_t* __restrict__ pos,
+                          const int32_t* __restrict__ ic, const double* __restrict__ vals, int32_t R, int32_t mw,
+                          double* __restrict__ dense, uint32_t* __restrict__ mask) {
+  const int lane = threadIdx.x & 31;
+  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= nq) return;
+  const int64_t row = oc[q];
+  for (int32_t p = pos[q] + lane; p < pos[q + 1]; p += 32) {
+    const int j = ic[p];
+    dense[row * R + j] = vals[p];
+    atomicOr(&mask[row * mw + (j >> 5)], 1u << (j & 31));
+  }
+}
+
+// fib_root[f] = coordinate of the root that owns level-1 fiber f
+__global__ void k_fiber_root(int32_t nk, const int32_t* __restrict__ roots, const int32_t* __restrict__ pos1,
+                             int32_t* __restrict__ fib_root) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= nk) return;
+  for (int32_t f = pos1[r] + lane; f < pos1[r + 1]; f += 32) fib_root[f] = roots[r];
+}
+
+// leaf_fib[p] = level-1 fiber that owns leaf p
+__global__ void k_leaf_fiber(int32_t nf, const int32_t* __restrict__ pos2, int32_t* __restrict__ leaf_fib) {
+  const int lane = threadIdx.x & 31;
+  const int64_t f = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (f >= nf) return;
+  for (int32_t p = pos2[f] + lane; p < pos2[f + 1]; p += 32) leaf_fib[p] = (int32_t)f;
+}
+
+// Bucket keys: MTTKRP buckets by the leaf coordinate, TTM by (root, leaf).
+__global__ void k_keys(int64_t nnz, int mode, const int32_t* __restrict__ crd2, const int32_t* __restrict__ leaf_fib,
+                       const int32_t* __restrict__ fib_root, int32_t dim_leaf, unsigned long long* __restrict__ keys,
+                       unsigned long long* __restrict__ pay) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nnz) return;
+  if (mode == 0)
+    keys[p] = (unsigned long long)crd2[p];
+  else
+    keys[p] = (unsigned long long)fib_root[leaf_fib[p]] * (unsigned long long)dim_leaf + (unsigned long long)crd2[p];
+  pay[p] = (unsigned long long)p;
+}
+
+// Per sorted leaf: the two factor rows it multiplies and its value.
+// MTTKRP: (k = root coordinate, l = level-1 coordinate); TTM: (i = level-1 coordinate, unused).
+__global__ void k_gather(int64_t nnz, int mode, const unsigned long long* __restrict__ perm,
+                         const int32_t* __restrict__ leaf_fib, const int32_t* __restrict__ fib_root,
+                         const int32_t* __restrict__ crd1, const double* __restrict__ vals, int32_t* __restrict__ r0,
+                         int32_t* __restrict__ r1, double* __restrict__ b) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nnz) return;
+  const int64_t p = (int64_t)perm[q];
+  const int32_t f = leaf_fib[p];
+  if (mode == 0) {
+    r0[q] = fib_root[f];
+    r1[q] = crd1[f];
+  } else {
+    r0[q] = crd1[f];
+    r1[q] = 0;
+  }
+  b[q] = vals[p];
+}
+
+__global__ void k_heads(int64_t n, const unsigned long long* __restrict__ keys, int32_t* __restrict__ head) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  head[p] = (p == 0 || keys[p] != keys[p - 1]) ? 1 : 0;
+}
+
+__global__ void k_starts(int64_t n, const int32_t* __restrict__ head, const long long* __restrict__ hpos,
+                         long long* __restrict__ starts) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  if (head[p]) starts[hpos[p]] = p;
+}
+
+__global__ void k_piece_counts(int64_t nseg, const long long* __restrict__ starts, int32_t* __restrict__ pc) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  pc[s] = (int32_t)((starts[s + 1] - starts[s] + kPiece - 1) / kPiece);
+}
+
+__global__ void k_piece_fill(int64_t nseg, const long long* __restrict__ starts, const long long* __restrict__ poff,
+                             int32_t* __restrict__ pseg, long long* __restrict__ pstart) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const long long n = (starts[s + 1] - starts[s] + kPiece - 1) / kPiece;
+  for (long long q = 0; q < n; q++) {
+    pseg[poff[s] + q] = (int32_t)s;
+    pstart[poff[s] + q] = starts[s] + q * kPiece;
+  }
+}
+
+struct Factor {
+  const double* dense;
+  const uint32_t* mask;
+  int32_t rows, R, mw;
+};
+
+// Warp per piece: left-to-right FP64 sums of the piece's leaves for output
+// columns [j0, j0 + kTileR) (lane handles j0 + lane + 32u). MTTKRP forms
+// (b * C(k,j)) * D(l,j) (hash_free.h:307), TTM forms b * C(i,l) (hash_il.h:317).
+template <int MODE>
+__global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, const long long* __restrict__ pstart,
+                         const long long* __restrict__ starts, const int32_t* __restrict__ r0,
+                         const int32_t* __restrict__ r1, const double* __restrict__ bv, Factor F0, Factor F1, int32_t R,
+                         int32_t j0, int32_t mw, double* __restrict__ partial, uint32_t* __restrict__ pmask) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= npieces) return;
+  const long long q0 = pstart[w];
+  const long long q1 = min(q0 + (long long)kPiece, starts[pseg[w] + 1]);
+  double acc[kJpl];
+  unsigned started = 0;
+#pragma unroll
+  for (int u = 0; u < kJpl; u++) acc[u] = 0.0;
+  for (long long qb = q0; qb < q1; qb += 32) {
+    const long long q = qb + lane;
+    int32_t a0 = -1, a1 = -1;
+    double b = 0.0;
+    if (q < q1) {
+      a0 = r0[q];
+      a1 = r1[q];
+      b = bv[q];
+    }
+    const int nb = (int)min(32LL, q1 - qb);
+    for (int t = 0; t < nb; t++) {
+      const int32_t x0 = __shfl_sync(0xffffffffu, a0, t);
+      const int32_t x1 = __shfl_sync(0xffffffffu, a1, t);
+      const double bb = __shfl_sync(0xffffffffu, b, t);
+      if (x0 >= F0.rows || (MODE == 0 && x1 >= F1.rows)) continue;  // factor row absent
+#pragma unroll
+      for (int u = 0; u < kJpl; u++) {
+        const int j = j0 + lane + 32 * u;
+        if (j >= R) break;
+        const bool have0 = (F0.mask[(int64_t)x0 * F0.mw + (j >> 5)] >> (j & 31)) & 1u;
+        bool have = have0;
+        if (MODE == 0) have = have && ((F1.mask[(int64_t)x1 * F1.mw + (j >> 5)] >> (j & 31)) & 1u);
+        if (!have) continue;
+        double t0 = __dmul_rn(bb, F0.dense[(int64_t)x0 * F0.R + j]);
+        if (MODE == 0) t0 = __dmul_rn(t0, F1.dense[(int64_t)x1 * F1.R + j]);
+        acc[u] = ((started >> u) & 1u) ? __dadd_rn(acc[u], t0) : t0;
+        started |= 1u << u;
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kJpl; u++) {
+    const int j = j0 + lane + 32 * u;
+    const bool in = j < R;
+    if (in) partial[w * (int64_t)kTileR + (j - j0)] = acc[u];
+    const unsigned m = __ballot_sync(0xffffffffu, in && ((started >> u) & 1u));  // all lanes, one call site
+    if (lane == 0) pmask[w * (int64_t)(kTileR / 32) + u] = m;
+  }
+  (void)mw;
+}
+
+// Warp per segment: add the pieces' partials in piece order into the
+// segment's running values for this column tile (first present value
+// assigns, later ones add), and accumulate the presence mask.
+__global__ void k_combine(int64_t nseg, const long long* __restrict__ poff, const double* __restrict__ partial,
+                          const uint32_t* __restrict__ pmask, int32_t R, int32_t j0, int32_t mw,
+                          double* __restrict__ segval, uint32_t* __restrict__ segmask) {
+  const int lane = threadIdx.x & 31;
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= nseg) return;
+  for (int u = 0; u < kJpl; u++) {
+    const int j = j0 + lane + 32 * u;
+    double v = 0.0;
+    bool have = false;
+    for (long long pc = poff[s]; pc < poff[s + 1]; pc++) {
+      const uint32_t m = pmask[pc * (kTileR / 32) + u];
+      if ((m >> lane) & 1u) {
+        const double x = partial[pc * (int64_t)kTileR + (j - j0)];
+        v = have ? __dadd_rn(v, x) : x;
+        have = true;
+      }
+    }
+    if (j < R) segval[s * (int64_t)R + j] = v;
+    const unsigned m = __ballot_sync(0xffffffffu, have && j < R);
+    if (lane == 0 && (j0 / 32 + u) < mw) segmask[s * (int64_t)mw + j0 / 32 + u] = m;
+  }
+}
+
+__global__ void k_seg_counts(int64_t nseg, const uint32_t* __restrict__ segmask, int32_t mw, int32_t* __restrict__ cnt) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  int c = 0;
+  for (int w = 0; w < mw; w++) c += __popc(segmask[s * (int64_t)mw + w]);
+  cnt[s] = c;
+}
+
+// Warp per segment: write (coordinates, value) for every present column.
+__global__ void k_write(int64_t nseg, int mode, const unsigned long long* __restrict__ skeys,
+                        const long long* __restrict__ starts, int32_t dim_leaf, const double* __restrict__ segval,
+                        const uint32_t* __restrict__ segmask, int32_t R, int32_t mw, const long long* __restrict__ off,
+                        int32_t* __restrict__ o0, int32_t* __restrict__ o1, int32_t* __restrict__ o2,
+                        double* __restrict__ ov) {
+  const int lane = threadIdx.x & 31;
+  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= nseg) return;
+  const unsigned long long key = skeys[starts[s]];
+  long long at = off[s];
+  for (int w = 0; w < mw; w++) {
+    const uint32_t m = segmask[s * (int64_t)mw + w];
+    const int j = w * 32 + lane;
+    if ((m >> lane) & 1u) {
+      const long long p = at + __popc(m & ((1u << lane) - 1u));
+      if (mode == 0) {
+        o0[p] = (int32_t)key;
+        o1[p] = j;
+      } else {
+        o0[p] = (int32_t)(key / (unsigned long long)dim_leaf);
+        o1[p] = (int32_t)(key % (unsigned long long)dim_leaf);
+        o2[p] = j;
+      }
+      ov[p] = segval[s * (int64_t)R + j];
+    }
+    at += __popc(m);
+  }
+}
+
+struct DevArr {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  ~DevArr() { dfree(p, s); }
+  template <typename T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+int alloc(DevArr& a, size_t bytes, cudaStream_t s) {
+  a.s = s;
+  return dalloc(&a.p, bytes ? bytes : 16, s);
+}
+
+}  // namespace
+
+int densify_factor(const DcsrDev& f, FactorDense* out, cudaStream_t s) {
+  out->rows = f.nrows;
+  out->R = f.ncols;
+  out->mw = std::max(1, (f.ncols + 31) / 32);
+  const size_t nd = (size_t)std::max(f.nrows, 1) * (size_t)std::max(f.ncols, 1);
+  const size_t nm = (size_t)std::max(f.nrows, 1) * (size_t)out->mw;
+  SPWS_TRY(dalloc((void**)&out->dense, sizeof(double) * nd, s));
+  SPWS_TRY(dalloc((void**)&out->mask, sizeof(uint32_t) * nm, s));
+  SPWS_CUDA(cudaMemsetAsync(out->dense, 0, sizeof(double) * nd, s));
+  SPWS_CUDA(cudaMemsetAsync(out->mask, 0, sizeof(uint32_t) * nm, s));
+  if (f.nq > 0) {
+    k_densify<<<(unsigned)((f.nq + 7) / 8), 256, 0, s>>>(f.nq, f.oc, f.pos, f.ic, f.vals, f.ncols, out->mw,
+                                                         out->dense, out->mask);
+    count_launch(1);
+  }
+  SPWS_CUDA(cudaGetLastError());
+  return SPWS_OK;
+}
+
+void free_factor(FactorDense* f, cudaStream_t s) {
+  dfree(f->dense, s);
+  dfree(f->mask, s);
+  f->dense = nullptr;
+  f->mask = nullptr;
+}
+
+int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const FactorDense* F1, CooOut* out,
+                  cudaStream_t s) {
+  const int64_t nnz = B.nnz;
+  const int32_t R = mode == 0 ? std::min(F0.R, F1->R) : F0.R;
+  const int32_t mw = std::max(1, (R + 31) / 32);
+  out->n = 0;
+  for (auto& c : out->crd) c = nullptr;
+  out->vals = nullptr;
+  DevArr fib_root, leaf_fib, k0, p0, k1, p1, r0, r1, bv, head, hpos, starts, pc, poff, pseg, pstart, partial, pmask,
+      segval, segmask, segcnt, segoff, tot;
+  SPWS_TRY(alloc(fib_root, sizeof(int32_t) * (size_t)B.nf, s));
+  SPWS_TRY(alloc(leaf_fib, sizeof(int32_t) * (size_t)nnz, s));
+  SPWS_TRY(alloc(tot, sizeof(long long), s));
+  if (B.nk > 0) {
+    k_fiber_root<<<(unsigned)((B.nk + 7) / 8), 256, 0, s>>>(B.nk, B.roots, B.pos1, fib_root.as<int32_t>());
+    count_launch(1);
+  }
+  if (B.nf > 0) {
+    k_leaf_fiber<<<(unsigned)((B.nf + 7) / 8), 256, 0, s>>>(B.nf, B.pos2, leaf_fib.as<int32_t>());
+    count_launch(1);
+  }
+  const size_t kb = sizeof(unsigned long long) * (size_t)std::max<int64_t>(nnz, 1);
+  SPWS_TRY(alloc(k0, kb, s));
+  SPWS_TRY(alloc(p0, kb, s));
+  SPWS_TRY(alloc(k1, kb, s));
+  SPWS_TRY(alloc(p1, kb, s));
+  const unsigned gn = (unsigned)((nnz + 255) / 256);
+  if (nnz > 0) {
+    k_keys<<<gn, 256, 0, s>>>(nnz, mode, B.crd2, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), B.d2,
+                              k0.as<unsigned long long>(), p0.as<unsigned long long>());
+    count_launch(1);
+  }
+  const unsigned long long keyspace =
+      mode == 0 ? (unsigned long long)std::max(B.d2, 1)
+                : (unsigned long long)std::max(B.d0, 1) * (unsigned long long)std::max(B.d2, 1);
+  bool in_tmp = false;
+  SPWS_TRY(radix_sort_pairs(k0.as<unsigned long long>(), p0.as<unsigned long long>(), k1.as<unsigned long long>(),
+                            p1.as<unsigned long long>(), nnz, bits_for(keyspace), &in_tmp, s));
+  const unsigned long long* sk = in_tmp ? k1.as<unsigned long long>() : k0.as<unsigned long long>();
+  const unsigned long long* perm = in_tmp ? p1.as<unsigned long long>() : p0.as<unsigned long long>();
+  SPWS_TRY(alloc(r0, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(alloc(r1, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(alloc(bv, sizeof(double) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(alloc(head, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(alloc(hpos, sizeof(long long) * (size_t)std::max<int64_t>(nnz, 1), s));
+  SPWS_TRY(alloc(starts, sizeof(long long) * ((size_t)nnz + 1), s));
+  if (nnz > 0) {
+    k_gather<<<gn, 256, 0, s>>>(nnz, mode, perm, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), B.crd1, B.vals,
+                                r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>());
+    k_heads<<<gn, 256, 0, s>>>(nnz, sk, head.as<int32_t>());
+    count_launch(2);
+  }
+  SPWS_TRY(scan_i32_to_i64(head.as<int32_t>(), hpos.as<long long>(), nnz, tot.as<long long>(), s));
+  if (nnz > 0) {
+    k_starts<<<gn, 256, 0, s>>>(nnz, head.as<int32_t>(), hpos.as<long long>(), starts.as<long long>());
+    count_launch(1);
+  }
+  long long nseg = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&nseg, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  const long long nnz_ll = nnz;
+  SPWS_CUDA(cudaMemcpyAsync(starts.as<long long>() + nseg, &nnz_ll, sizeof(long long), cudaMemcpyHostToDevice, s));
+
+  SPWS_TRY(alloc(pc, sizeof(int32_t) * (size_t)std::max<long long>(nseg, 1), s));
+  SPWS_TRY(alloc(poff, sizeof(long long) * ((size_t)nseg + 1), s));
+  const unsigned gs = (unsigned)((nseg + 255) / 256);
+  if (nseg > 0) {
+    k_piece_counts<<<gs, 256, 0, s>>>(nseg, starts.as<long long>(), pc.as<int32_t>());
+    count_launch(1);
+  }
+  SPWS_TRY(scan_i32_to_i64(pc.as<int32_t>(), poff.as<long long>(), nseg, tot.as<long long>(), s));
+  long long npieces = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&npieces, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  SPWS_CUDA(cudaMemcpyAsync(poff.as<long long>() + nseg, &npieces, sizeof(long long), cudaMemcpyHostToDevice, s));
+  SPWS_TRY(alloc(pseg, sizeof(int32_t) * (size_t)std::max<long long>(npieces, 1), s));
+  SPWS_TRY(alloc(pstart, sizeof(long long) * (size_t)std::max<long long>(npieces, 1), s));
+  if (nseg > 0) {
+    k_piece_fill<<<gs, 256, 0, s>>>(nseg, starts.as<long long>(), poff.as<long long>(), pseg.as<int32_t>(),
+                                    pstart.as<long long>());
+    count_launch(1);
+  }
+  SPWS_TRY(alloc(partial, sizeof(double) * (size_t)std::max<long long>(npieces, 1) * kTileR, s));
+  SPWS_TRY(alloc(pmask, sizeof(uint32_t) * (size_t)std::max<long long>(npieces, 1) * (kTileR / 32), s));
+  SPWS_TRY(alloc(segval, sizeof(double) * (size_t)std::max<long long>(nseg, 1) * std::max(R, 1), s));
+  SPWS_TRY(alloc(segmask, sizeof(uint32_t) * (size_t)std::max<long long>(nseg, 1) * mw, s));
+  Factor f0{F0.dense, F0.mask, F0.rows, F0.R, F0.mw};
+  Factor f1 = F1 ? Factor{F1->dense, F1->mask, F1->rows, F1->R, F1->mw} : f0;
+  for (int32_t j0 = 0; j0 < R; j0 += kTileR) {
+    if (npieces > 0) {
+      const unsigned gp = (unsigned)((npieces + 7) / 8);
+      if (mode == 0)
+        k_pieces<0><<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
+                                       r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw,
+                                       partial.as<double>(), pmask.as<uint32_t>());
+      else
+        k_pieces<1><<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
+                                       r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw,
+                                       partial.as<double>(), pmask.as<uint32_t>());
+      k_combine<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, poff.as<long long>(), partial.as<double>(),
+                                                           pmask.as<uint32_t>(), R, j0, mw, segval.as<double>(),
+                                                           segmask.as<uint32_t>());
+      count_launch(2);
+    }
+  }
+  SPWS_TRY(alloc(segcnt, sizeof(int32_t) * (size_t)std::max<long long>(nseg, 1), s));
+  SPWS_TRY(alloc(segoff, sizeof(long long) * (size_t)std::max<long long>(nseg, 1), s));
+  if (nseg > 0) {
+    k_seg_counts<<<gs, 256, 0, s>>>(nseg, segmask.as<uint32_t>(), mw, segcnt.as<int32_t>());
+    count_launch(1);
+  }
+  SPWS_TRY(scan_i32_to_i64(segcnt.as<int32_t>(), segoff.as<long long>(), nseg, tot.as<long long>(), s));
+  long long total = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&total, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  if (total > INT32_MAX) {
+    set_error("output has more than INT32_MAX nonzeros");
+    return SPWS_ERR_CAPACITY;
+  }
+  out->n = total;
+  const int ncrd = mode == 0 ? 2 : 3;
+  for (int d = 0; d < ncrd; d++) SPWS_TRY(dalloc((void**)&out->crd[d], sizeof(int32_t) * (size_t)std::max(total, 1LL), s));
+  SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max(total, 1LL), s));
+  if (nseg > 0) {
+    k_write<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, mode, sk, starts.as<long long>(), B.d2,
+                                                       segval.as<double>(), segmask.as<uint32_t>(), R, mw,
+                                                       segoff.as<long long>(), out->crd[0], out->crd[1],
+                                                       mode == 0 ? nullptr : out->crd[2], out->vals);
+    count_launch(1);
+  }
+  SPWS_CUDA(cudaGetLastError());
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  return SPWS_OK;
+}
+
+}  // namespace spws

@@ -1,0 +1,107 @@
+"""GPU parity of the outer-product (DCSC x DCSR: hash, bucket and coordinate
+workspaces), the CSR coordinate workspace and the transposed-output SpGEMM."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from _check import abs_csr, assert_csr_close, assert_csr_equal_structure
+from sparsews_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GOLDEN = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLD, "spgemm_*.npz"))
+                if "spgemm_t_" not in f)
+
+
+def csr(z, p):
+    n, m = (int(x) for x in z[p + "_shape"])
+    return z[p + "_pos"], z[p + "_crd"], z[p + "_vals"], n, m
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+@pytest.mark.parametrize("method", ["hash", "bucket", "coord"])
+def test_outer_golden(spws_lib, name, method):
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    A, B = csr(z, "A"), csr(z, "B")
+    got = sp.spgemm_outer(A, B, method)
+    key = {"hash": "outer_hash", "bucket": "outer_bucket", "coord": "outer_coord"}[method]
+    assert_csr_close(got, (z["pos"], z["crd"], z[key + "_vals"]), z["absprod_vals"], name)
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_coord_is_j_ordered_bit_exact(spws_lib, name):
+    """The coordinate workspace sums each entry left to right over j, as the
+    reference's TACO kernel does (CSR_CSR_taco.h:56-89): bit-exact."""
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    A, B = csr(z, "A"), csr(z, "B")
+    got = sp.spgemm(A, B, method="coord")
+    assert_csr_equal_structure(got, (z["pos"], z["crd"]), name)
+    assert np.array_equal(got[2], z["taco_vals"])
+
+
+@pytest.mark.parametrize("case", ["er", "rmat", "band"])
+def test_coord_against_oracle(spws_lib, case):
+    import sparsews_gb300 as sp
+    A = {"er": lambda: gen.er(2000, 9, seed=61), "rmat": lambda: gen.rmat(12, 8, seed=62),
+         "band": lambda: gen.band(30000, 8, 0.5, seed=63)}[case]()
+    got = sp.spgemm(A, A, method="coord")
+    ref = oracle.spgemm("taco", A, A)
+    assert_csr_equal_structure(got, ref, case)
+    assert np.array_equal(got[2], ref[2])
+    got_o = sp.spgemm_outer(A, A, "coord")
+    assert np.array_equal(got_o[2], ref[2])
+
+
+def test_outer_against_oracle_rmat(spws_lib):
+    import sparsews_gb300 as sp
+    A = gen.rmat(12, 10, seed=64)
+    ref = oracle.spgemm("outer_bucket", A, A)
+    scale = oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2]
+    for m in ("hash", "bucket"):
+        assert_csr_close(sp.spgemm_outer(A, A, m), ref, scale, m)
+
+
+def test_transposed_golden(spws_lib):
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, "spgemm_t_er100.npz"))
+    A, B = csr(z, "A"), csr(z, "B")
+    got, coll = sp.spgemm_t(A, B)
+    ref = (z["t_pos"], z["t_crd"], z["t_vals"])
+    At = (np.abs(A[2]))
+    scale = oracle.spgemm_t((A[0], A[1], np.abs(A[2]), A[3], A[4]), (B[0], B[1], np.abs(B[2]), B[3], B[4]))[0][2]
+    assert_csr_close(got, ref, scale, "t")
+    assert coll == int(z["t_collisions"])  # the golden run never refreshed its buffer
+
+
+def test_transposed_against_oracle(spws_lib):
+    import sparsews_gb300 as sp
+    A = gen.rmat(11, 6, seed=65)
+    B = gen.rmat(11, 7, seed=66)
+    got, coll = sp.spgemm_t(A, B)
+    (rp, rc, rv), rcoll = oracle.spgemm_t(A, B, w_cap=1 << 22)
+    scale = oracle.spgemm_t(abs_csr(A), abs_csr(B), w_cap=1 << 22)[0][2]
+    assert_csr_close(got, (rp, rc, rv), scale, "t")
+    assert coll == rcoll
+    # C^T is the transpose of A*B
+    C = oracle.spgemm("taco", A, B)
+    tp, tc, tv = sp._csr_transpose_np(C[0], C[1], C[2], A[3], B[4])
+    assert np.array_equal(tp, got[0]) and np.array_equal(tc, got[1])
+
+
+def test_outer_rejects_malformed(spws_lib):
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import taco
+    A = gen.er(40, 3, seed=67)
+    tp, tc, tv = sp._csr_transpose_np(*A)
+    bad_c = tc.copy()
+    bad_c[0] = 40  # row index out of range in the DCSC inner level
+    At = taco.dcsc(tp, bad_c, tv, 40, 40)
+    Bt = taco.dcsr(A[0], A[1], A[2], 40, 40)
+    Ct = taco.init_dc(40, 40)
+    L = sp.lib()
+    assert L.spws_dcsc_dcsr_hash_compute(Ct.ptr(), At.ptr(), Bt.ptr(), 0) == 1

@@ -1,0 +1,113 @@
+"""GPU parity of MTTKRP and TTM (bucket kernel behind the hash, bucket and
+coordinate entry points) against the reference's golden vectors and the
+oracle. A bucket handled by one warp sums in the reference's loop order, so
+the values are bit-exact whenever the reference itself did not split a sum
+(no workspace flush); the oracle is run with a capacity that never flushes."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from _check import assert_vals_close
+from sparsews_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+BIG = 1 << 26  # oracle capacity that never flushes at these sizes
+
+
+def csr(z, p):
+    n, m = (int(x) for x in z[p + "_shape"])
+    return z[p + "_pos"], z[p + "_crd"], z[p + "_vals"], n, m
+
+
+def abs_f(F):
+    return F[0], F[1], np.abs(F[2]), F[3], F[4]
+
+
+@pytest.mark.parametrize("R", [4, 16])
+@pytest.mark.parametrize("method", ["hash", "bucket"])
+def test_mttkrp_golden(spws_lib, R, method):
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, f"mttkrp_R{R}_s17.npz"))
+    dims = tuple(int(x) for x in z["dims"])
+    Bc = (z["B_c0"], z["B_c1"], z["B_c2"], z["B_vals"])
+    (i, j), v = sp.mttkrp(Bc, dims, csr(z, "C"), csr(z, "D"), method)
+    assert np.array_equal(i, z["hash_i"]) and np.array_equal(j, z["hash_j"])
+    assert np.array_equal(v, z["hash_vals"])  # golden hash run never flushed: bit-exact
+    assert np.array_equal(v, z["bucket_vals"])
+
+
+@pytest.mark.parametrize("method", ["hash", "bucket"])
+def test_ttm_golden(spws_lib, method):
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, "ttm_R4_s17.npz"))
+    dims = tuple(int(x) for x in z["dims"])
+    Bc = (z["B_c0"], z["B_c1"], z["B_c2"], z["B_vals"])
+    (k, j, l), v = sp.ttm(Bc, dims, csr(z, "C"), method)
+    for a, name in ((k, "k"), (j, "j"), (l, "l")):
+        assert np.array_equal(a, z["hash_" + name])
+    assert np.array_equal(v, z["hash_vals"])
+
+
+@pytest.mark.parametrize("R", [16, 32, 64, 300])
+def test_mttkrp_against_oracle(spws_lib, R):
+    import sparsews_gb300 as sp
+    i0, i1, i2, tv = gen.tensor3((3000, 800, 400), 60000, zipf_s=1.1, seed=71)
+    dims = (800, 400, 3000)
+    Cf, Df = gen.dense_factor(800, R, seed=72), gen.dense_factor(400, R, seed=73)
+    Bc = (i1, i2, i0, tv)
+    (gi, gj), gv = sp.mttkrp(Bc, dims, Cf, Df)
+    (ri, rj), rv = oracle.mttkrp("hash", Bc, dims, Cf, Df, w_cap=BIG)
+    assert np.array_equal(gi, ri) and np.array_equal(gj, rj)
+    (_, _), scale = oracle.mttkrp("hash", (i1, i2, i0, np.abs(tv)), dims, abs_f(Cf), abs_f(Df), w_cap=BIG)
+    assert_vals_close(gv, rv, scale, "mttkrp")
+
+
+def test_mttkrp_sparse_factors(spws_lib):
+    """Factors with missing entries: products exist only where C(k,j) and
+    D(l,j) both exist (the reference's co-iteration, hash_free.h:300-323)."""
+    import sparsews_gb300 as sp
+    i0, i1, i2, tv = gen.tensor3((200, 90, 70), 5000, seed=74)
+    dims = (90, 70, 200)
+    Cf = gen.poisson_rows(90, 6.0, seed=75)
+    Cf = (Cf[0], Cf[1] % 20, Cf[2], 90, 20)
+    rows = np.repeat(np.arange(90), np.diff(Cf[0]))
+    key = np.unique(rows.astype(np.int64) * 20 + Cf[1])
+    r, c = key // 20, key % 20
+    pos = np.zeros(91, np.int64)
+    np.add.at(pos, r + 1, 1)
+    Cf = (np.cumsum(pos).astype(np.int32), c.astype(np.int32), np.linspace(-1, 1, len(c)), 90, 20)
+    Df = gen.dense_factor(70, 20, seed=76)
+    Bc = (i1, i2, i0, tv)
+    (gi, gj), gv = sp.mttkrp(Bc, dims, Cf, Df)
+    (ri, rj), rv = oracle.mttkrp("hash", Bc, dims, Cf, Df, w_cap=BIG)
+    assert np.array_equal(gi, ri) and np.array_equal(gj, rj)
+    (_, _), scale = oracle.mttkrp("hash", (i1, i2, i0, np.abs(tv)), dims, abs_f(Cf), abs_f(Df), w_cap=BIG)
+    assert_vals_close(gv, rv, scale, "mttkrp sparse")
+
+
+@pytest.mark.parametrize("R", [8, 32])
+def test_ttm_against_oracle(spws_lib, R):
+    import sparsews_gb300 as sp
+    i0, i1, i2, tv = gen.tensor3((500, 400, 300), 40000, zipf_s=1.1, seed=77)
+    dims = (500, 300, 400)
+    Cf = gen.dense_factor(300, R, seed=78)
+    Bc = (i0, i2, i1, tv)
+    (gk, gj, gl), gv = sp.ttm(Bc, dims, Cf)
+    (rk, rj, rl), rv = oracle.ttm("hash", Bc, dims, Cf, w_cap=BIG)
+    assert np.array_equal(gk, rk) and np.array_equal(gj, rj) and np.array_equal(gl, rl)
+    assert np.array_equal(gv, rv)  # no bucket is split at this size: bit-exact
+
+
+def test_tensor_empty_and_invalid(spws_lib):
+    import sparsews_gb300 as sp
+    empty = (np.zeros(0, np.int32),) * 3 + (np.zeros(0),)
+    (i, j), v = sp.mttkrp(empty, (5, 6, 7), gen.dense_factor(5, 4), gen.dense_factor(6, 4))
+    assert len(v) == 0
+    i0, i1, i2, tv = gen.tensor3((20, 10, 8), 300, seed=79)
+    bad = (i1, i2, i0.copy(), tv)
+    bad[2][0] = 25  # leaf coordinate beyond its dimension
+    with pytest.raises(sp.SpwsError):
+        sp.mttkrp(bad, (10, 8, 20), gen.dense_factor(10, 4), gen.dense_factor(8, 4))
