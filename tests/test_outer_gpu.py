@@ -75,7 +75,12 @@ def test_transposed_golden(spws_lib):
     At = (np.abs(A[2]))
     scale = oracle.spgemm_t((A[0], A[1], np.abs(A[2]), A[3], A[4]), (B[0], B[1], np.abs(B[2]), B[3], B[4]))[0][2]
     assert_csr_close(got, ref, scale, "t")
-    assert coll == int(z["t_collisions"])  # the golden run never refreshed its buffer
+    # the GPU counts products landing on an entry already present (products -
+    # nnz); the reference's counter equals that only when its buffer never
+    # refreshes, which its default capacity does not guarantee
+    (_, _, _), coll_norefresh = oracle.spgemm_t(A, B, w_cap=1 << 22)
+    assert coll == coll_norefresh
+    assert coll >= int(z["t_collisions"])
 
 
 def test_transposed_against_oracle(spws_lib):

@@ -29,14 +29,20 @@ def abs_f(F):
 @pytest.mark.parametrize("R", [4, 16])
 @pytest.mark.parametrize("method", ["hash", "bucket"])
 def test_mttkrp_golden(spws_lib, R, method):
+    """Against the reference's own output. Its small default capacity flushes
+    the workspace, which splits some sums, so values are compared within the
+    tolerance; against the never-flushing sequential order they are bit-exact."""
     import sparsews_gb300 as sp
     z = np.load(os.path.join(GOLD, f"mttkrp_R{R}_s17.npz"))
     dims = tuple(int(x) for x in z["dims"])
     Bc = (z["B_c0"], z["B_c1"], z["B_c2"], z["B_vals"])
-    (i, j), v = sp.mttkrp(Bc, dims, csr(z, "C"), csr(z, "D"), method)
+    Cf, Df = csr(z, "C"), csr(z, "D")
+    (i, j), v = sp.mttkrp(Bc, dims, Cf, Df, method)
     assert np.array_equal(i, z["hash_i"]) and np.array_equal(j, z["hash_j"])
-    assert np.array_equal(v, z["hash_vals"])  # golden hash run never flushed: bit-exact
-    assert np.array_equal(v, z["bucket_vals"])
+    (_, _), scale = oracle.mttkrp("hash", (Bc[0], Bc[1], Bc[2], np.abs(Bc[3])), dims, abs_f(Cf), abs_f(Df), w_cap=BIG)
+    assert_vals_close(v, z[method + "_vals"], scale, "mttkrp golden")
+    (_, _), seq = oracle.mttkrp("hash", Bc, dims, Cf, Df, w_cap=BIG)
+    assert np.array_equal(v, seq)
 
 
 @pytest.mark.parametrize("method", ["hash", "bucket"])
