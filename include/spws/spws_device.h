@@ -58,6 +58,32 @@ int spws_csr_release(spws_csr_dev* m);
 int spws_spgemm_csr_device(const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C, int accum_mode,
                            spws_spgemm_stats* stats);
 
+/* Row-wise SpGEMM C = A*B that allocates no memory, for callers that cannot
+ * call cudaMalloc: a library embedded in a host framework that owns the GPU's
+ * memory through its own pool (a foreign cudaMalloc would bypass the pool's
+ * budget or fail once the pool holds the memory), or a latency-critical loop
+ * in which an allocation (cudaMalloc can synchronise the whole device) is not
+ * allowed. It has no counterpart in the reference, whose kernels run on the
+ * CPU and allocate with malloc.
+ *
+ * Limit: its scratch is one fixed device array of about 6 MiB, sized for A
+ * with at most 262144 rows; a larger A is rejected with SPWS_ERR_CAPACITY.
+ * Every GPU that loads the library holds that array until the process exits.
+ * The first call on a device looks up the array's device address with that
+ * device current; make that first call before any stream capture. All calls
+ * share the array and find the previous call's contents in it (the call
+ * clears what must start at zero), so calls whose GPU work overlaps race:
+ * issue them one at a time per device.
+ *
+ * A, B: device CSR operands (e.g. from spws_csr_upload). The caller allocates
+ * C in device memory: C_pos with A->nrows + 1 ints, C_crd and C_vals with room
+ * for c_cap entries. *c_nnz receives C's nonzero count; if it exceeds c_cap the
+ * call returns SPWS_ERR_CAPACITY with C_pos and *c_nnz already written, so the
+ * caller can size C and call again. The work runs on the calling thread's
+ * per-thread default stream and the call returns when it has finished. */
+int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev* B, int32_t* C_pos, int32_t* C_crd,
+                            double* C_vals, int64_t c_cap, int64_t* c_nnz);
+
 /* Make `device` current for the calling thread (cudaSetDevice). */
 int spws_set_device(int device);
 

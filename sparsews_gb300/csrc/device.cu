@@ -189,3 +189,38 @@ extern "C" int spws_set_device(int device) {
   SPWS_CUDA(cudaSetDevice(device));
   return SPWS_OK;
 }
+
+namespace spws {
+
+// validate_csr_device with the violation flag at a caller-provided device
+// address `bad` (one int) instead of a pool allocation. Synchronises `s`.
+int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
+                             const char* what, int* bad, cudaStream_t s) {
+  if (nrows < 0 || ncols < 0 || nnz < 0 || nnz > INT32_MAX) {
+    set_error(std::string(what) + ": negative or oversized dimensions");
+    return SPWS_ERR_INVALID;
+  }
+  int32_t ends[2] = {0, 0};
+  SPWS_CUDA(cudaMemcpyAsync(&ends[0], pos, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&ends[1], pos + nrows, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  if (nrows > 0) {
+    k_validate_csr<<<(unsigned)((nrows + 7) / 8), 256, 0, s>>>(nrows, nnz, ncols, pos, crd, bad);
+    count_launch(1);
+    SPWS_CUDA(cudaGetLastError());
+  }
+  int hbad = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  if (ends[0] != 0 || (int64_t)ends[1] != nnz) {
+    set_error(std::string(what) + ": pos[0] must be 0 and pos[nrows] must equal nnz");
+    return SPWS_ERR_INVALID;
+  }
+  if (hbad) {
+    set_error(std::string(what) + ": positions not monotone, or columns out of range / not strictly increasing");
+    return SPWS_ERR_INVALID;
+  }
+  return SPWS_OK;
+}
+
+}  // namespace spws

@@ -118,3 +118,25 @@ int scan_counts_i32(const int32_t* counts, int32_t* out, int64_t n, long long* t
 }
 
 }  // namespace spws
+
+namespace spws {
+
+// Same scan as scan_counts_i32, with the per-tile sums kept in `tile_scratch`
+// (at least ceil(n / 2048) entries) instead of a pool allocation.
+int scan_counts_i32_into(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev,
+                         long long* tile_scratch, cudaStream_t s) {
+  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  if (ntiles == 0) {
+    SPWS_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), s));
+    SPWS_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(long long), s));
+    return SPWS_OK;
+  }
+  k_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile_scratch);
+  k_scan_tile_sums<<<1, kScanThreads, 0, s>>>(tile_scratch, ntiles, total_dev);
+  k_tile_scan<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile_scratch, out, total_dev);
+  count_launch(3);
+  SPWS_CUDA(cudaGetLastError());
+  return SPWS_OK;
+}
+
+}  // namespace spws

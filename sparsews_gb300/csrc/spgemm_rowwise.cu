@@ -135,11 +135,15 @@ struct PassArgs {
   int* err;            // set on internal inconsistency
 };
 
-// Shared staging of one batch of j's: the B-row slice each thread loaded and
-// the exclusive prefix of slice lengths.
+constexpr int kPieceLen = 256;  // B entries per warp work piece
+
+// Shared staging of one batch of j's: the B-row slice each thread loaded
+// (start, length), its A value, and the exclusive prefix of the number of
+// pieces of at most kPieceLen entries each slice is cut into.
 struct Batch {
   int32_t s[kThreads];
-  int32_t excl[kThreads + 1];
+  int32_t len[kThreads];
+  int32_t pexcl[kThreads + 1];
   double a[kThreads];
 };
 
@@ -173,8 +177,8 @@ __device__ __forceinline__ int32_t span_end(int32_t wlo) {
 
 // Loads batch [qb, qb + kThreads) of row i's A entries into `b`: the B-row
 // slice limited to columns in [clo, chi) when `clip` is set (found by binary
-// search in the sorted B row), else the whole B row. Returns the batch total;
-// `b.excl` holds the prefix. Ends with a barrier.
+// search in the sorted B row), else the whole B row. Returns the number of
+// pieces; `b.pexcl` holds their prefix. Ends with a barrier.
 __device__ __forceinline__ int load_batch(const PassArgs& a, int32_t qb, int32_t q1, bool want_a, bool clip,
                                           int32_t clo, int32_t chi, Batch& b, int* wsum) {
   const int32_t q = qb + threadIdx.x;
@@ -202,32 +206,35 @@ __device__ __forceinline__ int load_batch(const PassArgs& a, int32_t qb, int32_t
     len = e - s;
     if (want_a) av = __ldg(a.Av + q);
   }
-  int total;
-  const int ex = block_excl_scan(len, wsum, &total);
+  int npieces;
+  const int ex = block_excl_scan((len + kPieceLen - 1) / kPieceLen, wsum, &npieces);
   b.s[threadIdx.x] = s;
-  b.excl[threadIdx.x] = ex;
+  b.len[threadIdx.x] = len;
+  b.pexcl[threadIdx.x] = ex;
   b.a[threadIdx.x] = av;
-  if (threadIdx.x == 0) b.excl[kThreads] = total;
+  if (threadIdx.x == 0) b.pexcl[kThreads] = npieces;
   __syncthreads();
-  return total;
+  return npieces;
 }
 
-// Calls f(position in B, A value) for the flat entries t, t+kThreads, ... of
-// the batch. The owner slice of the first entry is found by binary search,
-// later ones by walking forward.
+// Calls f(position in B, A value) for every entry of the batch. Warps take
+// the batch's pieces round-robin (pieces hold at most kPieceLen entries of one
+// slice, so the split is even up to the last piece) and their lanes stream a
+// piece with unit stride, so loads of B are coalesced.
 template <typename F>
-__device__ __forceinline__ void for_batch_entries(const Batch& b, int total, F&& f) {
-  int fidx = threadIdx.x;
-  if (fidx >= total) return;
-  int lo = 0, hi = kThreads - 1;  // largest o with excl[o] <= fidx
-  while (lo < hi) {
-    const int m = (lo + hi + 1) >> 1;
-    if (b.excl[m] <= fidx) lo = m; else hi = m - 1;
-  }
-  int o = lo;
-  for (; fidx < total; fidx += kThreads) {
-    while (b.excl[o + 1] <= fidx) o++;
-    f(b.s[o] + (fidx - b.excl[o]), b.a[o]);
+__device__ __forceinline__ void for_batch_entries(const Batch& b, int npieces, F&& f) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int g = warp; g < npieces; g += kWarps) {
+    int lo = 0, hi = kThreads - 1;  // slice owning piece g: largest o with pexcl[o] <= g
+    while (lo < hi) {
+      const int m = (lo + hi + 1) >> 1;
+      if (b.pexcl[m] <= g) lo = m; else hi = m - 1;
+    }
+    const int first = (g - b.pexcl[lo]) * kPieceLen;
+    const int32_t p0 = b.s[lo] + first;
+    const int32_t p1 = b.s[lo] + min(b.len[lo], first + kPieceLen);
+    const double av = b.a[lo];
+    for (int32_t p = p0 + lane; p < p1; p += 32) f(p, av);
   }
 }
 
@@ -640,3 +647,180 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
 }
 
 }  // namespace spws
+
+// ---------------------------------------------------------------------------
+// spws_spgemm_csr_noalloc: the row-wise SpGEMM for callers that must not
+// allocate device memory. Its scratch lives in one file-scope device array of
+// fixed size; the caller passes C's arrays. See include/spws/spws_device.h.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+#include "validate.h"
+
+namespace spws {
+namespace {
+
+constexpr int64_t kNoAllocMaxRows = int64_t(1) << 18;  // rows of A the array is sized for
+constexpr size_t kNoAllocHead = 1024;                   // counters, flags, totals
+constexpr size_t kNoAllocTiles = (size_t)((kNoAllocMaxRows + 2047) / 2048);
+constexpr size_t kNoAllocBytes = kNoAllocHead + sizeof(RowInfo) * kNoAllocMaxRows +
+                                 2 * sizeof(int32_t) * kNoAllocMaxRows + sizeof(long long) * kNoAllocTiles;
+
+struct NoAllocHead {
+  int hist[kBuckets];
+  int cursor[kBuckets];
+  int nwork;
+  int nheavy;
+  int counter[4];
+  int err;
+  int bad;
+  unsigned long long products;
+  long long nnz;
+};
+static_assert(sizeof(NoAllocHead) <= kNoAllocHead, "head block too small");
+
+// The scratch itself: about 6 MiB, held by every device that loads the
+// library until the process exits. Host code must not use this name as an
+// address; it gets the device address from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (the caller's first call on a device does this).
+int noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  SPWS_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("device ordinal out of range");
+    return SPWS_ERR_NO_DEVICE;
+  }
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      (void)cudaGetLastError();
+      set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch) failed: ") + cudaGetErrorString(e));
+      return SPWS_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  return SPWS_OK;
+}
+
+}  // namespace
+}  // namespace spws
+
+extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev* B, int32_t* C_pos, int32_t* C_crd,
+                                       double* C_vals, int64_t c_cap, int64_t* c_nnz) {
+  using namespace spws;
+  clear_error();
+  if (!A || !B || !C_pos || !c_nnz || c_cap < 0 || (c_cap > 0 && (!C_crd || !C_vals))) {
+    set_error("spws_spgemm_csr_noalloc: null output or negative capacity");
+    return SPWS_ERR_INVALID;
+  }
+  *c_nnz = 0;
+  if (A->ncols != B->nrows || A->nrows < 0) {
+    set_error("spws_spgemm_csr_noalloc: A's column count must equal B's row count");
+    return SPWS_ERR_INVALID;
+  }
+  if ((int64_t)A->nrows > kNoAllocMaxRows) {
+    set_error("spws_spgemm_csr_noalloc: A has more than 262144 rows, the size of its fixed scratch");
+    return SPWS_ERR_CAPACITY;
+  }
+  unsigned char* base = nullptr;
+  SPWS_TRY(noalloc_scratch(&base));
+  NoAllocHead* hd = reinterpret_cast<NoAllocHead*>(base);
+  RowInfo* info = reinterpret_cast<RowInfo*>(base + kNoAllocHead);
+  int32_t* order = reinterpret_cast<int32_t*>(info + kNoAllocMaxRows);
+  int32_t* rowcnt = order + kNoAllocMaxRows;
+  long long* tiles = reinterpret_cast<long long*>(rowcnt + kNoAllocMaxRows);
+
+  const cudaStream_t s = cudaStreamPerThread;
+  const int32_t nA = A->nrows;
+  SPWS_TRY(validate_csr_device_flag(A->pos, A->crd, A->nrows, A->ncols, A->nnz, "A", &hd->bad, s));
+  if (B != A) SPWS_TRY(validate_csr_device_flag(B->pos, B->crd, B->nrows, B->ncols, B->nnz, "B", &hd->bad, s));
+  if (nA == 0) {
+    SPWS_CUDA(cudaMemsetAsync(C_pos, 0, sizeof(int32_t), s));
+    SPWS_CUDA(cudaStreamSynchronize(s));
+    return SPWS_OK;
+  }
+  // the array keeps the previous call's contents: clear what must start at zero
+  SPWS_CUDA(cudaMemsetAsync(hd, 0, sizeof(NoAllocHead), s));
+  SPWS_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int32_t) * (size_t)nA, s));
+
+  int dev = 0, sms = 1;
+  SPWS_CUDA(cudaGetDevice(&dev));
+  SPWS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+
+  k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A->pos, A->crd, B->pos, B->crd, info, hd->hist,
+                                                      &hd->products, &hd->err);
+  k_order_offsets<<<1, 32, 0, s>>>(hd->hist, hd->cursor, &hd->nwork, &hd->nheavy);
+  k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, hd->cursor, order);
+  count_launch(3);
+  SPWS_CUDA(cudaGetLastError());
+
+  PassArgs pa{};
+  pa.Ap = A->pos;
+  pa.Aj = A->crd;
+  pa.Av = A->vals;
+  pa.Bp = B->pos;
+  pa.Bk = B->crd;
+  pa.Bv = B->vals;
+  pa.info = info;
+  pa.order = order;
+  pa.nwork = &hd->nwork;
+  pa.nheavy = &hd->nheavy;
+  pa.counter = &hd->counter[0];
+  pa.light_counter = &hd->counter[2];
+  pa.rowcnt = rowcnt;
+  pa.err = &hd->err;
+  SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
+  SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
+  SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
+  SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
+  int per_sym = 1, per_num = 1, per_ls = 1, per_ln = 1;
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sym, k_symbolic, kThreads, kSymSmem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_num, k_numeric, kThreads, kNumSmem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ls, k_light<false>, kLightWarps * 32, kLightSymSmem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ln, k_light<true>, kLightWarps * 32, kLightNumSmem));
+  k_symbolic<<<sms * std::max(per_sym, 1), kThreads, kSymSmem, s>>>(pa);
+  k_light<false><<<sms * std::max(per_ls, 1), kLightWarps * 32, kLightSymSmem, s>>>(pa);
+  count_launch(2);
+  SPWS_CUDA(cudaGetLastError());
+  SPWS_TRY(scan_counts_i32_into(rowcnt, C_pos, nA, &hd->nnz, tiles, s));
+
+  long long nnz = 0;
+  int err = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&nnz, &hd->nnz, sizeof(nnz), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&err, &hd->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  *c_nnz = nnz;
+  if (err == 2) {
+    set_error("a row of A has 2^31 or more products");
+    return SPWS_ERR_CAPACITY;
+  }
+  if (nnz > c_cap) {
+    set_error("C's capacity is smaller than its nonzero count (C_pos and *c_nnz are filled in)");
+    return SPWS_ERR_CAPACITY;
+  }
+  pa.counter = &hd->counter[1];
+  pa.light_counter = &hd->counter[3];
+  pa.Cp = C_pos;
+  pa.Ck = C_crd;
+  pa.Cv = C_vals;
+  k_numeric<<<sms * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
+  k_light<true><<<sms * std::max(per_ln, 1), kLightWarps * 32, kLightNumSmem, s>>>(pa);
+  count_launch(2);
+  SPWS_CUDA(cudaGetLastError());
+  SPWS_CUDA(cudaMemcpyAsync(&err, &hd->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  if (err) {
+    set_error("numeric pass wrote a different number of entries than the symbolic pass counted");
+    return SPWS_ERR_CUDA;
+  }
+  return SPWS_OK;
+}

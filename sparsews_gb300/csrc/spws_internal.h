@@ -77,5 +77,8 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
 // the total also returned through `total_dev` (int64, device) so callers can
 // detect overflow of int32 positions.
 int scan_counts_i32(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev, cudaStream_t s);
+// The same scan with its per-tile sums in caller-provided scratch (ceil(n/2048) entries).
+int scan_counts_i32_into(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev,
+                         long long* tile_scratch, cudaStream_t s);
 
 }  // namespace spws

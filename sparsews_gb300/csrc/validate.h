@@ -8,4 +8,7 @@ namespace spws {
 // columns in [0, ncols) and strictly increasing per row. Synchronises `s`.
 int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
                         const char* what, cudaStream_t s);
+// Same checks with the violation flag at a caller-provided device int.
+int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
+                             const char* what, int* bad, cudaStream_t s);
 }  // namespace spws
