@@ -39,7 +39,9 @@ constexpr int kSpanBits = 1 << 18;            // columns one bitmap covers
 constexpr int kSpanWords = kSpanBits / 32;    // 8192
 constexpr int kGroupWords = 2048;             // words per 32-bit prefix base (65536 bits)
 constexpr int kGroups = kSpanWords / kGroupWords;
-constexpr int kAcc = 6144;                    // ranks per numeric window (48 KB of FP64)
+constexpr int kAcc = 5120;                    // ranks per numeric window (40 KB of FP64)
+constexpr int kBoundInts = 2048;              // shared table of per-(j, window) slice bounds
+constexpr int kMaxWin = 64;                   // windows per span with precomputed bounds
 constexpr int kBuckets = 66;                  // cost buckets: 0 = no products, b = 1 + floor(log2(P))
 constexpr int kLightBucket = 9;               // rows with bucket <= 9 (fewer than 512 products) go to k_light
 constexpr int kLightMax = 512;                // staging entries per warp in k_light
@@ -217,12 +219,15 @@ __device__ __forceinline__ int load_batch(const PassArgs& a, int32_t qb, int32_t
   return npieces;
 }
 
-// Calls f(position in B, A value) for every entry of the batch. Warps take
+// Calls f(column, B value, A value) for every entry of the batch. Warps take
 // the batch's pieces round-robin (pieces hold at most kPieceLen entries of one
 // slice, so the split is even up to the last piece) and their lanes stream a
-// piece with unit stride, so loads of B are coalesced.
-template <typename F>
-__device__ __forceinline__ void for_batch_entries(const Batch& b, int npieces, F&& f) {
+// piece with unit stride, so loads of B are coalesced. Each lane loads four
+// entries (column and, when VALS, value) before it uses any of them, so four
+// loads per lane are in flight per round trip.
+template <bool VALS, typename F>
+__device__ __forceinline__ void for_batch_entries(const Batch& b, int npieces, const int32_t* __restrict__ Bk,
+                                                  const double* __restrict__ Bv, F&& f) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int g = warp; g < npieces; g += kWarps) {
     int lo = 0, hi = kThreads - 1;  // slice owning piece g: largest o with pexcl[o] <= g
@@ -234,7 +239,19 @@ __device__ __forceinline__ void for_batch_entries(const Batch& b, int npieces, F
     const int32_t p0 = b.s[lo] + first;
     const int32_t p1 = b.s[lo] + min(b.len[lo], first + kPieceLen);
     const double av = b.a[lo];
-    for (int32_t p = p0 + lane; p < p1; p += 32) f(p, av);
+    for (int32_t base = p0 + lane; base < p1; base += 128) {
+      int32_t col[4];
+      double bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int32_t p = base + 32 * u;
+        col[u] = p < p1 ? __ldg(Bk + p) : -1;
+        if (VALS) bv[u] = p < p1 ? __ldg(Bv + p) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (col[u] >= 0) f(col[u], VALS ? bv[u] : 0.0, av);
+    }
   }
 }
 
@@ -244,8 +261,8 @@ __device__ __forceinline__ void build_bitmap(const PassArgs& a, int32_t q0, int3
                                              uint32_t* bm, Batch& b, int* wsum) {
   for (int32_t qb = q0; qb < q1; qb += kThreads) {
     const int total = load_batch(a, qb, q1, false, clip, wlo, clip ? span_end(wlo) : INT_MAX, b, wsum);
-    for_batch_entries(b, total, [&](int32_t p, double) {
-      const int k = __ldg(a.Bk + p) - wlo;
+    for_batch_entries<false>(b, total, a.Bk, a.Bv, [&](int32_t col, double, double) {
+      const int k = col - wlo;
       atomicOr(&bm[k >> 5], 1u << (k & 31));
     });
     __syncthreads();
@@ -301,10 +318,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
   uint32_t* bm = reinterpret_cast<uint32_t*>(smem + sizeof(double) * kAcc);  // kSpanWords
   uint16_t* wpre = reinterpret_cast<uint16_t*>(bm + kSpanWords);             // kSpanWords
   Batch& b = *reinterpret_cast<Batch*>(reinterpret_cast<unsigned char*>(wpre + kSpanWords));
+  int32_t* bnd = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(&b) + sizeof(Batch));  // kBoundInts
   __shared__ uint32_t gbase[kGroups];
   __shared__ int wsum[kWarps];
   __shared__ int s_idx;
   __shared__ int32_t s_cols[2];
+  __shared__ int32_t s_wcol[kMaxWin + 1];
   for (int q = threadIdx.x; q < kAcc; q += kThreads) acc[q] = 0.0;
   const int nwork = *a.nheavy;
   for (;;) {
@@ -323,17 +342,35 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
       __syncthreads();
       build_bitmap(a, q0, q1, wlo, multi, bm, b, wsum);
 
-      // per-word prefix of set bits; thread t owns a contiguous run of words
-      const int per = (nw + kThreads - 1) / kThreads;
-      const int w0 = min(nw, (int)threadIdx.x * per), w1 = min(nw, w0 + per);
-      int c = 0;
-      for (int w = w0; w < w1; w++) c += __popc(bm[w]);
+      // Per-word prefix of set bits and the row's columns in order. Warp w
+      // owns a contiguous chunk of words and walks it 32 words at a time, one
+      // word per lane, so its C.crd stores are contiguous across the warp.
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      const int chunk = (nw + kWarps - 1) / kWarps;
+      const int c0 = min(nw, warp * chunk), c1 = min(nw, c0 + chunk);
+      int wc = 0;
+      for (int w = c0 + lane; w < c1; w += 32) wc += __popc(bm[w]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, o);
       int nnz_w;
-      int run = block_excl_scan(c, wsum, &nnz_w);
-      for (int w = w0; w < w1; w++) {
-        if ((w & (kGroupWords - 1)) == 0) gbase[w / kGroupWords] = (uint32_t)run;
-        wpre[w] = (uint16_t)run;
-        run += __popc(bm[w]);
+      int run = block_excl_scan(lane == 0 ? wc : 0, wsum, &nnz_w);  // prefix of warp totals
+      run = __shfl_sync(0xffffffffu, run, 0);
+      for (int wb = c0; wb < c1; wb += 32) {
+        const int w = wb + lane;
+        const uint32_t word = w < c1 ? bm[w] : 0u;
+        const int pc = __popc(word);
+        int incl = pc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int pre = run + incl - pc;
+        if (w < c1) {
+          if ((w & (kGroupWords - 1)) == 0) gbase[w / kGroupWords] = (uint32_t)pre;
+          wpre[w] = (uint16_t)pre;
+        }
+        run += __shfl_sync(0xffffffffu, incl, 31);
       }
       __syncthreads();
       if (out + nnz_w > row_end) {  // never write past the row the symbolic pass sized
@@ -345,40 +382,74 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
         const uint32_t base = gbase[w / kGroupWords];
         return (int)base + (int)(uint16_t)(wpre[w] - (uint16_t)base);
       };
-      // columns, in order
-      for (int w = w0; w < w1; w++) {
-        uint32_t word = bm[w];
-        int r = word_prefix(w);
-        while (word) {
-          const int bit = __ffs(word) - 1;
-          word &= word - 1;
-          a.Ck[out + r] = wlo + w * 32 + bit;
-          r++;
+      // columns, in order: word-interleaved per warp as above
+      for (int wb = c0; wb < c1; wb += 32) {
+        const int w = wb + lane;
+        if (w < c1) {
+          uint32_t word = bm[w];
+          int r = word_prefix(w);
+          while (word) {
+            const int bit = __ffs(word) - 1;
+            word &= word - 1;
+            a.Ck[out + r] = wlo + w * 32 + bit;
+            r++;
+          }
         }
       }
+      // column of output rank `target` (< nnz_w) in this span
+      auto col_of_rank = [&](int target) -> int32_t {
+        int lo = 0, hi = nw - 1;  // last word whose prefix <= target
+        while (lo < hi) {
+          const int m = (lo + hi + 1) >> 1;
+          if (word_prefix(m) <= target) lo = m; else hi = m - 1;
+        }
+        int need = target - word_prefix(lo);
+        uint32_t word = bm[lo];
+        while (need-- > 0) word &= word - 1;
+        return wlo + lo * 32 + (__ffs(word) - 1);
+      };
+      const int nwin = (nnz_w + kAcc - 1) / kAcc;
+      const int nj = q1 - q0;
+      const int32_t span_hi = multi ? span_end(wlo) : INT_MAX;
+      // Several windows and one batch of j's: find every (j, window) slice
+      // bound up front, all searches in parallel across the CTA, instead of
+      // two dependent searches per j in every window.
+      const bool prebound = nwin > 1 && nwin <= kMaxWin && nj <= kThreads && nj * (nwin + 1) <= kBoundInts;
+      if (prebound) {
+        for (int w = threadIdx.x; w <= nwin; w += kThreads)
+          s_wcol[w] = w == 0 ? wlo : (w == nwin ? span_hi : col_of_rank(w * kAcc));
+        __syncthreads();
+        for (int it = threadIdx.x; it < nj * (nwin + 1); it += kThreads) {
+          const int t = it / (nwin + 1), w = it - t * (nwin + 1);
+          const int32_t j = __ldg(a.Aj + q0 + t);
+          const int32_t s0 = __ldg(a.Bp + j), e0 = __ldg(a.Bp + j + 1);
+          int32_t pos;
+          if (w == 0 && !multi) {
+            pos = s0;
+          } else if (w == nwin && !multi) {
+            pos = e0;
+          } else {
+            const int32_t col = s_wcol[w];
+            int32_t lo = s0, hi = e0;  // first position with column >= col
+            while (lo < hi) {
+              const int32_t m = (lo + hi) >> 1;
+              if (__ldg(a.Bk + m) < col) lo = m + 1; else hi = m;
+            }
+            pos = lo;
+          }
+          bnd[t * (nwin + 1) + w] = pos;
+        }
+        __syncthreads();
+      }
       // values, one window of kAcc ranks at a time
-      for (int r0 = 0; r0 < nnz_w; r0 += kAcc) {
+      for (int r0 = 0, win = 0; r0 < nnz_w; r0 += kAcc, win++) {
         const int r1 = min(nnz_w, r0 + kAcc);
         const bool whole = r0 == 0 && r1 == nnz_w;
-        int32_t clo = wlo, chi = multi ? span_end(wlo) : INT_MAX;
-        if (!whole) {  // columns of ranks r0 and r1 bound the window
+        int32_t clo = wlo, chi = span_hi;
+        if (!whole && !prebound) {  // columns of ranks r0 and r1 bound the window
           if (threadIdx.x < 2) {
             const int target = threadIdx.x == 0 ? r0 : r1;
-            int32_t col;
-            if (target >= nnz_w) {
-              col = multi ? span_end(wlo) : INT_MAX;
-            } else {
-              int lo = 0, hi = nw - 1;  // last word whose prefix <= target
-              while (lo < hi) {
-                const int m = (lo + hi + 1) >> 1;
-                if (word_prefix(m) <= target) lo = m; else hi = m - 1;
-              }
-              int need = target - word_prefix(lo);
-              uint32_t word = bm[lo];
-              while (need-- > 0) word &= word - 1;
-              col = wlo + lo * 32 + (__ffs(word) - 1);
-            }
-            s_cols[threadIdx.x] = col;
+            s_cols[threadIdx.x] = target >= nnz_w ? span_hi : col_of_rank(target);
           }
           __syncthreads();
           clo = s_cols[0];
@@ -386,12 +457,31 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
         }
         const bool clip = multi || !whole;
         for (int32_t qb = q0; qb < q1; qb += kThreads) {
-          const int total = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
-          for_batch_entries(b, total, [&](int32_t p, double av) {
-            const int k = __ldg(a.Bk + p) - wlo;
+          int npieces;
+          if (prebound) {  // slices from the bound table (one batch)
+            const int t = threadIdx.x;
+            int32_t s0 = 0, len = 0;
+            double av = 0.0;
+            if (t < nj) {
+              s0 = bnd[t * (nwin + 1) + win];
+              len = bnd[t * (nwin + 1) + win + 1] - s0;
+              av = __ldg(a.Av + q0 + t);
+            }
+            const int ex = block_excl_scan((len + kPieceLen - 1) / kPieceLen, wsum, &npieces);
+            b.s[t] = s0;
+            b.len[t] = len;
+            b.pexcl[t] = ex;
+            b.a[t] = av;
+            if (t == 0) b.pexcl[kThreads] = npieces;
+            __syncthreads();
+          } else {
+            npieces = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
+          }
+          for_batch_entries<true>(b, npieces, a.Bk, a.Bv, [&](int32_t col, double bv, double av) {
+            const int k = col - wlo;
             const int w = k >> 5;
             const int rank = word_prefix(w) + __popc(bm[w] & ((1u << (k & 31)) - 1u));
-            atomicAdd(&acc[rank - r0], __dmul_rn(av, __ldg(a.Bv + p)));
+            atomicAdd(&acc[rank - r0], __dmul_rn(av, bv));
           });
           __syncthreads();
         }
@@ -491,8 +581,8 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
 constexpr size_t kLightSymSmem = sizeof(unsigned long long) * kLightMax * kLightWarps;
 constexpr size_t kLightNumSmem = (sizeof(unsigned long long) + sizeof(double)) * kLightMax * kLightWarps;
 constexpr size_t kSymSmem = sizeof(uint32_t) * kSpanWords + sizeof(Batch);
-constexpr size_t kNumSmem =
-    sizeof(double) * kAcc + sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords + sizeof(Batch);
+constexpr size_t kNumSmem = sizeof(double) * kAcc + sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords +
+                            sizeof(Batch) + sizeof(int32_t) * kBoundInts;
 
 }  // namespace
 
