@@ -28,6 +28,7 @@
 #include <climits>
 
 #include "common.cuh"
+#include "sort.h"
 #include "spws_internal.h"
 
 namespace spws {
@@ -55,42 +56,54 @@ struct RowInfo {
 
 __device__ __forceinline__ int cost_bucket(long long p) { return p <= 0 ? 0 : 64 - __clzll(p); }
 
-// Warp per row of A: products, column span, cost bucket.
+// Warp per row of A: products, column span, cost bucket. The bucket
+// histogram is gathered per CTA in shared memory first: with many rows of
+// similar cost, one global atomic per row would serialise on a few counters.
 __global__ void k_row_info(int32_t nA, const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
                            const int32_t* __restrict__ Bp, const int32_t* __restrict__ Bk, RowInfo* __restrict__ info,
                            int* __restrict__ hist, unsigned long long* __restrict__ total_products,
                            int* __restrict__ err) {
+  __shared__ int h[kBuckets];
+  __shared__ unsigned long long tp;
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) h[b] = 0;
+  if (threadIdx.x == 0) tp = 0;
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (warp >= nA) return;
-  const int32_t i = (int32_t)warp;
-  long long p = 0;
-  int lo = INT_MAX, hi = -1;
-  for (int32_t q = Ap[i] + lane; q < Ap[i + 1]; q += 32) {
-    const int32_t j = Aj[q];
-    const int32_t s = Bp[j], e = Bp[j + 1];
-    if (e > s) {
-      p += e - s;
-      lo = min(lo, Bk[s]);
-      hi = max(hi, Bk[e - 1]);
+  if (warp < nA) {
+    const int32_t i = (int32_t)warp;
+    long long p = 0;
+    int lo = INT_MAX, hi = -1;
+    for (int32_t q = Ap[i] + lane; q < Ap[i + 1]; q += 32) {
+      const int32_t j = Aj[q];
+      const int32_t s = Bp[j], e = Bp[j + 1];
+      if (e > s) {
+        p += e - s;
+        lo = min(lo, Bk[s]);
+        hi = max(hi, Bk[e - 1]);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      p += __shfl_xor_sync(0xffffffffu, p, o);
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) {
+      RowInfo r;
+      r.products = p;
+      r.lo = p > 0 ? lo : 0;
+      r.hi = p > 0 ? hi : -1;
+      info[i] = r;
+      atomicAdd(&h[cost_bucket(p)], 1);
+      atomicAdd(&tp, (unsigned long long)p);
+      if (p > INT_MAX) atomicExch(err, 2);  // per-row product streams are indexed in 32 bits
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    p += __shfl_xor_sync(0xffffffffu, p, o);
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  }
-  if (lane == 0) {
-    RowInfo r;
-    r.products = p;
-    r.lo = p > 0 ? lo : 0;
-    r.hi = p > 0 ? hi : -1;
-    info[i] = r;
-    atomicAdd(&hist[cost_bucket(p)], 1);
-    atomicAdd(total_products, (unsigned long long)p);
-    if (p > INT_MAX) atomicExch(err, 2);  // per-row product streams are indexed in 32 bits
-  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
+    if (h[b]) atomicAdd(&hist[b], h[b]);
+  if (threadIdx.x == 0 && tp) atomicAdd(total_products, tp);
 }
 
 // Single thread: bucket offsets in descending cost order (bucket 0 excluded).
@@ -108,13 +121,28 @@ __global__ void k_order_offsets(const int* __restrict__ hist, int* __restrict__ 
   }
 }
 
+// Rows into their bucket's range of `order`; lanes of a warp that share a
+// bucket take their slots with one atomic.
 __global__ void k_order_scatter(int32_t nA, const RowInfo* __restrict__ info, int* __restrict__ cursor,
                                 int32_t* __restrict__ order) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int b = i < nA ? cost_bucket(info[i].products) : 0;
+  const unsigned peers = __match_any_sync(0xffffffffu, b);
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (lane == leader && b != 0) base = atomicAdd(&cursor[b], __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  if (b != 0) order[base + __popc(peers & ((1u << lane) - 1u))] = (int32_t)i;
+}
+
+// Words of bitmap a heavy row keeps between the passes (0: rebuilt instead).
+__global__ void k_bitmap_words(int32_t nA, const RowInfo* __restrict__ info, int32_t* __restrict__ words) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nA) return;
-  const int b = cost_bucket(info[i].products);
-  if (b == 0) return;
-  order[atomicAdd(&cursor[b], 1)] = (int32_t)i;
+  const RowInfo r = info[i];
+  const long long span = (long long)r.hi - r.lo + 1;
+  words[i] = (cost_bucket(r.products) > kLightBucket && span <= kSpanBits) ? (int32_t)((span + 31) >> 5) : 0;
 }
 
 struct PassArgs {
@@ -135,6 +163,8 @@ struct PassArgs {
   int32_t* Ck;         // numeric output
   double* Cv;          // numeric output
   int* err;            // set on internal inconsistency
+  uint32_t* bmstore;   // heavy single-span rows: the symbolic pass keeps its bitmap
+  const long long* bmoff;  // here (word offset per row) for the numeric pass; null = rebuild
 };
 
 constexpr int kPieceLen = 256;  // B entries per warp work piece
@@ -301,6 +331,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_symbolic(PassArgs a) {
       for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = 0;
       __syncthreads();
       build_bitmap(a, q0, q1, (int32_t)wl, multi, bm, b, wsum);
+      if (a.bmstore && !multi) {
+        uint32_t* dst = a.bmstore + a.bmoff[i];
+        for (int w = threadIdx.x; w < nw; w += kThreads) dst[w] = bm[w];
+      }
       int c = 0;
       for (int w = threadIdx.x; w < nw; w += kThreads) c += __popc(bm[w]);
       int t;
@@ -338,9 +372,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
     for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
       const int32_t wlo = (int32_t)wl;
       const int nw = words_in(wl, ri.hi);
-      for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = 0;
-      __syncthreads();
-      build_bitmap(a, q0, q1, wlo, multi, bm, b, wsum);
+      if (a.bmstore && !multi) {  // the symbolic pass left this row's bitmap
+        const uint32_t* src = a.bmstore + a.bmoff[i];
+        for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = src[w];
+        __syncthreads();
+      } else {
+        for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = 0;
+        __syncthreads();
+        build_bitmap(a, q0, q1, wlo, multi, bm, b, wsum);
+      }
 
       // Per-word prefix of set bits and the row's columns in order. Warp w
       // owns a contiguous chunk of words and walks it 32 words at a time, one
@@ -639,9 +679,39 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
   k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, sm->cursor, order);
   count_launch(3);
   SPWS_CUDA(cudaGetLastError());
+
+  // Bitmaps of heavy single-span rows survive from the symbolic to the numeric
+  // pass (when they fit a memory budget), so the numeric pass reads them
+  // instead of going over the row's products a second time.
+  int32_t* bmwords = nullptr;
+  long long* bmoff = nullptr;
+  uint32_t* bmstore = nullptr;
+  {
+    SPWS_TRY(dalloc((void**)&bmwords, sizeof(int32_t) * (size_t)nA, s));
+    SPWS_TRY(dalloc((void**)&bmoff, sizeof(long long) * (size_t)nA, s));
+    k_bitmap_words<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, bmwords);
+    count_launch(1);
+    long long* tot = &sm->nnz;  // reused: cleared again before the count scan
+    SPWS_TRY(scan_i32_to_i64(bmwords, bmoff, nA, tot, s));
+    long long words = 0;
+    SPWS_CUDA(cudaMemcpyAsync(&words, tot, sizeof(words), cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaStreamSynchronize(s));
+    SPWS_CUDA(cudaMemsetAsync(tot, 0, sizeof(long long), s));
+    size_t free_b = 0, total_b = 0;
+    SPWS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t bytes = (size_t)words * sizeof(uint32_t);
+    if (words > 0 && bytes <= free_b / 8) {
+      if (dalloc((void**)&bmstore, bytes, s) != SPWS_OK) {
+        clear_error();
+        bmstore = nullptr;
+      }
+    }
+  }
   SPWS_CUDA(cudaEventRecord(ev[1], s));
 
   PassArgs pa{};
+  pa.bmstore = bmstore;
+  pa.bmoff = bmoff;
   pa.Ap = A.pos;
   pa.Aj = A.crd;
   pa.Av = A.vals;
@@ -688,6 +758,9 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
     dfree(info, s);
     dfree(order, s);
     dfree(rowcnt, s);
+    dfree(bmwords, s);
+    dfree(bmoff, s);
+    dfree(bmstore, s);
   };
   if (err == 2) {
     cleanup();
