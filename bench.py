@@ -41,11 +41,12 @@ RMAT = dict(scale=18, deg=16, a=0.57, b=0.19, c=0.19, seed=42)
 L2_FLUSH_BYTES = 512 << 20  # > 2x the 126 MB L2
 
 
-def make_workload(name):
+def make_workload(name, scale=None):
     from sparsews_gb300 import gen
     if name == "rmat":
-        A = gen.rmat(RMAT["scale"], RMAT["deg"], RMAT["a"], RMAT["b"], RMAT["c"], seed=RMAT["seed"])
-        cfg = {"workload": "rmat_spgemm_AxA", "n": 1 << RMAT["scale"], "edge_draws_per_row": RMAT["deg"],
+        sc = scale or RMAT["scale"]
+        A = gen.rmat(sc, RMAT["deg"], RMAT["a"], RMAT["b"], RMAT["c"], seed=RMAT["seed"])
+        cfg = {"workload": "rmat_spgemm_AxA", "n": 1 << sc, "edge_draws_per_row": RMAT["deg"],
                "rmat_abc": [RMAT["a"], RMAT["b"], RMAT["c"]], "seed": RMAT["seed"]}
     elif name == "er":
         A = gen.er(10000, 10, seed=42)
@@ -237,7 +238,7 @@ def barrier(dist):
 def bench_reference(args, ws, rank, dist):
     if rank != 0:
         return
-    A, cfg = make_workload(args.workload)
+    A, cfg = make_workload(args.workload, args.scale)
     threads = os.cpu_count() or 1
     kind = cpu_kind()
     per_step = args.cpu_step_products
@@ -269,7 +270,7 @@ def bench_spws(args, ws, rank, local, dist):
     L.spws_set_device.argtypes = [C.c_int]
     sp.check(L.spws_set_device(local))
 
-    A, cfg = make_workload(args.workload)
+    A, cfg = make_workload(args.workload, args.scale)
     nA = A[3]
     dA = sp.DeviceCsr.upload(*A)
 
@@ -323,7 +324,7 @@ def bench_spws(args, ws, rank, local, dist):
     e2e_walls = []
     h2d = 2 * (pos.nbytes + crd.nbytes + vals.nbytes)  # A and B are both copied in
     d2h = 0
-    for it in range(max(1, args.e2e_steps) + 1):
+    for it in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         Ct = taco.init_dc(nA, A[4])
         barrier(dist)
         t0 = time.perf_counter()
@@ -338,8 +339,8 @@ def bench_spws(args, ws, rank, local, dist):
             e2e_walls.append(t1 - t0)
     for arr in pinned:
         L.spws_host_unpin(arr.ctypes.data)
-    e2e_wall = reduce_max(dist, sum(e2e_walls) / len(e2e_walls))
-    e2e_value = flops_job / e2e_wall / 1e9
+    e2e_wall = reduce_max(dist, sum(e2e_walls) / len(e2e_walls)) if e2e_walls else float("nan")
+    e2e_value = flops_job / e2e_wall / 1e9 if e2e_walls else None
 
     if rank != 0:
         return
@@ -384,10 +385,11 @@ def bench_spws(args, ws, rank, local, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spws", choices=["spws", "reference"])
     ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band"])
+    ap.add_argument("--scale", type=int, default=None, help="R-MAT scale (default 18); smaller for profiling")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-products", type=int, default=60_000_000, help="products in the CPU-baseline sample")
     ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
