@@ -382,13 +382,86 @@ def bench_spws(args, ws, rank, local, dist):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ batched form
+def batch_workload(count, seed=42):
+    """The batched config: n_i log-uniform in [256, 65536], Poisson(8)
+    distinct columns per row; even instances uniform, odd ones R-MAT
+    (a, b, c = .57, .19, .19). Seeded per instance."""
+    from sparsews_gb300 import gen
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(256), np.log(65536), count)).astype(np.int64)
+    out = []
+    for t, n in enumerate(ns):
+        if t % 2 == 0:
+            out.append(gen.poisson_rows(int(n), 8.0, seed=seed * 100003 + t))
+        else:
+            out.append(gen.rmat_n(int(n), 8.0, seed=seed * 100003 + t))
+    return out
+
+
+def bench_batched(args):
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import build, taco
+    build.build()
+    L = sp.lib()
+    sp.check(L.spws_set_device(0))
+    t0 = time.perf_counter()
+    insts = batch_workload(args.instances)
+    gen_s = time.perf_counter() - t0
+    dev = [sp.DeviceCsr.upload(*A) for A in insts]
+    for _ in range(args.warmup):
+        sp.spgemm_batched(dev, dev).release()
+    walls, stats = [], None
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+            t0 = time.perf_counter()
+            b = sp.spgemm_batched(dev, dev)
+            walls.append(time.perf_counter() - t0)
+            stats = b.stats
+            b.release()
+    wall = sum(walls) / len(walls)
+    # one-at-a-time through the same device-resident entry point, and through
+    # the reference-compatible TACO entry point with host arrays
+    t0 = time.perf_counter()
+    for d in dev:
+        c, _ = sp.spgemm_device(d, d)
+        c.release()
+    seq_dev = time.perf_counter() - t0
+    nplain = min(len(insts), args.plain_sample)
+    t0 = time.perf_counter()
+    for A in insts[:nplain]:
+        At = taco.csr(*A)
+        Ct = taco.init_dc(A[3], A[4])
+        sp.check(L.spws_csr_csr_hash_compute(Ct.ptr(), At.ptr(), At.ptr(), 0))
+        taco.take_csr(Ct, A[3], L.spws_free)
+    seq_abi = (time.perf_counter() - t0) / nplain * len(insts)
+    n = len(insts)
+    line = {"metric": "batched_spgemm_solves_per_s", "value": n / wall, "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "batched_spgemm_AixAi", "instances": n, "n_range": [256, 65536],
+                       "row_nnz": "Poisson(8)", "mix": "even uniform, odd R-MAT", "groups": stats.groups,
+                       "l2": "flushed between timed steps"},
+            "gflops": 2.0 * stats.products / wall / 1e9, "products": int(stats.products), "nnz_C": int(stats.nnz),
+            "device_ms_kernels": stats.ms_kernels,
+            "one_at_a_time": {"device_entry_solves_per_s": n / seq_dev,
+                              "taco_abi_solves_per_s": n / seq_abi, "taco_abi_sample": nplain,
+                              "speedup_vs_device_entry": seq_dev / wall, "speedup_vs_taco_abi": seq_abi / wall},
+            "clocks": clk.summary(), "generation_s": gen_s}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spws", choices=["spws", "reference"])
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band"])
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched"])
+    ap.add_argument("--instances", type=int, default=1024,
+                    help="batched workload: number of products (4096 holds ~220 GB of output at once)")
+    ap.add_argument("--plain-sample", type=int, default=512, help="batched workload: one-at-a-time ABI sample")
     ap.add_argument("--scale", type=int, default=None, help="R-MAT scale (default 18); smaller for profiling")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-products", type=int, default=60_000_000, help="products in the CPU-baseline sample")
@@ -397,7 +470,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     ws, rank, local, dist = dist_init()
-    if args.impl == "reference":
+    if args.workload == "batched":
+        if rank == 0 and args.impl != "reference":
+            bench_batched(args)
+    elif args.impl == "reference":
         bench_reference(args, ws, rank, dist)
     else:
         bench_spws(args, ws, rank, local, dist)

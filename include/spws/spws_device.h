@@ -45,6 +45,19 @@ typedef struct spws_spgemm_stats {
   int32_t n_chunks;      /* chunks covering B's columns */
 } spws_spgemm_stats;
 
+/* Statistics of a batched SpGEMM. */
+typedef struct spws_batch_stats {
+  int32_t instances;  /* products in the batch */
+  int32_t groups;     /* row-wise pipeline runs (each group's output fits int32 positions) */
+  int64_t products;   /* scalar products over the batch */
+  int64_t nnz;        /* output nonzeros over the batch */
+  float ms_kernels;   /* device time of the row-wise pipelines */
+  float ms_total;     /* device time including assembly and splitting */
+} spws_batch_stats;
+
+/* Opaque owner of a batch's results. */
+typedef struct spws_batch spws_batch;
+
 /* Copy a host CSR into library-owned device memory. */
 int spws_csr_upload(const int32_t* pos, const int32_t* crd, const double* vals, int32_t nrows, int32_t ncols,
                     spws_csr_dev* out);
@@ -86,6 +99,17 @@ int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev* B, int32_
 
 /* Make `device` current for the calling thread (cudaSetDevice). */
 int spws_set_device(int device);
+
+/* Batched SpGEMM: C[i] = A[i] * B[i] for `count` independent products of
+ * uneven sizes, run as one row-wise pipeline over block-diagonal operands
+ * (every instance's rows share the same cost-ordered work queue), split into
+ * as few groups as int32 output positions allow. C[i] are views into memory
+ * owned by *batch: read them with spws_csr_download, never pass them to
+ * spws_csr_release, and free them all with spws_batch_release. No counterpart
+ * in the reference (its kernels take one product per call). */
+int spws_spgemm_batched(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
+                        spws_batch** batch, spws_batch_stats* stats);
+int spws_batch_release(spws_batch* batch);
 
 /* Block until the library's stream on the current device is idle. */
 int spws_device_sync(void);

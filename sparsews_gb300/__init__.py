@@ -35,6 +35,11 @@ class CsrDev(C.Structure):
                 ("pos", C.c_void_p), ("crd", C.c_void_p), ("vals", C.c_void_p)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("instances", C.c_int32), ("groups", C.c_int32), ("products", C.c_int64), ("nnz", C.c_int64),
+                ("ms_kernels", C.c_float), ("ms_total", C.c_float)]
+
+
 class SpgemmStats(C.Structure):
     _fields_ = [("products", C.c_int64), ("nnz", C.c_int64), ("ms_setup", C.c_float), ("ms_symbolic", C.c_float),
                 ("ms_scan", C.c_float), ("ms_numeric", C.c_float), ("ms_total", C.c_float),
@@ -80,6 +85,9 @@ def lib():
         "spws_flush_l2": ([C.c_size_t], C.c_int),
         "spws_host_pin": ([C.c_void_p, C.c_size_t], C.c_int),
         "spws_host_unpin": ([C.c_void_p], C.c_int),
+        "spws_spgemm_batched": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p),
+                                 C.POINTER(BatchStats)], C.c_int),
+        "spws_batch_release": ([C.c_void_p], C.c_int),
         "spws_csr_upload": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CsrDev)], C.c_int),
         "spws_csr_download": ([C.POINTER(CsrDev), C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "spws_csr_release": ([C.POINTER(CsrDev)], C.c_int),
@@ -192,10 +200,12 @@ def ttm(Bcoo, dims, Cf, method="bucket"):
 
 
 class DeviceCsr:
-    """A CSR matrix in library-owned device memory."""
+    """A CSR matrix in library-owned device memory. `owns=False` wraps a view
+    into memory owned elsewhere (a Batch): it is never released from here."""
 
-    def __init__(self, m=None):
+    def __init__(self, m=None, owns=True):
         self.m = m if m is not None else CsrDev()
+        self.owns = owns
 
     @classmethod
     def upload(cls, pos, crd, vals, nrows, ncols):
@@ -216,9 +226,9 @@ class DeviceCsr:
         return pos, crd[: self.m.nnz], vals[: self.m.nnz]
 
     def release(self):
-        if self.m.pos:
+        if self.owns and self.m.pos:
             lib().spws_csr_release(C.byref(self.m))
-            self.m = CsrDev()
+        self.m = CsrDev()
 
     def __del__(self):
         try:
@@ -234,3 +244,43 @@ def spgemm_device(A, B, accum_mode=0):
     st = SpgemmStats()
     check(L.spws_spgemm_csr_device(C.byref(A.m), C.byref(B.m), C.byref(Cd.m), accum_mode, C.byref(st)))
     return Cd, st
+
+
+class Batch:
+    """Results of spgemm_batched: per-instance device CSR views plus their owner."""
+
+    def __init__(self, handle, views, stats):
+        self.handle = handle
+        self.views = views
+        self.stats = stats
+
+    def download(self, i):
+        if not self.handle:
+            raise RuntimeError("batch already released")
+        return DeviceCsr(self.views[i], owns=False).download()
+
+    def release(self):
+        if self.handle:
+            lib().spws_batch_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def spgemm_batched(As, Bs):
+    """C_i = A_i * B_i for lists of DeviceCsr in one batched launch set."""
+    L = lib()
+    n = len(As)
+    Aarr = (CsrDev * max(n, 1))(*[a.m for a in As])
+    Barr = (CsrDev * max(n, 1))(*[b.m for b in Bs])
+    Carr = (CsrDev * max(n, 1))()
+    h = C.c_void_p()
+    st = BatchStats()
+    check(L.spws_spgemm_batched(n, C.cast(Aarr, C.c_void_p), C.cast(Barr, C.c_void_p), C.cast(Carr, C.c_void_p),
+                                C.byref(h), C.byref(st)))
+    views = [CsrDev(Carr[i].nrows, Carr[i].ncols, Carr[i].nnz, Carr[i].pos, Carr[i].crd, Carr[i].vals) for i in range(n)]
+    return Batch(h, views, st)

@@ -213,6 +213,20 @@ int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double*
   clear_error();
   DeviceState* ds = nullptr;
   SPWS_TRY(device_state(&ds));
+  if (!m || !pos || m->nrows < 0 || m->nnz < 0 || (m->nnz > 0 && (!crd || !vals))) {
+    set_error("spws_csr_download: bad arguments");
+    return SPWS_ERR_INVALID;
+  }
+  // refuse pointers that are not live device memory (e.g. a released batch view)
+  const void* ptrs[3] = {m->pos, m->crd, m->vals};
+  for (int k = 0; k < (m->nnz > 0 ? 3 : 1); k++) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, ptrs[k]) != cudaSuccess || at.type != cudaMemoryTypeDevice) {
+      (void)cudaGetLastError();
+      set_error("spws_csr_download: source is not live device memory");
+      return SPWS_ERR_INVALID;
+    }
+  }
   cudaStream_t s = ds->stream;
   SPWS_CUDA(cudaMemcpyAsync(pos, m->pos, sizeof(int32_t) * ((size_t)m->nrows + 1), cudaMemcpyDeviceToHost, s));
   if (m->nnz > 0) {
@@ -220,6 +234,37 @@ int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double*
     SPWS_CUDA(cudaMemcpyAsync(vals, m->vals, sizeof(double) * (size_t)m->nnz, cudaMemcpyDeviceToHost, s));
   }
   SPWS_CUDA(cudaStreamSynchronize(s));
+  return SPWS_OK;
+}
+
+struct spws_batch {
+  spws::BatchBlocks blocks;
+};
+
+int spws_spgemm_batched(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
+                        spws_batch** batch, spws_batch_stats* stats) {
+  clear_error();
+  if (count < 0 || (count > 0 && (!A || !B || !C)) || !batch) {
+    set_error("spws_spgemm_batched: bad arguments");
+    return SPWS_ERR_INVALID;
+  }
+  *batch = nullptr;
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  spws_batch* b = new spws_batch();
+  const int rc = spgemm_batched(count, A, B, C, stats, &b->blocks, ds->stream);
+  if (rc != SPWS_OK) {
+    delete b;
+    return rc;
+  }
+  *batch = b;
+  return SPWS_OK;
+}
+
+int spws_batch_release(spws_batch* batch) {
+  if (!batch) return SPWS_OK;
+  for (void* p : batch->blocks.blocks) dfree(p, batch->blocks.stream);
+  delete batch;
   return SPWS_OK;
 }
 

@@ -1,0 +1,350 @@
+// Batched SpGEMM: C_i = A_i * B_i for many independent, uneven products in
+// one pass of the row-wise kernels.
+//
+// The instances are laid side by side as block-diagonal super-operands
+// A* = diag(A_1..A_m) and B* = diag(B_1..B_m) (columns of A_i and B_i shifted
+// by the widths of the instances before them), so A* x B* = diag(C_1..C_m).
+// One row-wise pipeline over A* then orders every instance's rows together by
+// cost (heavy rows to CTAs, light rows to warps) and runs them in the same
+// launches. Instances are grouped so that a group's output positions fit
+// int32, the position type of taco_tensor_t; a group is a row range of A*.
+// The product of a group is split back into per-instance CSR views whose
+// positions start at 0 and whose columns are the instance's own.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <vector>
+
+#include "sort.h"
+#include "spws_internal.h"
+#include "validate.h"
+
+namespace spws {
+namespace {
+
+struct Inst {
+  const int32_t* pos;
+  const int32_t* crd;
+  const double* vals;
+  int32_t rows;
+  int32_t row_off;    // first row in the super-matrix
+  int32_t col_off;    // column shift
+  int32_t pad;
+  long long nnz_off;  // first entry in the super-matrix
+};
+
+__device__ __forceinline__ int find_inst(const long long* __restrict__ offs, int count, long long x) {
+  int lo = 0, hi = count - 1;  // last instance whose offset <= x
+  while (lo < hi) {
+    const int m = (lo + hi + 1) >> 1;
+    if (offs[m] <= x) lo = m; else hi = m - 1;
+  }
+  return lo;
+}
+
+// Super-matrix positions: pos*[row_off_i + r] = nnz_off_i + pos_i[r].
+__global__ void k_cat_pos(int count, const Inst* __restrict__ in, const long long* __restrict__ row_offs,
+                          int32_t total_rows, long long total_nnz, int32_t* __restrict__ pos) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > total_rows) return;
+  if (r == total_rows) {
+    pos[r] = (int32_t)total_nnz;
+    return;
+  }
+  const int i = find_inst(row_offs, count, r);
+  const Inst t = in[i];
+  pos[r] = (int32_t)(t.nnz_off + t.pos[r - t.row_off]);
+}
+
+// Super-matrix entries: column shifted by the instance's column offset.
+__global__ void k_cat_ent(int count, const Inst* __restrict__ in, const long long* __restrict__ nnz_offs,
+                          long long total_nnz, int32_t* __restrict__ crd, double* __restrict__ vals) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= total_nnz) return;
+  const int i = find_inst(nnz_offs, count, e);
+  const Inst t = in[i];
+  const int64_t k = e - t.nnz_off;
+  crd[e] = t.crd[k] + t.col_off;
+  vals[e] = t.vals[k];
+}
+
+// Per-instance positions of a group's product: instance i owns rows
+// [ro_i, ro_i + n_i) of the group result; its own array starts at
+// out_off_i = ro_i + i (one extra end entry per instance).
+__global__ void k_split_pos(int count, const Inst* __restrict__ ia, const long long* __restrict__ row_offs,
+                            int first, int32_t group_row0, int32_t group_rows, const int32_t* __restrict__ gpos,
+                            int32_t* __restrict__ opos, long long* __restrict__ inst_nnz_off) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // row within the group, or an end entry
+  if (r >= group_rows) return;
+  const int i = find_inst(row_offs, count, group_row0 + r);
+  const Inst t = ia[i];
+  const int32_t lr = (int32_t)(group_row0 + r - t.row_off);  // row within the instance
+  const int32_t gr0 = t.row_off - group_row0;                // instance's first row within the group
+  const int32_t base = gpos[gr0];
+  const int64_t at = (int64_t)gr0 + (i - first);
+  opos[at + lr] = gpos[r] - base;
+  if (lr == t.rows - 1) {
+    opos[at + t.rows] = gpos[gr0 + t.rows] - base;
+    inst_nnz_off[i] = base;
+  }
+  if (lr == 0 && t.rows == 0) inst_nnz_off[i] = base;
+}
+
+// Columns of a group's product back to each instance's own range.
+__global__ void k_split_crd(int count, const Inst* __restrict__ ib, const long long* __restrict__ row_offs,
+                            int first, int last, const long long* __restrict__ inst_nnz_off,
+                            long long group_nnz, int32_t* __restrict__ crd) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= group_nnz) return;
+  int lo = first, hi = last - 1;  // last instance of the group whose output starts at or before e
+  while (lo < hi) {
+    const int m = (lo + hi + 1) >> 1;
+    if (inst_nnz_off[m] <= e) lo = m; else hi = m - 1;
+  }
+  crd[e] -= ib[lo].col_off;
+  (void)row_offs;
+  (void)count;
+}
+
+// Products of each A row, summed per instance (an upper bound of the
+// instance's output nonzeros, used to cut the batch into int32-sized groups).
+__global__ void k_inst_products(int count, const long long* __restrict__ row_offs, int32_t total_rows,
+                                const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
+                                const int32_t* __restrict__ Bp, unsigned long long* __restrict__ prods) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= total_rows) return;
+  long long p = 0;
+  for (int32_t q = Ap[r] + lane; q < Ap[r + 1]; q += 32) {
+    const int32_t j = Aj[q];
+    p += Bp[j + 1] - Bp[j];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+  if (lane == 0 && p) atomicAdd(&prods[find_inst(row_offs, count, r)], (unsigned long long)p);
+}
+
+__global__ void k_zero_rows(int count, const Inst* __restrict__ ia, int first, int last,
+                            long long* __restrict__ inst_nnz_off, int32_t group_row0, const int32_t* __restrict__ gpos,
+                            int32_t* __restrict__ opos) {
+  // instances with no rows still need their single position entry and offset
+  const int i = first + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= last) return;
+  const Inst t = ia[i];
+  if (t.rows != 0) return;
+  const int32_t gr0 = t.row_off - group_row0;
+  opos[(int64_t)gr0 + (i - first)] = 0;
+  inst_nnz_off[i] = gpos[gr0];
+}
+
+}  // namespace
+
+int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
+                   spws_batch_stats* stats, BatchBlocks* owner, cudaStream_t s) {
+  if (count <= 0) return SPWS_OK;
+  std::vector<Inst> ia(count), ib(count);
+  std::vector<long long> arow(count), annz(count), bnnz(count), brow(count);
+  long long ar = 0, az = 0, bz = 0, acol = 0, bcol = 0, br = 0;
+  for (int i = 0; i < count; i++) {
+    if (A[i].ncols != B[i].nrows || A[i].nrows < 0 || B[i].ncols < 0) {
+      set_error("batched: instance " + std::to_string(i) + " has mismatched shapes");
+      return SPWS_ERR_INVALID;
+    }
+    ia[i] = Inst{A[i].pos, A[i].crd, A[i].vals, A[i].nrows, (int32_t)ar, (int32_t)acol, 0, az};
+    ib[i] = Inst{B[i].pos, B[i].crd, B[i].vals, B[i].nrows, (int32_t)br, (int32_t)bcol, 0, bz};
+    arow[i] = ar;
+    annz[i] = az;
+    brow[i] = br;
+    bnnz[i] = bz;
+    ar += A[i].nrows;
+    az += A[i].nnz;
+    br += B[i].nrows;
+    bz += B[i].nnz;
+    acol += A[i].ncols;
+    bcol += B[i].ncols;
+  }
+  if (ar > INT32_MAX - 1 || az > INT32_MAX || br > INT32_MAX - 1 || bz > INT32_MAX || acol > INT32_MAX ||
+      bcol > INT32_MAX) {
+    set_error("batched: the batch's operands exceed int32 sizes in total");
+    return SPWS_ERR_CAPACITY;
+  }
+  cudaEvent_t e0, e1;
+  SPWS_CUDA(cudaEventCreate(&e0));
+  SPWS_CUDA(cudaEventCreate(&e1));
+  SPWS_CUDA(cudaEventRecord(e0, s));
+
+  // device copies of the instance tables
+  Inst *dia = nullptr, *dib = nullptr;
+  long long *darow = nullptr, *dannz = nullptr, *dbrow = nullptr, *dbnnz = nullptr, *dnnzoff = nullptr;
+  SPWS_TRY(dalloc((void**)&dia, sizeof(Inst) * count, s));
+  SPWS_TRY(dalloc((void**)&dib, sizeof(Inst) * count, s));
+  SPWS_TRY(dalloc((void**)&darow, sizeof(long long) * count, s));
+  SPWS_TRY(dalloc((void**)&dannz, sizeof(long long) * count, s));
+  SPWS_TRY(dalloc((void**)&dbrow, sizeof(long long) * count, s));
+  SPWS_TRY(dalloc((void**)&dbnnz, sizeof(long long) * count, s));
+  SPWS_TRY(dalloc((void**)&dnnzoff, sizeof(long long) * count, s));
+  SPWS_CUDA(cudaMemcpyAsync(dia, ia.data(), sizeof(Inst) * count, cudaMemcpyHostToDevice, s));
+  SPWS_CUDA(cudaMemcpyAsync(dib, ib.data(), sizeof(Inst) * count, cudaMemcpyHostToDevice, s));
+  SPWS_CUDA(cudaMemcpyAsync(darow, arow.data(), sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  SPWS_CUDA(cudaMemcpyAsync(dannz, annz.data(), sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  SPWS_CUDA(cudaMemcpyAsync(dbrow, brow.data(), sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  SPWS_CUDA(cudaMemcpyAsync(dbnnz, bnnz.data(), sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+
+  // super-operands
+  spws_csr_dev Ab{}, Bb{};
+  Ab.nrows = (int32_t)ar;
+  Ab.ncols = (int32_t)acol;
+  Ab.nnz = az;
+  Bb.nrows = (int32_t)br;
+  Bb.ncols = (int32_t)bcol;
+  Bb.nnz = bz;
+  SPWS_TRY(dalloc((void**)&Ab.pos, sizeof(int32_t) * ((size_t)ar + 1), s));
+  SPWS_TRY(dalloc((void**)&Ab.crd, sizeof(int32_t) * (size_t)std::max(az, 1LL), s));
+  SPWS_TRY(dalloc((void**)&Ab.vals, sizeof(double) * (size_t)std::max(az, 1LL), s));
+  SPWS_TRY(dalloc((void**)&Bb.pos, sizeof(int32_t) * ((size_t)br + 1), s));
+  SPWS_TRY(dalloc((void**)&Bb.crd, sizeof(int32_t) * (size_t)std::max(bz, 1LL), s));
+  SPWS_TRY(dalloc((void**)&Bb.vals, sizeof(double) * (size_t)std::max(bz, 1LL), s));
+  k_cat_pos<<<(unsigned)((ar + 256) / 256), 256, 0, s>>>(count, dia, darow, (int32_t)ar, az, Ab.pos);
+  k_cat_pos<<<(unsigned)((br + 256) / 256), 256, 0, s>>>(count, dib, dbrow, (int32_t)br, bz, Bb.pos);
+  if (az > 0) k_cat_ent<<<(unsigned)((az + 255) / 256), 256, 0, s>>>(count, dia, dannz, az, Ab.crd, Ab.vals);
+  if (bz > 0) k_cat_ent<<<(unsigned)((bz + 255) / 256), 256, 0, s>>>(count, dib, dbnnz, bz, Bb.crd, Bb.vals);
+  count_launch(4);
+  SPWS_CUDA(cudaGetLastError());
+  // the instances may come from anywhere: check the assembled operands once
+  int rc = validate_csr_device(Ab.pos, Ab.crd, Ab.nrows, Ab.ncols, Ab.nnz, "batched A", s);
+  if (rc == SPWS_OK) rc = validate_csr_device(Bb.pos, Bb.crd, Bb.nrows, Bb.ncols, Bb.nnz, "batched B", s);
+
+  // Group instances so that each group's products (an upper bound of its
+  // output) stay below 2^31 and its positions fit int32.
+  std::vector<int> gstart;
+  std::vector<unsigned long long> iprod(count, 0);
+  if (rc == SPWS_OK) {
+    unsigned long long* dprod = nullptr;
+    SPWS_TRY(dalloc((void**)&dprod, sizeof(unsigned long long) * count, s));
+    SPWS_CUDA(cudaMemsetAsync(dprod, 0, sizeof(unsigned long long) * count, s));
+    if (ar > 0) {
+      k_inst_products<<<(unsigned)((ar + 7) / 8), 256, 0, s>>>(count, darow, (int32_t)ar, Ab.pos, Ab.crd, Bb.pos, dprod);
+      count_launch(1);
+    }
+    SPWS_CUDA(cudaMemcpyAsync(iprod.data(), dprod, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaStreamSynchronize(s));
+    dfree(dprod, s);
+    gstart.push_back(0);
+    unsigned long long acc = 0;
+    for (int i = 0; i < count; i++) {
+      if (iprod[i] > (unsigned long long)INT32_MAX) {
+        // one instance alone may still fit: its real output can be smaller
+        // than its products; the pipeline checks the exact count
+      }
+      if (i > gstart.back() && acc + iprod[i] > (unsigned long long)INT32_MAX) {
+        gstart.push_back(i);
+        acc = 0;
+      }
+      acc += iprod[i];
+    }
+    gstart.push_back(count);
+  }
+
+  // results: one shared allocation per array for the whole batch
+  int32_t* opos = nullptr;
+  SPWS_TRY(dalloc((void**)&opos, sizeof(int32_t) * ((size_t)ar + count), s));
+  std::vector<spws_csr_dev> parts;
+  long long total_nnz = 0, total_products = 0;
+  float ms_kernels = 0.f;
+  for (size_t g = 0; rc == SPWS_OK && g + 1 < gstart.size(); g++) {
+    const int first = gstart[g], last = gstart[g + 1];
+    const int32_t row0 = (int32_t)arow[first];
+    const int32_t rows = (int32_t)((last < count ? arow[last] : ar) - row0);
+    CsrView Av;
+    Av.nrows = rows;
+    Av.ncols = Ab.ncols;
+    Av.nnz = Ab.nnz;
+    Av.pos = Ab.pos + row0;
+    Av.crd = Ab.crd;
+    Av.vals = Ab.vals;
+    CsrView Bv;
+    Bv.nrows = Bb.nrows;
+    Bv.ncols = Bb.ncols;
+    Bv.nnz = Bb.nnz;
+    Bv.pos = Bb.pos;
+    Bv.crd = Bb.crd;
+    Bv.vals = Bb.vals;
+    spws_csr_dev Cg{};
+    spws_spgemm_stats st{};
+    SpgemmOpts opt;
+    rc = spgemm_rowwise(Av, Bv, &Cg, opt, &st, s);
+    if (rc != SPWS_OK) break;
+    total_nnz += Cg.nnz;
+    total_products += st.products;
+    ms_kernels += st.ms_total;
+    if (rows > 0) {
+      k_split_pos<<<(unsigned)((rows + 255) / 256), 256, 0, s>>>(count, dia, darow, first, row0, rows, Cg.pos,
+                                                                 opos + row0 + first, dnnzoff);
+      count_launch(1);
+    }
+    k_zero_rows<<<(unsigned)((last - first + 255) / 256), 256, 0, s>>>(count, dia, first, last, dnnzoff, row0, Cg.pos,
+                                                                      opos + row0 + first);
+    count_launch(1);
+    if (Cg.nnz > 0) {
+      k_split_crd<<<(unsigned)((Cg.nnz + 255) / 256), 256, 0, s>>>(count, dib, darow, first, last, dnnzoff, Cg.nnz,
+                                                                   Cg.crd);
+      count_launch(1);
+    }
+    SPWS_CUDA(cudaGetLastError());
+    parts.push_back(Cg);
+  }
+  std::vector<long long> nnzoff(count);
+  if (rc == SPWS_OK) {
+    SPWS_CUDA(cudaMemcpyAsync(nnzoff.data(), dnnzoff, sizeof(long long) * count, cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaEventRecord(e1, s));
+    SPWS_CUDA(cudaStreamSynchronize(s));
+    // per-instance views into the group results; the first instance of each
+    // group owns its group's crd/vals arrays and the first instance of the
+    // batch owns opos
+    for (size_t g = 0; g + 1 < gstart.size(); g++) {
+      const int first = gstart[g], last = gstart[g + 1];
+      for (int i = first; i < last; i++) {
+        C[i].nrows = A[i].nrows;
+        C[i].ncols = B[i].ncols;
+        C[i].pos = opos + arow[i] + i;
+        C[i].crd = parts[g].crd + nnzoff[i];
+        C[i].vals = parts[g].vals + nnzoff[i];
+        const long long end = (i + 1 < last) ? nnzoff[i + 1] : parts[g].nnz;
+        C[i].nnz = end - nnzoff[i];
+      }
+      dfree(parts[g].pos, s);
+    }
+  } else {
+    for (auto& p : parts) {
+      dfree(p.pos, s);
+      dfree(p.crd, s);
+      dfree(p.vals, s);
+    }
+    dfree(opos, s);
+  }
+  if (stats && rc == SPWS_OK) {
+    stats->instances = count;
+    stats->groups = (int32_t)(gstart.size() - 1);
+    stats->products = total_products;
+    stats->nnz = total_nnz;
+    stats->ms_kernels = ms_kernels;
+    cudaEventElapsedTime(&stats->ms_total, e0, e1);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dfree(dia, s); dfree(dib, s); dfree(darow, s); dfree(dannz, s); dfree(dbrow, s); dfree(dbnnz, s); dfree(dnnzoff, s);
+  dfree(Ab.pos, s); dfree(Ab.crd, s); dfree(Ab.vals, s);
+  dfree(Bb.pos, s); dfree(Bb.crd, s); dfree(Bb.vals, s);
+  if (rc == SPWS_OK && owner) {
+    owner->stream = s;
+    owner->blocks.push_back(opos);
+    for (size_t g = 0; g + 1 < gstart.size(); g++) {
+      owner->blocks.push_back(parts[g].crd);
+      owner->blocks.push_back(parts[g].vals);
+    }
+  }
+  return rc;
+}
+
+}  // namespace spws

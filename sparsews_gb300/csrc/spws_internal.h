@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/spws/taco_abi.h"
 #include "../../include/spws/spws_device.h"
@@ -72,6 +73,18 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
 // Coordinate-workspace SpGEMM (expand, stable radix sort, ordered run
 // reduction): C = A*B with every value summed in ascending-j order.
 int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgemm_stats* stats, cudaStream_t stream);
+
+// Memory behind a batch's per-instance result views (freed together).
+struct BatchBlocks {
+  std::vector<void*> blocks;
+  cudaStream_t stream = nullptr;
+};
+
+// C_i = A_i * B_i for `count` instances in one row-wise pipeline per group
+// (block-diagonal super-operands); C receives per-instance views whose memory
+// is recorded in `owner`.
+int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
+                   spws_batch_stats* stats, BatchBlocks* owner, cudaStream_t s);
 
 // Exclusive scan of `n` int32 counts into `out[0..n]` (out[n] = total), with
 // the total also returned through `total_dev` (int64, device) so callers can

@@ -21,18 +21,24 @@ import numpy as np
 
 
 def _coo_to_csr(rows, cols, vals, nrows):
-    order = np.lexsort((cols, rows))
-    rows = rows[order]
-    cols = cols[order].astype(np.int32)
-    vals = vals[order]
+    """Row-major sorted CSR from COO (rows/cols already sorted by (row, col)
+    when they come from _unique_coo; sorted here otherwise)."""
+    rows = np.asarray(rows, np.int64)
+    cols = np.asarray(cols, np.int64)
+    if len(rows) > 1 and not (np.all(rows[1:] >= rows[:-1])):
+        order = np.lexsort((cols, rows))
+        rows, cols, vals = rows[order], cols[order], vals[order]
     pos = np.zeros(nrows + 1, np.int64)
-    np.add.at(pos, rows.astype(np.int64) + 1, 1)
-    pos = np.cumsum(pos).astype(np.int32)
-    return pos, cols, vals
+    pos[1:] = np.cumsum(np.bincount(rows, minlength=nrows))
+    return pos.astype(np.int32), cols.astype(np.int32), vals
 
 
 def _unique_coo(rows, cols, n_cols):
-    key = np.unique(rows.astype(np.int64) * n_cols + cols.astype(np.int64))
+    """Distinct (row, col) pairs in row-major order (same result as
+    np.unique on the packed keys, computed with a sort)."""
+    key = np.sort(rows.astype(np.int64) * n_cols + cols.astype(np.int64))
+    if len(key):
+        key = key[np.concatenate(([True], key[1:] != key[:-1]))]
     return (key // n_cols), (key % n_cols)
 
 
@@ -96,23 +102,32 @@ def poisson_rows(n, mean=8.0, seed=42):
 
 
 def rmat_n(n, mean_deg, a=0.57, b=0.19, c=0.19, seed=42):
-    """R-MAT on an n x n matrix (n not necessarily a power of two): draws on
-    the enclosing power of two and keeps the edges inside n x n."""
+    """R-MAT on an n x n matrix for any n: mean_deg * n edge draws on the
+    enclosing 2^s x 2^s grid (two levels per random draw), folded into n x n
+    by taking coordinates modulo n; duplicates removed."""
     scale = max(1, int(np.ceil(np.log2(max(n, 2)))))
     rng = np.random.default_rng(seed)
-    big = 1 << scale
-    m = int(mean_deg * n * (big / n) ** 2 * 1.0) if n < big else int(mean_deg * n)
-    m = max(m, 1)
+    m = max(1, int(mean_deg * n))
+    # quadrant probabilities for two levels at once (16 outcomes)
+    q = np.array([a, b, c, 1.0 - a - b - c])
+    cdf2 = np.cumsum(np.outer(q, q).ravel())
+    cdf2[-1] = 1.0
     r = np.zeros(m, np.int64)
     cc = np.zeros(m, np.int64)
-    for _ in range(scale):
-        u = rng.random(m)
-        rowbit = u >= a + b
-        colbit = ((u >= a) & (u < a + b)) | (u >= a + b + c)
-        r = (r << 1) | rowbit
-        cc = (cc << 1) | colbit
-    keep = (r < n) & (cc < n)
-    rows, cols = _unique_coo(r[keep], cc[keep], n)
+    lev = 0
+    while lev < scale:
+        if scale - lev >= 2:
+            o = np.searchsorted(cdf2, rng.random(m), side="right")
+            q1, q2 = o // 4, o % 4
+            r = (r << 2) | ((q1 >> 1) << 1) | (q2 >> 1)
+            cc = (cc << 2) | ((q1 & 1) << 1) | (q2 & 1)
+            lev += 2
+        else:
+            u = rng.random(m)
+            r = (r << 1) | (u >= a + b)
+            cc = (cc << 1) | (((u >= a) & (u < a + b)) | (u >= a + b + c))
+            lev += 1
+    rows, cols = _unique_coo(r % n, cc % n, n)
     vals = uniform_vals(rng, len(rows))
     pos, crd, vals = _coo_to_csr(rows, cols, vals, n)
     return pos, crd, vals, n, n
