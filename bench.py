@@ -452,13 +452,189 @@ def bench_batched(args):
     print(json.dumps(line), flush=True)
 
 
+SERVED_MIX = (0.90, 0.09, 0.01)  # small products, R-MAT 2^18 products, TTM requests
+
+
+def served_operands(args, seed=42):
+    """Resident operands of the served config: a pool of batched-size products,
+    the R-MAT 2^18 degree-16 matrix, and TTM tensors of 1-5M nonzeros (Zipf
+    1.1 slices, uniform other modes, dims of the tensor config) with a dense
+    rank-32 factor. All seeded synthetic data."""
+    from sparsews_gb300 import gen
+    small = batch_workload(args.served_pool, seed)
+    big = gen.rmat(args.scale or RMAT["scale"], RMAT["deg"], seed=seed)
+    tensors = []
+    for t, nnz in enumerate((1_000_000, 5_000_000)):
+        i0, i1, i2, tv = gen.tensor3((50000, 40000, 20000), nnz, zipf_s=1.1, seed=seed + 10 + t)
+        tensors.append(((i0, i2, i1, tv), (50000, 20000, 40000)))  # CSF order (k, i, j): contract mode 3
+    factor = gen.dense_factor(20000, 32, seed=seed + 20)
+    return small, big, tensors, factor
+
+
+def served_requests(n, pools, seed):
+    """Request list [(kind, operand index)], kind 0 small / 1 R-MAT / 2 TTM."""
+    rng = np.random.default_rng(seed)
+    kinds = rng.choice(3, size=n, p=SERVED_MIX)
+    return [(int(k), int(rng.integers(0, pools[k]))) for k in kinds]
+
+
+def pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) * 1e3 if len(xs) else None
+
+
+def run_served(srv, submit, reqs, arrivals):
+    """Submit reqs at `arrivals` (seconds from start; None = all at once) from a
+    feeder thread, collect completions with wait_any and release each result.
+    Returns (wall seconds from first submit to last completion, infos)."""
+    infos = {}
+    kinds = {}
+    errors = []
+
+    def feeder():
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            if arrivals is not None:
+                dt = t0 + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+            try:
+                kinds[submit(r)] = r[0]
+            except Exception as e:  # noqa: BLE001 - reported below
+                errors.append(e)
+                return
+
+    th = threading.Thread(target=feeder)
+    th.start()
+    while len(infos) < len(reqs) and not errors:
+        t, info = srv.wait_any(timeout_ms=120000)
+        if info.status != 0:
+            errors.append(RuntimeError(f"request {t} failed with status {info.status}"))
+        infos[t] = info
+        srv.release(t)
+    th.join()
+    if errors:
+        raise errors[0]
+    t_first = min(i.t_submit for i in infos.values())
+    t_last = max(i.t_done for i in infos.values())
+    return t_last - t_first, [(kinds[t], infos[t]) for t in sorted(infos)]
+
+
+def latency_summary(done):
+    lat = [i.t_done - i.t_submit for _, i in done]
+    out = {"p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "mean_ms": float(np.mean(lat)) * 1e3}
+    for k, name in enumerate(("small", "rmat", "ttm")):
+        lk = [i.t_done - i.t_submit for kk, i in done if kk == k]
+        out[name] = {"count": len(lk), "p50_ms": pct(lk, 50), "p99_ms": pct(lk, 99)}
+    return out
+
+
+def bench_served(args):
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import build, served, taco
+    build.build()
+    L = sp.lib()
+    sp.check(L.spws_set_device(0))
+    t0 = time.perf_counter()
+    small, big, tensors, factor = served_operands(args)
+    gen_s = time.perf_counter() - t0
+    dsmall = [sp.DeviceCsr.upload(*A) for A in small]
+    dbig = sp.DeviceCsr.upload(*big)
+    dtens = [served.DeviceCsf3(c, d) for c, d in tensors]
+    dfac = served.DeviceFactor(factor)
+    pools = (len(dsmall), 1, len(dtens))
+
+    srv = served.Server(workers=args.served_workers, memory_budget=int(args.served_budget_gb * (1 << 30)))
+
+    def submit(r):
+        k, i = r
+        if k == 0:
+            return srv.submit_spgemm(dsmall[i], dsmall[i])
+        if k == 1:
+            return srv.submit_spgemm(dbig, dbig)
+        return srv.submit_ttm(dtens[i], dfac)
+
+    # warm-up: every kind through the server
+    warm = [(0, i % pools[0]) for i in range(32)] + [(1, 0)] * args.warmup + [(2, 0), (2, 1)]
+    run_served(srv, submit, warm, None)
+
+    n = args.served_requests
+    reqs = served_requests(n, pools, seed=7)
+    runs = []
+    with ClockSampler(0) as clk:
+        wall, done = run_served(srv, submit, reqs, None)  # offered load above capacity: throughput
+        cap = n / wall
+        runs.append(dict(rate="saturating", offered_per_s=None, solves_per_s=cap, **latency_summary(done)))
+        for frac in args.served_rates:
+            rate = frac * cap
+            rng = np.random.default_rng(int(frac * 1000))
+            arr = np.cumsum(rng.exponential(1.0 / rate, n))
+            reqs_r = served_requests(n, pools, seed=8 + int(frac * 100))
+            wall_r, done_r = run_served(srv, submit, reqs_r, arr)
+            runs.append(dict(rate=f"{frac:.2f}x capacity", offered_per_s=rate, solves_per_s=n / wall_r,
+                             **latency_summary(done_r)))
+    st = srv.stats()
+    srv.close()
+
+    # plain one-at-a-time: the same request list through the device entry points
+    outc = served.CooDev()
+    Ls = served._lib()
+    t0 = time.perf_counter()
+    for k, i in reqs:
+        if k == 2:
+            sp.check(Ls.spws_ttm_device(C.byref(dtens[i].t), C.byref(dfac.f), C.byref(outc), None))
+            Ls.spws_coo_release(C.byref(outc))
+        else:
+            c, _ = sp.spgemm_device(dsmall[i] if k == 0 else dbig, dsmall[i] if k == 0 else dbig)
+            c.release()
+    seq_dev = time.perf_counter() - t0
+    # plain one-at-a-time through the TACO entry points (host arrays in and out), per kind on a sample
+    per_kind = []
+    ttm_args = [(taco.csf3_from_coo(*c, d), taco.dcsr(*factor), d) for c, d in tensors]
+    for k in range(3):
+        reps = {0: min(args.plain_sample, 64), 1: 1, 2: len(ttm_args)}[k]
+        t0 = time.perf_counter()
+        for q in range(reps):
+            if k == 2:
+                Bt, Ft, d = ttm_args[q]
+                At = taco.init_coo((d[0], d[2], factor[4]))
+                sp.check(L.spws_coo_csf_dcsr_hash_compute(At.ptr(), Bt.ptr(), Ft.ptr(), 0))
+                taco.take_coo(At, 3, L.spws_free)
+            else:
+                A = small[q % len(small)] if k == 0 else big
+                At = taco.csr(*A)
+                Ct = taco.init_dc(A[3], A[4])
+                sp.check(L.spws_csr_csr_hash_compute(Ct.ptr(), At.ptr(), At.ptr(), 0))
+                taco.take_csr(Ct, A[3], L.spws_free)
+        per_kind.append((time.perf_counter() - t0) / reps)
+    abi_mean = sum(SERVED_MIX[k] * per_kind[k] for k in range(3))
+    line = {"metric": "served_solves_per_s", "value": cap, "unit": "solves/s", "n_gpus": 1,
+            "steps": 1 + len(args.served_rates), "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "served_spgemm_ttm_stream", "requests_per_run": n,
+                       "mix": {"small_batched_size": SERVED_MIX[0], "rmat_2^18_deg16": SERVED_MIX[1],
+                               "ttm_1M_5M_nnz_R32": SERVED_MIX[2]},
+                       "small_pool": len(small), "workers": args.served_workers,
+                       "memory_budget_gb": st.budget / (1 << 30), "arrivals": "Poisson at swept rates",
+                       "l2": "inputs resident; R-MAT operands and outputs far larger than L2"},
+            "p50_ms": runs[-1]["p50_ms"], "p99_ms": runs[-1]["p99_ms"], "runs": runs,
+            "admission": {"peak_reserved_gb": st.peak_reserved / (1 << 30), "admit_waits": int(st.admit_waits),
+                          "failed": int(st.failed)},
+            "one_at_a_time": {"device_entry_solves_per_s": n / seq_dev,
+                              "taco_abi_solves_per_s": 1.0 / abi_mean,
+                              "taco_abi_ms_per_kind": [x * 1e3 for x in per_kind],
+                              "speedup_vs_device_entry": cap / (n / seq_dev),
+                              "speedup_vs_taco_abi": cap * abi_mean},
+            "clocks": clk.summary(), "generation_s": gen_s}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spws", choices=["spws", "reference"])
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched"])
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched", "served"])
     ap.add_argument("--instances", type=int, default=1024,
                     help="batched workload: number of products (4096 holds ~220 GB of output at once)")
     ap.add_argument("--plain-sample", type=int, default=512, help="batched workload: one-at-a-time ABI sample")
@@ -468,11 +644,20 @@ def main():
     ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
                     help="products per step of the reference arm (all cores)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--served-requests", type=int, default=400, help="served workload: requests per run")
+    ap.add_argument("--served-pool", type=int, default=512, help="served workload: distinct small products")
+    ap.add_argument("--served-workers", type=int, default=8)
+    ap.add_argument("--served-budget-gb", type=float, default=120.0)
+    ap.add_argument("--served-rates", type=float, nargs="*", default=[0.5, 0.8],
+                    help="Poisson arrival rates as fractions of the saturating throughput")
     args = ap.parse_args()
     ws, rank, local, dist = dist_init()
     if args.workload == "batched":
         if rank == 0 and args.impl != "reference":
             bench_batched(args)
+    elif args.workload == "served":
+        if rank == 0 and args.impl != "reference":
+            bench_served(args)
     elif args.impl == "reference":
         bench_reference(args, ws, rank, dist)
     else:

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "abi_util.h"
+#include "served.h"
 #include "convert.h"
 #include "spws_internal.h"
 #include "tensor.h"
@@ -275,6 +276,217 @@ double COO_CSF_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C,
 void COO_CSF_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print) {
   (void)print;
   spws_coo_csf_dcsr_bucket_compute(A, B, C, w_cap);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Device-resident tensor operands (the served form's TTM requests use them).
+// ---------------------------------------------------------------------------
+namespace spws {
+
+Csf3Dev csf3_view(const spws_csf3_dev& t) {
+  Csf3Dev d;
+  d.d0 = t.dims[0];
+  d.d1 = t.dims[1];
+  d.d2 = t.dims[2];
+  d.nk = t.nroots;
+  d.nf = t.nfibers;
+  d.nnz = t.nnz;
+  d.roots = t.roots;
+  d.pos1 = t.pos1;
+  d.crd1 = t.crd1;
+  d.pos2 = t.pos2;
+  d.crd2 = t.crd2;
+  d.vals = t.vals;
+  return d;
+}
+
+FactorDense factor_view(const spws_factor_dev& f) {
+  FactorDense d;
+  d.rows = f.rows;
+  d.R = f.cols;
+  d.mw = f.mask_words;
+  d.dense = f.dense;
+  d.mask = f.mask;
+  return d;
+}
+
+int check_csf3(const spws_csf3_dev* t) {
+  if (!t || t->nroots < 0 || t->nfibers < 0 || t->nnz < 0 || t->dims[0] < 0 || t->dims[1] < 0 || t->dims[2] < 0 ||
+      !t->pos1 || !t->pos2 || (t->nroots > 0 && !t->roots) || (t->nfibers > 0 && !t->crd1) ||
+      (t->nnz > 0 && (!t->crd2 || !t->vals))) {
+    set_error("B: not a device CSF tensor");
+    return SPWS_ERR_INVALID;
+  }
+  return SPWS_OK;
+}
+
+int check_factor(const spws_factor_dev* f) {
+  if (!f || f->rows < 0 || f->cols < 0 || f->mask_words != std::max(1, (f->cols + 31) / 32) ||
+      (f->rows > 0 && (!f->dense || !f->mask))) {
+    set_error("F: not a device factor");
+    return SPWS_ERR_INVALID;
+  }
+  return SPWS_OK;
+}
+
+int ttm_on_stream(const spws_csf3_dev* B, const spws_factor_dev* F, spws_coo_dev* A, cudaStream_t s) {
+  SPWS_TRY(check_csf3(B));
+  SPWS_TRY(check_factor(F));
+  CooOut o;
+  const FactorDense f = factor_view(*F);
+  int rc = tensor_bucket(1, csf3_view(*B), f, nullptr, &o, s);
+  if (rc != SPWS_OK) {
+    for (auto& c : o.crd) dfree(c, s);
+    dfree(o.vals, s);
+    return rc;
+  }
+  A->order = 3;
+  A->nnz = o.n;
+  for (int d = 0; d < 3; d++) A->crd[d] = o.crd[d];
+  A->vals = o.vals;
+  return SPWS_OK;
+}
+
+}  // namespace spws
+
+extern "C" {
+
+int spws_csf3_upload(const taco_tensor_t* B, spws_csf3_dev* out) {
+  clear_error();
+  if (!out) {
+    set_error("out is NULL");
+    return SPWS_ERR_INVALID;
+  }
+  *out = spws_csf3_dev{};
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  CsfUp u;
+  SPWS_TRY(upload_csf(B, &u, ds->stream));
+  const Csf3Dev& d = u.d;
+  out->dims[0] = d.d0;
+  out->dims[1] = d.d1;
+  out->dims[2] = d.d2;
+  out->nroots = d.nk;
+  out->nfibers = d.nf;
+  out->nnz = d.nnz;
+  // take ownership of the uploaded arrays
+  out->roots = (int32_t*)u.roots.p;
+  out->pos1 = (int32_t*)u.pos1.p;
+  out->crd1 = (int32_t*)u.crd1.p;
+  out->pos2 = (int32_t*)u.pos2.p;
+  out->crd2 = (int32_t*)u.crd2.p;
+  out->vals = (double*)u.vals.p;
+  u.roots.p = u.pos1.p = u.crd1.p = u.pos2.p = u.crd2.p = u.vals.p = nullptr;
+  return SPWS_OK;
+}
+
+int spws_csf3_release(spws_csf3_dev* t) {
+  if (!t) return SPWS_OK;
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  for (void* p : {(void*)t->roots, (void*)t->pos1, (void*)t->crd1, (void*)t->pos2, (void*)t->crd2, (void*)t->vals})
+    dfree(p, ds->stream);
+  *t = spws_csf3_dev{};
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
+  return SPWS_OK;
+}
+
+int spws_factor_upload(const taco_tensor_t* F, spws_factor_dev* out) {
+  clear_error();
+  if (!out) {
+    set_error("out is NULL");
+    return SPWS_ERR_INVALID;
+  }
+  *out = spws_factor_dev{};
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  FactorDense f;
+  int rc = upload_factor(F, "F", &f, ds->stream);
+  if (rc != SPWS_OK) {
+    free_factor(&f, ds->stream);
+    return rc;
+  }
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
+  out->rows = f.rows;
+  out->cols = f.R;
+  out->mask_words = f.mw;
+  out->dense = f.dense;
+  out->mask = f.mask;
+  return SPWS_OK;
+}
+
+int spws_factor_release(spws_factor_dev* f) {
+  if (!f) return SPWS_OK;
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  dfree(f->dense, ds->stream);
+  dfree(f->mask, ds->stream);
+  *f = spws_factor_dev{};
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
+  return SPWS_OK;
+}
+
+int spws_ttm_device(const spws_csf3_dev* B, const spws_factor_dev* F, spws_coo_dev* A, float* ms) {
+  clear_error();
+  if (!A) {
+    set_error("A is NULL");
+    return SPWS_ERR_INVALID;
+  }
+  *A = spws_coo_dev{};
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  cudaEvent_t e0, e1;
+  SPWS_CUDA(cudaEventCreate(&e0));
+  SPWS_CUDA(cudaEventCreate(&e1));
+  cudaEventRecord(e0, ds->stream);
+  const int rc = ttm_on_stream(B, F, A, ds->stream);
+  cudaEventRecord(e1, ds->stream);
+  cudaEventSynchronize(e1);
+  if (ms) cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int spws_coo_download(const spws_coo_dev* A, int32_t* crd0, int32_t* crd1, int32_t* crd2, double* vals) {
+  clear_error();
+  if (!A || A->order < 1 || A->order > 3 || A->nnz < 0) {
+    set_error("A: not a device COO");
+    return SPWS_ERR_INVALID;
+  }
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  int32_t* dst[3] = {crd0, crd1, crd2};
+  const size_t n = (size_t)A->nnz;
+  if (n) {
+    for (int d = 0; d < A->order; d++) {
+      if (!dst[d] || !A->crd[d]) {
+        set_error("coordinate array is NULL");
+        return SPWS_ERR_INVALID;
+      }
+      SPWS_CUDA(cudaMemcpyAsync(dst[d], A->crd[d], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ds->stream));
+    }
+    if (!vals || !A->vals) {
+      set_error("vals is NULL");
+      return SPWS_ERR_INVALID;
+    }
+    SPWS_CUDA(cudaMemcpyAsync(vals, A->vals, sizeof(double) * n, cudaMemcpyDeviceToHost, ds->stream));
+  }
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
+  return SPWS_OK;
+}
+
+int spws_coo_release(spws_coo_dev* A) {
+  if (!A) return SPWS_OK;
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  for (auto& c : A->crd) dfree(c, ds->stream);
+  dfree(A->vals, ds->stream);
+  *A = spws_coo_dev{};
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
+  return SPWS_OK;
 }
 
 }  // extern "C"

@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cmath>
 
 #include "common.cuh"
 #include "sort.h"
@@ -165,7 +166,27 @@ struct PassArgs {
   int* err;            // set on internal inconsistency
   uint32_t* bmstore;   // heavy single-span rows: the symbolic pass keeps its bitmap
   const long long* bmoff;  // here (word offset per row) for the numeric pass; null = rebuild
+  // Time slicing: CTAs (k_light: warps of CTAs) with blockIdx.x < yield_ctas
+  // stop claiming rows once they have run yield_ns, so that kernels of other
+  // streams get SMs between CTA waves; the remaining CTAs never stop, so every
+  // row is processed whatever order the CTAs run in. yield_ctas = 0: every CTA
+  // runs until the queue is empty.
+  long long yield_ns;
+  int yield_ctas;
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Next work index from `counter`, or INT_MAX once this CTA (or warp) has used
+// its time slice (see PassArgs::yield_ns).
+__device__ __forceinline__ int claim_or_yield(int* counter, const PassArgs& a, unsigned long long t0) {
+  if ((int)blockIdx.x < a.yield_ctas && global_ns() - t0 > (unsigned long long)a.yield_ns) return INT_MAX;
+  return atomicAdd(counter, 1);
+}
 
 constexpr int kPieceLen = 256;  // B entries per warp work piece
 
@@ -299,9 +320,9 @@ __device__ __forceinline__ void build_bitmap(const PassArgs& a, int32_t q0, int3
   }
 }
 
-__device__ __forceinline__ int claim(int* counter, int* s_idx) {
+__device__ __forceinline__ int claim(int* counter, int* s_idx, const PassArgs& a, unsigned long long t0) {
   __syncthreads();
-  if (threadIdx.x == 0) *s_idx = atomicAdd(counter, 1);
+  if (threadIdx.x == 0) *s_idx = claim_or_yield(counter, a, t0);
   __syncthreads();
   return *s_idx;
 }
@@ -318,8 +339,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_symbolic(PassArgs a) {
   __shared__ int wsum[kWarps];
   __shared__ int s_idx;
   const int nwork = *a.nheavy;
+  const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
-    const int idx = claim(a.counter, &s_idx);
+    const int idx = claim(a.counter, &s_idx, a, t0);
     if (idx >= nwork) break;
     const int32_t i = a.order[idx];
     const RowInfo ri = a.info[i];
@@ -360,8 +382,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
   __shared__ int32_t s_wcol[kMaxWin + 1];
   for (int q = threadIdx.x; q < kAcc; q += kThreads) acc[q] = 0.0;
   const int nwork = *a.nheavy;
+  const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
-    const int idx = claim(a.counter, &s_idx);
+    const int idx = claim(a.counter, &s_idx, a, t0);
     if (idx >= nwork) break;
     const int32_t i = a.order[idx];
     const RowInfo ri = a.info[i];
@@ -552,9 +575,13 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
   double* val = reinterpret_cast<double*>(smem + sizeof(unsigned long long) * kLightMax * kLightWarps) +
                 (size_t)warp * kLightMax;
   const int lo_idx = *a.nheavy, hi_idx = *a.nwork;
+  const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
     int idx = 0;
-    if (lane == 0) idx = atomicAdd(a.light_counter, 1) + lo_idx;
+    if (lane == 0) {
+      idx = claim_or_yield(a.light_counter, a, t0);
+      idx = idx == INT_MAX ? INT_MAX : idx + lo_idx;
+    }
     idx = __shfl_sync(0xffffffffu, idx, 0);
     if (idx >= hi_idx) break;
     const int32_t i = a.order[idx];
@@ -626,32 +653,7 @@ constexpr size_t kNumSmem = sizeof(double) * kAcc + sizeof(uint32_t) * kSpanWord
 
 }  // namespace
 
-int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const SpgemmOpts& opt,
-                   spws_spgemm_stats* stats, cudaStream_t s) {
-  (void)opt;
-  const int32_t nA = A.nrows;
-  const int32_t ncols = B.ncols;
-  C->nrows = nA;
-  C->ncols = ncols;
-  C->nnz = 0;
-  C->pos = nullptr;
-  C->crd = nullptr;
-  C->vals = nullptr;
-
-  DeviceState* ds = nullptr;
-  SPWS_TRY(device_state(&ds));
-  cudaEvent_t ev[6];
-  for (auto& e : ev) SPWS_CUDA(cudaEventCreate(&e));
-  SPWS_CUDA(cudaEventRecord(ev[0], s));
-
-  SPWS_TRY(dalloc((void**)&C->pos, sizeof(int32_t) * ((size_t)nA + 1), s));
-  if (nA == 0) {
-    SPWS_CUDA(cudaMemsetAsync(C->pos, 0, sizeof(int32_t), s));
-    if (stats) *stats = spws_spgemm_stats{};
-    for (auto& e : ev) cudaEventDestroy(e);
-    return SPWS_OK;
-  }
-
+struct RowwisePlanImpl {
   struct Small {
     int hist[kBuckets];
     int cursor[kBuckets];
@@ -662,98 +664,45 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
     unsigned long long products;
     long long nnz;
   };
+  cudaStream_t s = nullptr;
+  CsrView A, B;
+  cudaEvent_t ev[6] = {};
+  bool have_events = false;
   Small* sm = nullptr;
   RowInfo* info = nullptr;
   int32_t* order = nullptr;
   int32_t* rowcnt = nullptr;
-  SPWS_TRY(dalloc((void**)&sm, sizeof(Small), s));
-  SPWS_TRY(dalloc((void**)&info, sizeof(RowInfo) * (size_t)nA, s));
-  SPWS_TRY(dalloc((void**)&order, sizeof(int32_t) * (size_t)nA, s));
-  SPWS_TRY(dalloc((void**)&rowcnt, sizeof(int32_t) * (size_t)nA, s));
-  SPWS_CUDA(cudaMemsetAsync(sm, 0, sizeof(Small), s));
-  SPWS_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int32_t) * (size_t)nA, s));
-
-  k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A.pos, A.crd, B.pos, B.crd, info, sm->hist, &sm->products,
-                                                      &sm->err);
-  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy);
-  k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, sm->cursor, order);
-  count_launch(3);
-  SPWS_CUDA(cudaGetLastError());
-
-  // Bitmaps of heavy single-span rows survive from the symbolic to the numeric
-  // pass (when they fit a memory budget), so the numeric pass reads them
-  // instead of going over the row's products a second time.
   int32_t* bmwords = nullptr;
   long long* bmoff = nullptr;
   uint32_t* bmstore = nullptr;
-  {
-    SPWS_TRY(dalloc((void**)&bmwords, sizeof(int32_t) * (size_t)nA, s));
-    SPWS_TRY(dalloc((void**)&bmoff, sizeof(long long) * (size_t)nA, s));
-    k_bitmap_words<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, bmwords);
-    count_launch(1);
-    long long* tot = &sm->nnz;  // reused: cleared again before the count scan
-    SPWS_TRY(scan_i32_to_i64(bmwords, bmoff, nA, tot, s));
-    long long words = 0;
-    SPWS_CUDA(cudaMemcpyAsync(&words, tot, sizeof(words), cudaMemcpyDeviceToHost, s));
-    SPWS_CUDA(cudaStreamSynchronize(s));
-    SPWS_CUDA(cudaMemsetAsync(tot, 0, sizeof(long long), s));
-    size_t free_b = 0, total_b = 0;
-    SPWS_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t bytes = (size_t)words * sizeof(uint32_t);
-    if (words > 0 && bytes <= free_b / 8) {
-      if (dalloc((void**)&bmstore, bytes, s) != SPWS_OK) {
-        clear_error();
-        bmstore = nullptr;
-      }
-    }
-  }
-  SPWS_CUDA(cudaEventRecord(ev[1], s));
-
+  size_t bmstore_bytes = 0;
   PassArgs pa{};
-  pa.bmstore = bmstore;
-  pa.bmoff = bmoff;
-  pa.Ap = A.pos;
-  pa.Aj = A.crd;
-  pa.Av = A.vals;
-  pa.Bp = B.pos;
-  pa.Bk = B.crd;
-  pa.Bv = B.vals;
-  pa.info = info;
-  pa.order = order;
-  pa.nwork = &sm->nwork;
-  pa.nheavy = &sm->nheavy;
-  pa.counter = &sm->counter[0];
-  pa.light_counter = &sm->counter[2];
-  pa.rowcnt = rowcnt;
-  pa.err = &sm->err;
-  SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
-  SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
-  int per_sym = 1, per_num = 1;
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sym, k_symbolic, kThreads, kSymSmem));
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_num, k_numeric, kThreads, kNumSmem));
-  k_symbolic<<<ds->sm_count * std::max(per_sym, 1), kThreads, kSymSmem, s>>>(pa);
-  SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
-  SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
-  int per_ls = 1, per_ln = 1;
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ls, k_light<false>, kLightWarps * 32, kLightSymSmem));
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ln, k_light<true>, kLightWarps * 32, kLightNumSmem));
-  k_light<false><<<ds->sm_count * std::max(per_ls, 1), kLightWarps * 32, kLightSymSmem, s>>>(pa);
-  count_launch(2);
-  SPWS_CUDA(cudaGetLastError());
-  SPWS_CUDA(cudaEventRecord(ev[2], s));
-
-  SPWS_TRY(scan_counts_i32(rowcnt, C->pos, nA, &sm->nnz, s));
-  SPWS_CUDA(cudaEventRecord(ev[3], s));
-
+  int per_num = 1, per_ln = 1;
   long long nnz = 0;
   unsigned long long products = 0;
-  int err = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&nnz, &sm->nnz, sizeof(nnz), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&products, &sm->products, sizeof(products), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&err, &sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
-  auto cleanup = [&] {
-    for (auto& e : ev) cudaEventDestroy(e);
+  bool empty = false;
+  long long yield_ns = 0;
+  int waves_sym = 1, waves_num = 1;
+
+  // CTA waves for a pass that runs `rate` products per microsecond, so that
+  // each wave lasts about one time slice (1 = persistent launch).
+  int waves(double rate) const {
+    if (yield_ns <= 0) return 1;
+    const double w = (double)products / (rate * (double)yield_ns * 1e-3);
+    return (int)std::min(256.0, std::max(1.0, std::ceil(w)));
+  }
+  // The pass arguments for a launch of `resident` x `w` CTAs: all but the
+  // last `resident` CTAs yield after their time slice.
+  PassArgs sliced(int resident, int w) const {
+    PassArgs p = pa;
+    p.yield_ns = yield_ns;
+    p.yield_ctas = w > 1 ? resident * (w - 1) : 0;
+    return p;
+  }
+
+  ~RowwisePlanImpl() {
+    if (have_events)
+      for (auto& e : ev) cudaEventDestroy(e);
     dfree(sm, s);
     dfree(info, s);
     dfree(order, s);
@@ -761,52 +710,208 @@ int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const Sp
     dfree(bmwords, s);
     dfree(bmoff, s);
     dfree(bmstore, s);
-  };
+  }
+};
+
+size_t rowwise_scratch_bytes(int32_t nrows) {
+  return sizeof(RowwisePlanImpl::Small) + (size_t)std::max(nrows, 1) * (sizeof(RowInfo) + 3 * sizeof(int32_t) +
+                                                                         sizeof(long long)) + 4096;
+}
+
+// Phase 1: row analysis, cost order, symbolic pass, scan into C->pos.
+// Allocates C->pos; returns the output nonzero count in plan->nnz.
+int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, const SpgemmOpts& opt,
+                          RowwisePlan* plan, cudaStream_t s) {
+  RowwisePlanImpl* P = new RowwisePlanImpl();
+  plan->impl = P;
+  P->s = s;
+  P->A = A;
+  P->B = B;
+  const int32_t nA = A.nrows;
+  C->nrows = nA;
+  C->ncols = B.ncols;
+  C->nnz = 0;
+  C->pos = nullptr;
+  C->crd = nullptr;
+  C->vals = nullptr;
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  for (auto& e : P->ev) SPWS_CUDA(cudaEventCreate(&e));
+  P->have_events = true;
+  SPWS_CUDA(cudaEventRecord(P->ev[0], s));
+  SPWS_TRY(dalloc((void**)&C->pos, sizeof(int32_t) * ((size_t)nA + 1), s));
+  if (nA == 0) {
+    SPWS_CUDA(cudaMemsetAsync(C->pos, 0, sizeof(int32_t), s));
+    P->empty = true;
+    plan->nnz = 0;
+    plan->products = 0;
+    return SPWS_OK;
+  }
+  SPWS_TRY(dalloc((void**)&P->sm, sizeof(RowwisePlanImpl::Small), s));
+  SPWS_TRY(dalloc((void**)&P->info, sizeof(RowInfo) * (size_t)nA, s));
+  SPWS_TRY(dalloc((void**)&P->order, sizeof(int32_t) * (size_t)nA, s));
+  SPWS_TRY(dalloc((void**)&P->rowcnt, sizeof(int32_t) * (size_t)nA, s));
+  SPWS_CUDA(cudaMemsetAsync(P->sm, 0, sizeof(RowwisePlanImpl::Small), s));
+  SPWS_CUDA(cudaMemsetAsync(P->rowcnt, 0, sizeof(int32_t) * (size_t)nA, s));
+  auto* sm = P->sm;
+
+  k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A.pos, A.crd, B.pos, B.crd, P->info, sm->hist,
+                                                      &sm->products, &sm->err);
+  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy);
+  k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, sm->cursor, P->order);
+  count_launch(3);
+  SPWS_CUDA(cudaGetLastError());
+
+  // Bitmaps of heavy single-span rows survive from the symbolic to the numeric
+  // pass (when they fit the memory budget), so the numeric pass reads them
+  // instead of going over the row's products a second time.
+  SPWS_TRY(dalloc((void**)&P->bmwords, sizeof(int32_t) * (size_t)nA, s));
+  SPWS_TRY(dalloc((void**)&P->bmoff, sizeof(long long) * (size_t)nA, s));
+  k_bitmap_words<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, P->bmwords);
+  count_launch(1);
+  SPWS_TRY(scan_i32_to_i64(P->bmwords, P->bmoff, nA, &sm->nnz, s));
+  long long words = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&words, &sm->nnz, sizeof(words), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&P->products, &sm->products, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  P->yield_ns = opt.yield_ns;
+  SPWS_CUDA(cudaMemsetAsync(&sm->nnz, 0, sizeof(long long), s));
+  size_t free_b = 0, total_b = 0;
+  SPWS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const size_t bytes = (size_t)words * sizeof(uint32_t);
+  const size_t cap = std::min(free_b / 8, opt.max_bitmap_bytes);
+  if (words > 0 && bytes <= cap) {
+    if (dalloc((void**)&P->bmstore, bytes, s) != SPWS_OK) {
+      clear_error();
+      P->bmstore = nullptr;
+    } else {
+      P->bmstore_bytes = bytes;
+    }
+  }
+  SPWS_CUDA(cudaEventRecord(P->ev[1], s));
+
+  PassArgs& pa = P->pa;
+  pa.bmstore = P->bmstore;
+  pa.bmoff = P->bmoff;
+  pa.Ap = A.pos;
+  pa.Aj = A.crd;
+  pa.Av = A.vals;
+  pa.Bp = B.pos;
+  pa.Bk = B.crd;
+  pa.Bv = B.vals;
+  pa.info = P->info;
+  pa.order = P->order;
+  pa.nwork = &sm->nwork;
+  pa.nheavy = &sm->nheavy;
+  pa.counter = &sm->counter[0];
+  pa.light_counter = &sm->counter[2];
+  pa.rowcnt = P->rowcnt;
+  pa.err = &sm->err;
+  SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
+  SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
+  int per_sym = 1;
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sym, k_symbolic, kThreads, kSymSmem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&P->per_num, k_numeric, kThreads, kNumSmem));
+  // products per microsecond of the whole GPU, R-MAT-like rows: sizes the CTA waves of time-sliced launches
+  constexpr double kSymRate = 5e5, kNumRate = 9e4;
+  P->waves_sym = P->waves(kSymRate);
+  P->waves_num = P->waves(kNumRate);
+  const int g_sym = ds->sm_count * std::max(per_sym, 1);
+  k_symbolic<<<g_sym * P->waves_sym, kThreads, kSymSmem, s>>>(P->sliced(g_sym, P->waves_sym));
+  SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
+  SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
+  int per_ls = 1;
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ls, k_light<false>, kLightWarps * 32, kLightSymSmem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&P->per_ln, k_light<true>, kLightWarps * 32, kLightNumSmem));
+  const int g_ls = ds->sm_count * std::max(per_ls, 1);
+  k_light<false><<<g_ls * P->waves_sym, kLightWarps * 32, kLightSymSmem, s>>>(P->sliced(g_ls, P->waves_sym));
+  count_launch(2);
+  SPWS_CUDA(cudaGetLastError());
+  SPWS_CUDA(cudaEventRecord(P->ev[2], s));
+
+  SPWS_TRY(scan_counts_i32(P->rowcnt, C->pos, nA, &sm->nnz, s));
+  SPWS_CUDA(cudaEventRecord(P->ev[3], s));
+
+  int err = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&P->nnz, &sm->nnz, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&P->products, &sm->products, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(&err, &sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaStreamSynchronize(s));
   if (err == 2) {
-    cleanup();
     set_error("a row of A has 2^31 or more products");
     return SPWS_ERR_CAPACITY;
   }
-  if (nnz > INT32_MAX) {
-    cleanup();
+  if (P->nnz > INT32_MAX) {
     set_error("output has more than INT32_MAX nonzeros; taco_tensor_t positions are int32");
     return SPWS_ERR_CAPACITY;
   }
+  plan->nnz = P->nnz;
+  plan->products = (int64_t)P->products;
+  plan->scratch_bytes = rowwise_scratch_bytes(nA) + P->bmstore_bytes;
+  return SPWS_OK;
+}
+
+// Phase 2: allocate C->crd/vals and run the numeric pass.
+int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* stats) {
+  RowwisePlanImpl* P = static_cast<RowwisePlanImpl*>(plan->impl);
+  cudaStream_t s = P->s;
+  if (P->empty) {
+    if (stats) *stats = spws_spgemm_stats{};
+    return SPWS_OK;
+  }
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  const long long nnz = P->nnz;
   C->nnz = nnz;
   SPWS_TRY(dalloc((void**)&C->crd, sizeof(int32_t) * (size_t)std::max<long long>(nnz, 1), s));
   SPWS_TRY(dalloc((void**)&C->vals, sizeof(double) * (size_t)std::max<long long>(nnz, 1), s));
-
-  pa.counter = &sm->counter[1];
-  pa.light_counter = &sm->counter[3];
+  PassArgs& pa = P->pa;
+  pa.counter = &P->sm->counter[1];
+  pa.light_counter = &P->sm->counter[3];
   pa.Cp = C->pos;
   pa.Ck = C->crd;
   pa.Cv = C->vals;
-  SPWS_CUDA(cudaEventRecord(ev[4], s));
-  k_numeric<<<ds->sm_count * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
-  k_light<true><<<ds->sm_count * std::max(per_ln, 1), kLightWarps * 32, kLightNumSmem, s>>>(pa);
+  SPWS_CUDA(cudaEventRecord(P->ev[4], s));
+  const int g_num = ds->sm_count * std::max(P->per_num, 1);
+  const int g_ln = ds->sm_count * std::max(P->per_ln, 1);
+  k_numeric<<<g_num * P->waves_num, kThreads, kNumSmem, s>>>(P->sliced(g_num, P->waves_num));
+  k_light<true><<<g_ln * P->waves_num, kLightWarps * 32, kLightNumSmem, s>>>(P->sliced(g_ln, P->waves_num));
   count_launch(2);
   SPWS_CUDA(cudaGetLastError());
-  SPWS_CUDA(cudaEventRecord(ev[5], s));
-
-  SPWS_CUDA(cudaMemcpyAsync(&err, &sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaEventRecord(P->ev[5], s));
+  int err = 0;
+  SPWS_CUDA(cudaMemcpyAsync(&err, &P->sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
   SPWS_CUDA(cudaStreamSynchronize(s));
   if (stats) {
-    stats->products = (int64_t)products;
+    stats->products = (int64_t)P->products;
     stats->nnz = nnz;
-    cudaEventElapsedTime(&stats->ms_setup, ev[0], ev[1]);
-    cudaEventElapsedTime(&stats->ms_symbolic, ev[1], ev[2]);
-    cudaEventElapsedTime(&stats->ms_scan, ev[2], ev[3]);
-    cudaEventElapsedTime(&stats->ms_numeric, ev[4], ev[5]);
+    cudaEventElapsedTime(&stats->ms_setup, P->ev[0], P->ev[1]);
+    cudaEventElapsedTime(&stats->ms_symbolic, P->ev[1], P->ev[2]);
+    cudaEventElapsedTime(&stats->ms_scan, P->ev[2], P->ev[3]);
+    cudaEventElapsedTime(&stats->ms_numeric, P->ev[4], P->ev[5]);
     stats->ms_total = stats->ms_setup + stats->ms_symbolic + stats->ms_scan + stats->ms_numeric;
     stats->chunk_width = kAcc;
-    stats->n_chunks = (ncols + kSpanBits - 1) / kSpanBits;
+    stats->n_chunks = (C->ncols + kSpanBits - 1) / kSpanBits;
   }
-  cleanup();
   if (err) {
     set_error("numeric pass wrote a different number of entries than the symbolic pass counted");
     return SPWS_ERR_CUDA;
   }
   return SPWS_OK;
+}
+
+void rowwise_plan_free(RowwisePlan* plan) {
+  delete static_cast<RowwisePlanImpl*>(plan->impl);
+  plan->impl = nullptr;
+}
+
+int spgemm_rowwise(const CsrView& A, const CsrView& B, spws_csr_dev* C, const SpgemmOpts& opt,
+                   spws_spgemm_stats* stats, cudaStream_t s) {
+  RowwisePlan plan;
+  int rc = rowwise_plan_symbolic(A, B, C, opt, &plan, s);
+  if (rc == SPWS_OK) rc = rowwise_plan_numeric(&plan, C, stats);
+  rowwise_plan_free(&plan);
+  return rc;
 }
 
 }  // namespace spws

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stddef.h>
+#include <cstdint>
 
 #include <string>
 #include <vector>
@@ -54,6 +56,11 @@ void dfree(void* p, cudaStream_t s);
 // ---- SpGEMM (row-wise, column-chunked dense workspace) ----
 struct SpgemmOpts {
   int accum_mode = SPWS_ACCUM_ATOMIC;
+  size_t max_bitmap_bytes = SIZE_MAX;  // cap on bitmaps kept between the passes
+  // > 0: the row kernels run as waves of CTAs that each stop after about this
+  // many nanoseconds, so that kernels of higher-priority streams get SMs in
+  // between (the served form); 0: persistent CTAs (fastest alone).
+  long long yield_ns = 0;
 };
 
 // Device CSR view used by the kernels (pointers on the device).
@@ -64,6 +71,21 @@ struct CsrView {
   const int32_t* crd = nullptr;
   const double* vals = nullptr;
 };
+
+// The row-wise pipeline in two phases, so a caller (the served form) can
+// admit a request by its exact output size between them.
+struct RowwisePlan {
+  void* impl = nullptr;
+  long long nnz = 0;          // output nonzeros (after the symbolic phase)
+  int64_t products = 0;
+  size_t scratch_bytes = 0;   // device scratch the plan holds until freed
+};
+int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, const SpgemmOpts& opt,
+                          RowwisePlan* plan, cudaStream_t s);
+int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* stats);
+void rowwise_plan_free(RowwisePlan* plan);
+// Scratch bound of a plan before its bitmaps (bytes), for admission.
+size_t rowwise_scratch_bytes(int32_t nrows);
 
 // Full pipeline on `stream`: C = A*B. Allocates C's arrays with dalloc.
 // `transpose_key` is reserved (0).

@@ -146,7 +146,8 @@ template <int MODE>
 __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, const long long* __restrict__ pstart,
                          const long long* __restrict__ starts, const int32_t* __restrict__ r0,
                          const int32_t* __restrict__ r1, const double* __restrict__ bv, Factor F0, Factor F1, int32_t R,
-                         int32_t j0, int32_t mw, double* __restrict__ partial, uint32_t* __restrict__ pmask) {
+                         int32_t j0, int32_t mw, int32_t pw, double* __restrict__ partial,
+                         uint32_t* __restrict__ pmask) {
   const int lane = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= npieces) return;
@@ -190,9 +191,9 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   for (int u = 0; u < kJpl; u++) {
     const int j = j0 + lane + 32 * u;
     const bool in = j < R;
-    if (in) partial[w * (int64_t)kTileR + (j - j0)] = acc[u];
+    if (in) partial[w * (int64_t)(32 * pw) + (j - j0)] = acc[u];
     const unsigned m = __ballot_sync(0xffffffffu, in && ((started >> u) & 1u));  // all lanes, one call site
-    if (lane == 0) pmask[w * (int64_t)(kTileR / 32) + u] = m;
+    if (lane == 0 && u < pw) pmask[w * (int64_t)pw + u] = m;
   }
   (void)mw;
 }
@@ -201,7 +202,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
 // segment's running values for this column tile (first present value
 // assigns, later ones add), and accumulate the presence mask.
 __global__ void k_combine(int64_t nseg, const long long* __restrict__ poff, const double* __restrict__ partial,
-                          const uint32_t* __restrict__ pmask, int32_t R, int32_t j0, int32_t mw,
+                          const uint32_t* __restrict__ pmask, int32_t R, int32_t j0, int32_t mw, int32_t pw,
                           double* __restrict__ segval, uint32_t* __restrict__ segmask) {
   const int lane = threadIdx.x & 31;
   const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -210,10 +211,10 @@ __global__ void k_combine(int64_t nseg, const long long* __restrict__ poff, cons
     const int j = j0 + lane + 32 * u;
     double v = 0.0;
     bool have = false;
-    for (long long pc = poff[s]; pc < poff[s + 1]; pc++) {
-      const uint32_t m = pmask[pc * (kTileR / 32) + u];
+    for (long long pc = poff[s]; u < pw && pc < poff[s + 1]; pc++) {
+      const uint32_t m = pmask[pc * pw + u];
       if ((m >> lane) & 1u) {
-        const double x = partial[pc * (int64_t)kTileR + (j - j0)];
+        const double x = partial[pc * (int64_t)(32 * pw) + (j - j0)];
         v = have ? __dadd_rn(v, x) : x;
         have = true;
       }
@@ -303,6 +304,24 @@ void free_factor(FactorDense* f, cudaStream_t s) {
   f->mask = nullptr;
 }
 
+size_t tensor_bucket_bound(int mode, const Csf3Dev& B, int32_t R, size_t* out_bytes) {
+  const size_t nnz = (size_t)std::max<int64_t>(B.nnz, 0);
+  const size_t mw = (size_t)std::max(1, (R + 31) / 32);
+  const size_t pw = std::min<size_t>(kTileR / 32, mw);
+  // segments (distinct output keys) and pieces (<= kPiece leaves of one segment)
+  const size_t keys = mode == 0 ? (size_t)std::max(B.d2, 1) : (size_t)std::max(B.d0, 1) * (size_t)std::max(B.d2, 1);
+  const size_t nseg = std::min(nnz, keys);
+  const size_t npieces = nseg + nnz / kPiece + 1;
+  const size_t per_leaf = 4 + 32 + 8 + 8 + 4 + 8 + 8 + 1;  // leaf_fib, sort keys/perm x2, r0/r1, bv, head, hpos, starts, sort tiles
+  size_t ws = 4 * (size_t)std::max(B.nf, 0) + per_leaf * nnz;
+  ws += nseg * (4 + 8 + 8 * (size_t)std::max(R, 1) + 4 * mw + 4 + 8);  // pc, poff, segval, segmask, segcnt, segoff
+  ws += npieces * (4 + 8 + 8 * 32 * pw + 4 * pw);                      // pseg, pstart, partial, pmask
+  ws += (size_t)1 << 20;                                                  // scan tiles, counters
+  const size_t outn = std::min(nseg * (size_t)std::max(R, 0), (size_t)INT32_MAX);
+  if (out_bytes) *out_bytes = outn * (mode == 0 ? 16 : 20);
+  return ws;
+}
+
 int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const FactorDense* F1, CooOut* out,
                   cudaStream_t s) {
   const int64_t nnz = B.nnz;
@@ -385,8 +404,10 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
                                     pstart.as<long long>());
     count_launch(1);
   }
-  SPWS_TRY(alloc(partial, sizeof(double) * (size_t)std::max<long long>(npieces, 1) * kTileR, s));
-  SPWS_TRY(alloc(pmask, sizeof(uint32_t) * (size_t)std::max<long long>(npieces, 1) * (kTileR / 32), s));
+  // per piece and column tile: 32*pw partial sums and pw presence words
+  const int32_t pw = std::min(kTileR / 32, mw);
+  SPWS_TRY(alloc(partial, sizeof(double) * (size_t)std::max<long long>(npieces, 1) * 32 * pw, s));
+  SPWS_TRY(alloc(pmask, sizeof(uint32_t) * (size_t)std::max<long long>(npieces, 1) * pw, s));
   SPWS_TRY(alloc(segval, sizeof(double) * (size_t)std::max<long long>(nseg, 1) * std::max(R, 1), s));
   SPWS_TRY(alloc(segmask, sizeof(uint32_t) * (size_t)std::max<long long>(nseg, 1) * mw, s));
   Factor f0{F0.dense, F0.mask, F0.rows, F0.R, F0.mw};
@@ -397,13 +418,13 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
       if (mode == 0)
         k_pieces<0><<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
                                        r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw,
-                                       partial.as<double>(), pmask.as<uint32_t>());
+                                       pw, partial.as<double>(), pmask.as<uint32_t>());
       else
         k_pieces<1><<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
                                        r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw,
-                                       partial.as<double>(), pmask.as<uint32_t>());
+                                       pw, partial.as<double>(), pmask.as<uint32_t>());
       k_combine<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, poff.as<long long>(), partial.as<double>(),
-                                                           pmask.as<uint32_t>(), R, j0, mw, segval.as<double>(),
+                                                           pmask.as<uint32_t>(), R, j0, mw, pw, segval.as<double>(),
                                                            segmask.as<uint32_t>());
       count_launch(2);
     }

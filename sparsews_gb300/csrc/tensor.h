@@ -1,6 +1,7 @@
 // Device-side tensor operands and the bucket-workspace MTTKRP/TTM driver (tensor.cu).
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 namespace spws {
@@ -47,6 +48,9 @@ void free_factor(FactorDense* f, cudaStream_t s);
 
 // mode 0: MTTKRP A(i,j) = sum B(k,l,i) F0(k,j) F1(l,j)  -> COO (i, j)
 // mode 1: TTM    A(k,j,l) = sum_i B(k,i,j) F0(i,l)      -> COO (k, j, l)
+// Device bytes tensor_bucket allocates besides its output (an upper bound),
+// and in *out_bytes an upper bound of the output's bytes.
+size_t tensor_bucket_bound(int mode, const Csf3Dev& B, int32_t R, size_t* out_bytes);
 int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const FactorDense* F1, CooOut* out,
                   cudaStream_t s);
 
