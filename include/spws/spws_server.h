@@ -122,6 +122,10 @@ typedef struct spws_request_info {
   double t_start;      /* a worker took it */
   double t_admit;      /* output admitted (numeric pass may start) */
   double t_done;       /* result complete in device memory */
+  float ms_setup;      /* SpGEMM: device time of the pipeline phases (spws_spgemm_stats) */
+  float ms_symbolic;
+  float ms_scan;
+  float ms_numeric;
 } spws_request_info;
 
 typedef struct spws_server_stats {

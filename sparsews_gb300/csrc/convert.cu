@@ -132,8 +132,9 @@ int validate_cc_device(const int32_t* oc, const int32_t* pos, const int32_t* ic,
     return SPWS_ERR_INVALID;
   }
   int32_t ends[2] = {0, 0};
-  SPWS_CUDA(cudaMemcpyAsync(&ends[0], pos, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&ends[1], pos + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  Readback rb(s);
+  SPWS_TRY(rb.get(&ends[0], pos, sizeof(int32_t)));
+  SPWS_TRY(rb.get(&ends[1], pos + nq, sizeof(int32_t)));
   int* bad = nullptr;
   SPWS_TRY(dalloc((void**)&bad, sizeof(int), s));
   SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
@@ -143,8 +144,8 @@ int validate_cc_device(const int32_t* oc, const int32_t* pos, const int32_t* ic,
     SPWS_CUDA(cudaGetLastError());
   }
   int hbad = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
+  SPWS_TRY(rb.get(&hbad, bad, sizeof(int)));
+  SPWS_TRY(rb.wait());
   dfree(bad, s);
   if (ends[0] != 0 || (int64_t)ends[1] != nnz) {
     set_error(std::string(what) + ": fiber positions must start at 0 and end at nnz");

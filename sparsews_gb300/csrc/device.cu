@@ -54,10 +54,14 @@ int device_state(DeviceState** out) {
   return SPWS_OK;
 }
 
+static thread_local cudaMemPool_t t_pool = nullptr;
+
+void set_thread_pool(cudaMemPool_t pool) { t_pool = pool; }
+
 int dalloc(void** p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMallocAsync(p, bytes, s);
+  cudaError_t e = t_pool ? cudaMallocFromPoolAsync(p, bytes, t_pool, s) : cudaMallocAsync(p, bytes, s);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     set_error("device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
@@ -69,6 +73,54 @@ int dalloc(void** p, size_t bytes, cudaStream_t s) {
 
 void dfree(void* p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
+}
+
+namespace {
+
+// Page-locked staging area of the calling thread (allocated on first use).
+struct HostStaging {
+  unsigned char* p = nullptr;
+  ~HostStaging() {
+    if (p) cudaFreeHost(p);
+  }
+};
+thread_local HostStaging t_staging;
+constexpr size_t kStagingBytes = 4096;
+
+__global__ void k_store_i64(long long* dst, long long v) { *dst = v; }
+
+}  // namespace
+
+int Readback::get(void* host, const void* dev, size_t bytes) {
+  if (!t_staging.p) {
+    void* p = nullptr;
+    SPWS_CUDA(cudaHostAlloc(&p, kStagingBytes, cudaHostAllocDefault));
+    t_staging.p = static_cast<unsigned char*>(p);
+  }
+  const size_t off = (used_ + 15) & ~(size_t)15;
+  if (n_ == 16 || off + bytes > kStagingBytes) {
+    set_error("internal: readback batch too large");
+    return SPWS_ERR_INVALID;
+  }
+  SPWS_CUDA(cudaMemcpyAsync(t_staging.p + off, dev, bytes, cudaMemcpyDeviceToHost, s_));
+  items_[n_++] = Item{host, off, bytes};
+  used_ = off + bytes;
+  return SPWS_OK;
+}
+
+int Readback::wait() {
+  SPWS_CUDA(cudaStreamSynchronize(s_));
+  for (int i = 0; i < n_; i++) memcpy(items_[i].host, t_staging.p + items_[i].off, items_[i].bytes);
+  n_ = 0;
+  used_ = 0;
+  return SPWS_OK;
+}
+
+int store_i64(long long* dst, long long v, cudaStream_t s) {
+  k_store_i64<<<1, 1, 0, s>>>(dst, v);
+  count_launch(1);
+  SPWS_CUDA(cudaGetLastError());
+  return SPWS_OK;
 }
 
 namespace {
@@ -102,8 +154,9 @@ int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, i
     return SPWS_ERR_INVALID;
   }
   int32_t ends[2] = {0, 0};
-  SPWS_CUDA(cudaMemcpyAsync(&ends[0], pos, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&ends[1], pos + nrows, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  Readback rb(s);
+  SPWS_TRY(rb.get(&ends[0], pos, sizeof(int32_t)));
+  SPWS_TRY(rb.get(&ends[1], pos + nrows, sizeof(int32_t)));
   int* bad = nullptr;
   SPWS_TRY(dalloc((void**)&bad, sizeof(int), s));
   SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
@@ -113,8 +166,8 @@ int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, i
     SPWS_CUDA(cudaGetLastError());
   }
   int hbad = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
+  SPWS_TRY(rb.get(&hbad, bad, sizeof(int)));
+  SPWS_TRY(rb.wait());
   dfree(bad, s);
   if (ends[0] != 0 || (int64_t)ends[1] != nnz) {
     set_error(std::string(what) + ": pos[0] must be 0 and pos[nrows] must equal nnz");
@@ -201,8 +254,9 @@ int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nro
     return SPWS_ERR_INVALID;
   }
   int32_t ends[2] = {0, 0};
-  SPWS_CUDA(cudaMemcpyAsync(&ends[0], pos, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&ends[1], pos + nrows, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  Readback rb(s);
+  SPWS_TRY(rb.get(&ends[0], pos, sizeof(int32_t)));
+  SPWS_TRY(rb.get(&ends[1], pos + nrows, sizeof(int32_t)));
   SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (nrows > 0) {
     k_validate_csr<<<(unsigned)((nrows + 7) / 8), 256, 0, s>>>(nrows, nnz, ncols, pos, crd, bad);
@@ -210,8 +264,8 @@ int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nro
     SPWS_CUDA(cudaGetLastError());
   }
   int hbad = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
+  SPWS_TRY(rb.get(&hbad, bad, sizeof(int)));
+  SPWS_TRY(rb.wait());
   if (ends[0] != 0 || (int64_t)ends[1] != nnz) {
     set_error(std::string(what) + ": pos[0] must be 0 and pos[nrows] must equal nnz");
     return SPWS_ERR_INVALID;

@@ -83,6 +83,12 @@ struct spws_server {
   size_t budget = 0;
   size_t bitmap_cap = 0;  // bytes of symbolic-pass bitmaps a SpGEMM request may keep
   cudaStream_t aux = nullptr;
+  cudaMemPool_t pool = nullptr;  // every allocation of the workers; mapped up front to the budget
+
+  ~spws_server() {
+    if (aux) cudaStreamDestroy(aux);
+    if (pool) cudaMemPoolDestroy(pool);
+  }
 
   std::mutex mu;
   std::condition_variable cv_work, cv_mem, cv_done;
@@ -187,6 +193,10 @@ struct spws_server {
       spws_spgemm_stats stats{};
       rc = spws::rowwise_plan_numeric(&plan, &r->C, &stats);
       r->info.products = stats.products;
+      r->info.ms_setup = stats.ms_setup;
+      r->info.ms_symbolic = stats.ms_symbolic;
+      r->info.ms_scan = stats.ms_scan;
+      r->info.ms_numeric = stats.ms_numeric;
       r->info.nnz = plan.nnz;
     }
     spws::rowwise_plan_free(&plan);
@@ -230,6 +240,7 @@ struct spws_server {
 
   void worker_main(bool takes_large) {
     cudaSetDevice(device);
+    spws::set_thread_pool(pool);
     int lo_prio = 0, hi_prio = 0;
     cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     cudaStream_t st_hi = nullptr, st_lo = nullptr;
@@ -318,6 +329,26 @@ int spws_server_create(const spws_server_config* cfg, spws_server** out) {
   S->budget = std::min(want, free_b / 10 * 9);
   S->bitmap_cap = S->budget / 16;
   SPWS_CUDA(cudaStreamCreateWithFlags(&S->aux, cudaStreamNonBlocking));
+  // The workers' own pool, grown to the budget now: growing a pool maps
+  // memory under a lock that stalls every CUDA call of the process (a large
+  // request's 15 GB output would hold up the small requests for milliseconds),
+  // so requests then only carve blocks out of memory that is already mapped.
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = S->device;
+  SPWS_CUDA(cudaMemPoolCreate(&S->pool, &props));
+  uint64_t keep = UINT64_MAX;
+  SPWS_CUDA(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  for (size_t want_map = S->budget; want_map >= ((size_t)1 << 30); want_map /= 2) {
+    void* p = nullptr;
+    if (cudaMallocFromPoolAsync(&p, want_map, S->pool, S->aux) == cudaSuccess) {
+      cudaFreeAsync(p, S->aux);
+      break;
+    }
+    (void)cudaGetLastError();
+  }
+  SPWS_CUDA(cudaStreamSynchronize(S->aux));
   try {
     for (int i = 0; i < S->workers; i++)
       S->threads.emplace_back([p = S.get(), large = i < S->large_workers] { p->worker_main(large); });
@@ -328,7 +359,6 @@ int spws_server_create(const spws_server_config* cfg, spws_server** out) {
     }
     S->cv_work.notify_all();
     for (auto& t : S->threads) t.join();
-    cudaStreamDestroy(S->aux);
     spws::set_error("could not start the worker threads");
     return SPWS_ERR_NOMEM;
   }
@@ -352,8 +382,7 @@ int spws_server_destroy(spws_server* S) {
     for (auto& kv : S->reqs) S->free_result(kv.second.get());
   }
   cudaStreamSynchronize(S->aux);
-  cudaStreamDestroy(S->aux);
-  delete S;
+  delete S;  // destroys the stream and the pool
   return SPWS_OK;
 }
 

@@ -194,8 +194,8 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
     k_run_starts<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, head, hpos, starts);
     count_launch(1);
     long long nruns = 0;
-    SPWS_CUDA(cudaMemcpyAsync(&nruns, tot, sizeof(long long), cudaMemcpyDeviceToHost, s));
-    SPWS_CUDA(cudaStreamSynchronize(s));
+    Readback rb(s);
+    if ((rc = rb.get(&nruns, tot, sizeof(long long))) != SPWS_OK || (rc = rb.wait()) != SPWS_OK) break;
     Part pt{nullptr, nullptr, nruns};
     if ((rc = dalloc((void**)&pt.crd, sizeof(int32_t) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
     if ((rc = dalloc((void**)&pt.val, sizeof(double) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 #include "sort.h"
@@ -653,6 +654,45 @@ constexpr size_t kNumSmem = sizeof(double) * kAcc + sizeof(uint32_t) * kSpanWord
 
 }  // namespace
 
+// Launch shapes of the row kernels on one device. The shared-memory opt-in
+// and occupancy queries run once per device: setting a kernel's attribute
+// while that kernel runs in another stream can wait for it, which would tie a
+// small product's latency to a large one's.
+struct RowKernelCfg {
+  int per_sym = 1, per_num = 1, per_ls = 1, per_ln = 1;
+  bool init = false;
+};
+
+int row_kernel_cfg(int device, RowKernelCfg* out) {
+  static std::mutex mu;
+  static RowKernelCfg cfg[64];
+  if (device < 0 || device >= 64) {
+    set_error("device ordinal out of range");
+    return SPWS_ERR_NO_DEVICE;
+  }
+  std::lock_guard<std::mutex> g(mu);
+  RowKernelCfg& c = cfg[device];
+  if (!c.init) {
+    SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
+    SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
+    SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
+    SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sym, k_symbolic, kThreads, kSymSmem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num, k_numeric, kThreads, kNumSmem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_ls, k_light<false>, kLightWarps * 32,
+                                                            kLightSymSmem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_ln, k_light<true>, kLightWarps * 32,
+                                                            kLightNumSmem));
+    c.per_sym = std::max(c.per_sym, 1);
+    c.per_num = std::max(c.per_num, 1);
+    c.per_ls = std::max(c.per_ls, 1);
+    c.per_ln = std::max(c.per_ln, 1);
+    c.init = true;
+  }
+  *out = c;
+  return SPWS_OK;
+}
+
 struct RowwisePlanImpl {
   struct Small {
     int hist[kBuckets];
@@ -771,16 +811,16 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   count_launch(1);
   SPWS_TRY(scan_i32_to_i64(P->bmwords, P->bmoff, nA, &sm->nnz, s));
   long long words = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&words, &sm->nnz, sizeof(words), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&P->products, &sm->products, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
+  Readback rb(s);
+  SPWS_TRY(rb.get(&words, &sm->nnz, sizeof(words)));
+  SPWS_TRY(rb.get(&P->products, &sm->products, sizeof(unsigned long long)));
+  SPWS_TRY(rb.wait());
   P->yield_ns = opt.yield_ns;
   SPWS_CUDA(cudaMemsetAsync(&sm->nnz, 0, sizeof(long long), s));
-  size_t free_b = 0, total_b = 0;
-  SPWS_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const size_t bytes = (size_t)words * sizeof(uint32_t);
-  const size_t cap = std::min(free_b / 8, opt.max_bitmap_bytes);
-  if (words > 0 && bytes <= cap) {
+  size_t free_b = 0, total_b = 0;
+  if (words > 0 && bytes <= opt.max_bitmap_bytes) SPWS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (words > 0 && bytes <= std::min(free_b / 8, opt.max_bitmap_bytes)) {
     if (dalloc((void**)&P->bmstore, bytes, s) != SPWS_OK) {
       clear_error();
       P->bmstore = nullptr;
@@ -807,22 +847,17 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   pa.light_counter = &sm->counter[2];
   pa.rowcnt = P->rowcnt;
   pa.err = &sm->err;
-  SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
-  SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
-  int per_sym = 1;
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sym, k_symbolic, kThreads, kSymSmem));
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&P->per_num, k_numeric, kThreads, kNumSmem));
+  RowKernelCfg kc;
+  SPWS_TRY(row_kernel_cfg(ds->device, &kc));
+  const int per_sym = kc.per_sym, per_ls = kc.per_ls;
+  P->per_num = kc.per_num;
+  P->per_ln = kc.per_ln;
   // products per microsecond of the whole GPU, R-MAT-like rows: sizes the CTA waves of time-sliced launches
   constexpr double kSymRate = 5e5, kNumRate = 9e4;
   P->waves_sym = P->waves(kSymRate);
   P->waves_num = P->waves(kNumRate);
   const int g_sym = ds->sm_count * std::max(per_sym, 1);
   k_symbolic<<<g_sym * P->waves_sym, kThreads, kSymSmem, s>>>(P->sliced(g_sym, P->waves_sym));
-  SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
-  SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
-  int per_ls = 1;
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ls, k_light<false>, kLightWarps * 32, kLightSymSmem));
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&P->per_ln, k_light<true>, kLightWarps * 32, kLightNumSmem));
   const int g_ls = ds->sm_count * std::max(per_ls, 1);
   k_light<false><<<g_ls * P->waves_sym, kLightWarps * 32, kLightSymSmem, s>>>(P->sliced(g_ls, P->waves_sym));
   count_launch(2);
@@ -833,10 +868,10 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   SPWS_CUDA(cudaEventRecord(P->ev[3], s));
 
   int err = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&P->nnz, &sm->nnz, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&P->products, &sm->products, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaMemcpyAsync(&err, &sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
+  SPWS_TRY(rb.get(&P->nnz, &sm->nnz, sizeof(long long)));
+  SPWS_TRY(rb.get(&P->products, &sm->products, sizeof(unsigned long long)));
+  SPWS_TRY(rb.get(&err, &sm->err, sizeof(int)));
+  SPWS_TRY(rb.wait());
   if (err == 2) {
     set_error("a row of A has 2^31 or more products");
     return SPWS_ERR_CAPACITY;
@@ -880,8 +915,9 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
   SPWS_CUDA(cudaGetLastError());
   SPWS_CUDA(cudaEventRecord(P->ev[5], s));
   int err = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&err, &P->sm->err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
+  Readback rb(s);
+  SPWS_TRY(rb.get(&err, &P->sm->err, sizeof(int)));
+  SPWS_TRY(rb.wait());
   if (stats) {
     stats->products = (int64_t)P->products;
     stats->nnz = nnz;
@@ -1046,15 +1082,9 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.light_counter = &hd->counter[2];
   pa.rowcnt = rowcnt;
   pa.err = &hd->err;
-  SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
-  SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
-  SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
-  SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
-  int per_sym = 1, per_num = 1, per_ls = 1, per_ln = 1;
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sym, k_symbolic, kThreads, kSymSmem));
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_num, k_numeric, kThreads, kNumSmem));
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ls, k_light<false>, kLightWarps * 32, kLightSymSmem));
-  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_ln, k_light<true>, kLightWarps * 32, kLightNumSmem));
+  RowKernelCfg kc;
+  SPWS_TRY(row_kernel_cfg(dev, &kc));
+  const int per_sym = kc.per_sym, per_num = kc.per_num, per_ls = kc.per_ls, per_ln = kc.per_ln;
   k_symbolic<<<sms * std::max(per_sym, 1), kThreads, kSymSmem, s>>>(pa);
   k_light<false><<<sms * std::max(per_ls, 1), kLightWarps * 32, kLightSymSmem, s>>>(pa);
   count_launch(2);

@@ -52,6 +52,9 @@ int device_state(DeviceState** out);  // current device's state, created on firs
 // Stream-ordered allocation helpers (cudaMallocAsync on the given stream).
 int dalloc(void** p, size_t bytes, cudaStream_t s);
 void dfree(void* p, cudaStream_t s);
+// dalloc on the calling thread draws from `pool` (nullptr: the device's
+// default pool). The served form gives its workers their own pool.
+void set_thread_pool(cudaMemPool_t pool);
 
 // ---- SpGEMM (row-wise, column-chunked dense workspace) ----
 struct SpgemmOpts {
@@ -71,6 +74,32 @@ struct CsrView {
   const int32_t* crd = nullptr;
   const double* vals = nullptr;
 };
+
+// Small device-to-host reads on stream `s`, staged through a page-locked
+// buffer of the calling thread. A cudaMemcpyAsync into pageable memory runs
+// synchronously and, while it waits for the stream's kernels, holds a driver
+// lock that stalls the CUDA calls of every other thread; staging in
+// page-locked memory keeps the copy asynchronous, and wait() synchronises only
+// this stream. Up to 16 reads and 4 KiB per batch.
+class Readback {
+ public:
+  explicit Readback(cudaStream_t s) : s_(s) {}
+  int get(void* host, const void* dev, size_t bytes);
+  int wait();
+
+ private:
+  struct Item {
+    void* host;
+    size_t off, bytes;
+  };
+  cudaStream_t s_;
+  Item items_[16];
+  int n_ = 0;
+  size_t used_ = 0;
+};
+
+// *dst = v on stream `s` (a one-thread kernel: no host memory involved).
+int store_i64(long long* dst, long long v, cudaStream_t s);
 
 // The row-wise pipeline in two phases, so a caller (the served form) can
 // admit a request by its exact output size between them.

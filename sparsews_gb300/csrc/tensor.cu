@@ -380,10 +380,10 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
     count_launch(1);
   }
   long long nseg = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&nseg, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
-  const long long nnz_ll = nnz;
-  SPWS_CUDA(cudaMemcpyAsync(starts.as<long long>() + nseg, &nnz_ll, sizeof(long long), cudaMemcpyHostToDevice, s));
+  Readback rb(s);
+  SPWS_TRY(rb.get(&nseg, tot.p, sizeof(long long)));
+  SPWS_TRY(rb.wait());
+  SPWS_TRY(store_i64(starts.as<long long>() + nseg, nnz, s));
 
   SPWS_TRY(alloc(pc, sizeof(int32_t) * (size_t)std::max<long long>(nseg, 1), s));
   SPWS_TRY(alloc(poff, sizeof(long long) * ((size_t)nseg + 1), s));
@@ -394,9 +394,9 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   }
   SPWS_TRY(scan_i32_to_i64(pc.as<int32_t>(), poff.as<long long>(), nseg, tot.as<long long>(), s));
   long long npieces = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&npieces, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
-  SPWS_CUDA(cudaMemcpyAsync(poff.as<long long>() + nseg, &npieces, sizeof(long long), cudaMemcpyHostToDevice, s));
+  SPWS_TRY(rb.get(&npieces, tot.p, sizeof(long long)));
+  SPWS_TRY(rb.wait());
+  SPWS_TRY(store_i64(poff.as<long long>() + nseg, npieces, s));
   SPWS_TRY(alloc(pseg, sizeof(int32_t) * (size_t)std::max<long long>(npieces, 1), s));
   SPWS_TRY(alloc(pstart, sizeof(long long) * (size_t)std::max<long long>(npieces, 1), s));
   if (nseg > 0) {
@@ -437,8 +437,8 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   }
   SPWS_TRY(scan_i32_to_i64(segcnt.as<int32_t>(), segoff.as<long long>(), nseg, tot.as<long long>(), s));
   long long total = 0;
-  SPWS_CUDA(cudaMemcpyAsync(&total, tot.p, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  SPWS_CUDA(cudaStreamSynchronize(s));
+  SPWS_TRY(rb.get(&total, tot.p, sizeof(long long)));
+  SPWS_TRY(rb.wait());
   if (total > INT32_MAX) {
     set_error("output has more than INT32_MAX nonzeros");
     return SPWS_ERR_CAPACITY;

@@ -40,7 +40,8 @@ class ServerConfig(C.Structure):
 class RequestInfo(C.Structure):
     _fields_ = [("kind", C.c_int32), ("status", C.c_int32), ("products", C.c_int64), ("nnz", C.c_int64),
                 ("reserved", C.c_uint64), ("t_submit", C.c_double), ("t_start", C.c_double),
-                ("t_admit", C.c_double), ("t_done", C.c_double)]
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("ms_setup", C.c_float),
+                ("ms_symbolic", C.c_float), ("ms_scan", C.c_float), ("ms_numeric", C.c_float)]
 
     @property
     def latency_s(self):
