@@ -189,16 +189,33 @@ __device__ __forceinline__ int claim_or_yield(int* counter, const PassArgs& a, u
   return atomicAdd(counter, 1);
 }
 
-constexpr int kPieceLen = 256;  // B entries per warp work piece
+constexpr int kPieceLen = 256;   // B entries per warp work piece of a long slice
+constexpr int kLongMin = 128;    // slices this long are cut into pieces; shorter ones are packed
+constexpr int kChunkLen = 128;   // packed entries per warp work item (4 rounds of 32 lanes)
 
-// Shared staging of one batch of j's: the B-row slice each thread loaded
-// (start, length), its A value, and the exclusive prefix of the number of
-// pieces of at most kPieceLen entries each slice is cut into.
+// Shared staging of one batch of j's. Every thread t loads one B-row slice
+// (start s[t], length len[t], A value a[t]). Long slices (>= kLongMin
+// entries) are cut into pieces of at most kPieceLen entries; pexcl[t] is the
+// exclusive prefix of the pieces. Short slices are packed into one flat
+// stream: the c-th short slice is slot[c] and starts at flat offset E[c]
+// (E[nshort] = the stream's length), so a warp's 32 lanes take 32 consecutive
+// entries of the stream whatever the slices' lengths.
 struct Batch {
   int32_t s[kThreads];
   int32_t len[kThreads];
   int32_t pexcl[kThreads + 1];
   double a[kThreads];
+  int32_t E[kThreads + 1];
+  int16_t slot[kThreads];
+};
+
+// Work of one loaded batch: pieces of long slices, then chunks of the
+// packed short-slice stream.
+struct BatchWork {
+  int pieces;       // long-slice pieces
+  int nshort;       // short slices
+  int short_total;  // entries in the packed stream
+  __device__ __forceinline__ int items() const { return pieces + (short_total + kChunkLen - 1) / kChunkLen; }
 };
 
 // Block exclusive scan of one int per thread. Returns the exclusive prefix;
@@ -229,12 +246,40 @@ __device__ __forceinline__ int32_t span_end(int32_t wlo) {
   return (int32_t)min((long long)wlo + kSpanBits, (long long)INT_MAX);
 }
 
+// Stores thread t's slice into the batch, classifies it long or short and
+// builds both work lists. Ends with a barrier.
+__device__ __forceinline__ BatchWork fill_batch(int32_t s, int32_t len, double av, Batch& b, int* wsum) {
+  const int t = threadIdx.x;
+  const bool is_long = len >= kLongMin;
+  const bool is_short = len > 0 && !is_long;
+  BatchWork w;
+  const int pex = block_excl_scan(is_long ? (len + kPieceLen - 1) / kPieceLen : 0, wsum, &w.pieces);
+  // count of short slices (high bits) and their entries (low 16 bits: at most 512 * 127)
+  int packed;
+  const int ex = block_excl_scan(is_short ? (len | (1 << 16)) : 0, wsum, &packed);
+  b.s[t] = s;
+  b.len[t] = len;
+  b.pexcl[t] = pex;
+  b.a[t] = av;
+  if (is_short) {
+    b.E[ex >> 16] = ex & 0xffff;
+    b.slot[ex >> 16] = (int16_t)t;
+  }
+  w.nshort = packed >> 16;
+  w.short_total = packed & 0xffff;
+  if (t == 0) {
+    b.pexcl[kThreads] = w.pieces;
+    b.E[w.nshort] = w.short_total;
+  }
+  __syncthreads();
+  return w;
+}
+
 // Loads batch [qb, qb + kThreads) of row i's A entries into `b`: the B-row
 // slice limited to columns in [clo, chi) when `clip` is set (found by binary
-// search in the sorted B row), else the whole B row. Returns the number of
-// pieces; `b.pexcl` holds their prefix. Ends with a barrier.
-__device__ __forceinline__ int load_batch(const PassArgs& a, int32_t qb, int32_t q1, bool want_a, bool clip,
-                                          int32_t clo, int32_t chi, Batch& b, int* wsum) {
+// search in the sorted B row), else the whole B row. Ends with a barrier.
+__device__ __forceinline__ BatchWork load_batch(const PassArgs& a, int32_t qb, int32_t q1, bool want_a, bool clip,
+                                                int32_t clo, int32_t chi, Batch& b, int* wsum) {
   const int32_t q = qb + threadIdx.x;
   int32_t s = 0, len = 0;
   double av = 0.0;
@@ -260,49 +305,97 @@ __device__ __forceinline__ int load_batch(const PassArgs& a, int32_t qb, int32_t
     len = e - s;
     if (want_a) av = __ldg(a.Av + q);
   }
-  int npieces;
-  const int ex = block_excl_scan((len + kPieceLen - 1) / kPieceLen, wsum, &npieces);
-  b.s[threadIdx.x] = s;
-  b.len[threadIdx.x] = len;
-  b.pexcl[threadIdx.x] = ex;
-  b.a[threadIdx.x] = av;
-  if (threadIdx.x == 0) b.pexcl[kThreads] = npieces;
-  __syncthreads();
-  return npieces;
+  return fill_batch(s, len, av, b, wsum);
 }
 
 // Calls f(column, B value, A value) for every entry of the batch. Warps take
-// the batch's pieces round-robin (pieces hold at most kPieceLen entries of one
-// slice, so the split is even up to the last piece) and their lanes stream a
-// piece with unit stride, so loads of B are coalesced. Each lane loads four
-// entries (column and, when VALS, value) before it uses any of them, so four
-// loads per lane are in flight per round trip.
+// work items round-robin: a piece (at most kPieceLen entries of one long
+// slice, lanes streaming it with unit stride) or a chunk of kChunkLen entries
+// of the packed short slices, where lane l takes entry base + l of each round
+// and finds its slice from the slices that start inside the round (a ballot
+// over the next 31 slice starts), so short slices keep all 32 lanes busy.
+// Loads of B are coalesced, and each lane loads four entries (column and,
+// when VALS, value) before it uses any of them.
 template <bool VALS, typename F>
-__device__ __forceinline__ void for_batch_entries(const Batch& b, int npieces, const int32_t* __restrict__ Bk,
-                                                  const double* __restrict__ Bv, F&& f) {
+__device__ __forceinline__ void for_batch_entries(const Batch& b, const BatchWork& bw,
+                                                  const int32_t* __restrict__ Bk, const double* __restrict__ Bv,
+                                                  F&& f) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int g = warp; g < npieces; g += kWarps) {
-    int lo = 0, hi = kThreads - 1;  // slice owning piece g: largest o with pexcl[o] <= g
-    while (lo < hi) {
-      const int m = (lo + hi + 1) >> 1;
-      if (b.pexcl[m] <= g) lo = m; else hi = m - 1;
-    }
-    const int first = (g - b.pexcl[lo]) * kPieceLen;
-    const int32_t p0 = b.s[lo] + first;
-    const int32_t p1 = b.s[lo] + min(b.len[lo], first + kPieceLen);
-    const double av = b.a[lo];
-    for (int32_t base = p0 + lane; base < p1; base += 128) {
+  const int items = bw.items();
+  for (int g = warp; g < items; g += kWarps) {
+    int32_t pos[4];
+    double av[4];
+    if (g < bw.pieces) {
+      int lo = 0, hi = kThreads - 1;  // slice owning piece g: largest o with pexcl[o] <= g
+      while (lo < hi) {
+        const int m = (lo + hi + 1) >> 1;
+        if (b.pexcl[m] <= g) lo = m; else hi = m - 1;
+      }
+      const int first = (g - b.pexcl[lo]) * kPieceLen;
+      const int32_t p0 = b.s[lo] + first;
+      const int32_t p1 = b.s[lo] + min(b.len[lo], first + kPieceLen);
+      const double a0 = b.a[lo];
+      for (int32_t base = p0; base < p1; base += 128) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int32_t p = base + 32 * u + lane;
+          pos[u] = p < p1 ? p : -1;
+          av[u] = a0;
+        }
+        int32_t col[4];
+        double bv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          col[u] = pos[u] >= 0 ? __ldg(Bk + pos[u]) : -1;
+          if (VALS) bv[u] = pos[u] >= 0 ? __ldg(Bv + pos[u]) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (col[u] >= 0) f(col[u], VALS ? bv[u] : 0.0, av[u]);
+      }
+    } else {
+      const int f0 = (g - bw.pieces) * kChunkLen;
+      const int f1 = min(bw.short_total, f0 + kChunkLen);
+      int lo = 0, hi = bw.nshort - 1;  // short slice holding entry f0: largest o with E[o] <= f0
+      while (lo < hi) {
+        const int m = (lo + hi + 1) >> 1;
+        if (b.E[m] <= f0) lo = m; else hi = m - 1;
+      }
+      int o0 = lo;  // slice holding the round's first entry
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int rb = f0 + 32 * u;
+        const int fl = rb + lane;
+        // lanes 1..31 look at the starts of the next 31 slices; those inside
+        // (rb, rb + 31] mark their offset in the round
+        const int nx = o0 + lane;
+        const int el = nx <= bw.nshort ? b.E[nx] : INT_MAX;
+        const unsigned bit = (lane >= 1 && el <= rb + 31) ? 1u << (el - rb) : 0u;
+        const unsigned starts = __reduce_or_sync(0xffffffffu, bit);
+        const int own = o0 + __popc(starts & (0xffffffffu >> (31 - lane)));
+        if (fl < f1) {
+          const int t = b.slot[own];
+          pos[u] = b.s[t] + (fl - b.E[own]);
+          av[u] = b.a[t];
+        } else {
+          pos[u] = -1;
+          av[u] = 0.0;
+        }
+        // slice holding rb + 32: the last one started in this round, or the
+        // next one if it starts exactly there
+        o0 += __popc(starts);
+        if (o0 + 1 <= bw.nshort && b.E[o0 + 1] <= rb + 32) o0++;
+      }
       int32_t col[4];
       double bv[4];
 #pragma unroll
       for (int u = 0; u < 4; u++) {
-        const int32_t p = base + 32 * u;
-        col[u] = p < p1 ? __ldg(Bk + p) : -1;
-        if (VALS) bv[u] = p < p1 ? __ldg(Bv + p) : 0.0;
+        col[u] = pos[u] >= 0 ? __ldg(Bk + pos[u]) : -1;
+        if (VALS) bv[u] = pos[u] >= 0 ? __ldg(Bv + pos[u]) : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < 4; u++)
-        if (col[u] >= 0) f(col[u], VALS ? bv[u] : 0.0, av);
+        if (col[u] >= 0) f(col[u], VALS ? bv[u] : 0.0, av[u]);
     }
   }
 }
@@ -312,8 +405,8 @@ __device__ __forceinline__ void for_batch_entries(const Batch& b, int npieces, c
 __device__ __forceinline__ void build_bitmap(const PassArgs& a, int32_t q0, int32_t q1, int32_t wlo, bool clip,
                                              uint32_t* bm, Batch& b, int* wsum) {
   for (int32_t qb = q0; qb < q1; qb += kThreads) {
-    const int total = load_batch(a, qb, q1, false, clip, wlo, clip ? span_end(wlo) : INT_MAX, b, wsum);
-    for_batch_entries<false>(b, total, a.Bk, a.Bv, [&](int32_t col, double, double) {
+    const BatchWork bw = load_batch(a, qb, q1, false, clip, wlo, clip ? span_end(wlo) : INT_MAX, b, wsum);
+    for_batch_entries<false>(b, bw, a.Bk, a.Bv, [&](int32_t col, double, double) {
       const int k = col - wlo;
       atomicOr(&bm[k >> 5], 1u << (k & 31));
     });
@@ -521,7 +614,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
         }
         const bool clip = multi || !whole;
         for (int32_t qb = q0; qb < q1; qb += kThreads) {
-          int npieces;
+          BatchWork bw;
           if (prebound) {  // slices from the bound table (one batch)
             const int t = threadIdx.x;
             int32_t s0 = 0, len = 0;
@@ -531,17 +624,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
               len = bnd[t * (nwin + 1) + win + 1] - s0;
               av = __ldg(a.Av + q0 + t);
             }
-            const int ex = block_excl_scan((len + kPieceLen - 1) / kPieceLen, wsum, &npieces);
-            b.s[t] = s0;
-            b.len[t] = len;
-            b.pexcl[t] = ex;
-            b.a[t] = av;
-            if (t == 0) b.pexcl[kThreads] = npieces;
-            __syncthreads();
+            bw = fill_batch(s0, len, av, b, wsum);
           } else {
-            npieces = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
+            bw = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
           }
-          for_batch_entries<true>(b, npieces, a.Bk, a.Bv, [&](int32_t col, double bv, double av) {
+          for_batch_entries<true>(b, bw, a.Bk, a.Bv, [&](int32_t col, double bv, double av) {
             const int k = col - wlo;
             const int w = k >> 5;
             const int rank = word_prefix(w) + __popc(bm[w] & ((1u << (k & 31)) - 1u));
