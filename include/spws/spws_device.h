@@ -63,6 +63,9 @@ int spws_csr_upload(const int32_t* pos, const int32_t* crd, const double* vals, 
                     spws_csr_dev* out);
 /* Copy a device CSR back into caller-provided host arrays (sizes from `m`). */
 int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double* vals);
+/* Overwrite the values of a device CSR with `m->nnz` host values (structure
+ * unchanged), e.g. before re-solving a batch plan. */
+int spws_csr_set_values(const spws_csr_dev* m, const double* vals);
 /* Release a device CSR allocated by the library (upload or spgemm). */
 int spws_csr_release(spws_csr_dev* m);
 
@@ -110,6 +113,52 @@ int spws_set_device(int device);
 int spws_spgemm_batched(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
                         spws_batch** batch, spws_batch_stats* stats);
 int spws_batch_release(spws_batch* batch);
+
+/* Tunable parameters of the row-wise pipeline (all products: plain, batched,
+ * served). Zero fields take the defaults.
+ *  light_max:    rows with fewer scalar products than this go to the
+ *                warp-per-row kernel, the others to a 512-thread CTA each
+ *                (a power of two in [32, 512]; default 512).
+ *  long_min:     B-row slices at least this long are cut into 256-entry
+ *                pieces, one warp each; shorter ones are packed into one
+ *                lane-dense stream ([32, 256]; default 128).
+ *  wide_windows: 1 = numeric windows of 18432 output ranks with one CTA per
+ *                SM; 0 = windows of 5120 ranks with two CTAs per SM. */
+typedef struct spws_tuning {
+  int32_t light_max;
+  int32_t long_min;
+  int32_t wide_windows;
+  int32_t reserved;
+} spws_tuning;
+
+/* Autotuner: runs the pipeline on A*B with every candidate tuning (light_max
+ * in {256, 512} x long_min in {64, 128, 256} x wide_windows in {0, 1}),
+ * `repeats` times each (>= 1), and returns the fastest by wall time in *best
+ * (and its time in *best_ms, may be NULL). The products are discarded. */
+int spws_autotune_spgemm(const spws_csr_dev* A, const spws_csr_dev* B, int32_t repeats, spws_tuning* best,
+                         float* best_ms);
+/* Autotuner for the batched form: the same candidates, timed on a batch of at
+ * most `sample` instances spread evenly over the given ones (0 = all). */
+int spws_autotune_batched(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, int32_t sample,
+                          int32_t repeats, spws_tuning* best, float* best_ms);
+/* spws_spgemm_csr_device / spws_spgemm_batched with a tuning (NULL = defaults). */
+int spws_spgemm_csr_device_tuned(const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
+                                 const spws_tuning* tuning, spws_spgemm_stats* stats);
+int spws_spgemm_batched_tuned(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
+                              spws_batch** batch, const spws_tuning* tuning, spws_batch_stats* stats);
+
+/* A batch kept for re-solving: spws_batch_plan_create runs the batched
+ * product like spws_spgemm_batched and keeps every group's symbolic result
+ * (output structure, row order, column bitmaps) and a CUDA graph of the
+ * numeric work. spws_batch_plan_execute replays that graph with one launch:
+ * it reads the instances' current values (same A_i / B_i arrays, structure
+ * unchanged) and rewrites the values of the C views in place. The views
+ * belong to the plan until spws_batch_plan_release. */
+typedef struct spws_batch_plan spws_batch_plan;
+int spws_batch_plan_create(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
+                           const spws_tuning* tuning, spws_batch_plan** plan, spws_batch_stats* stats);
+int spws_batch_plan_execute(spws_batch_plan* plan, float* ms);
+int spws_batch_plan_release(spws_batch_plan* plan);
 
 /* Block until the library's stream on the current device is idle. */
 int spws_device_sync(void);

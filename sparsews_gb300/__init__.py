@@ -40,6 +40,15 @@ class BatchStats(C.Structure):
                 ("ms_kernels", C.c_float), ("ms_total", C.c_float)]
 
 
+class Tuning(C.Structure):
+    """spws_tuning: zero fields take the defaults."""
+    _fields_ = [("light_max", C.c_int32), ("long_min", C.c_int32), ("wide_windows", C.c_int32),
+                ("reserved", C.c_int32)]
+
+    def __repr__(self):
+        return f"Tuning(light_max={self.light_max}, long_min={self.long_min}, wide_windows={self.wide_windows})"
+
+
 class SpgemmStats(C.Structure):
     _fields_ = [("products", C.c_int64), ("nnz", C.c_int64), ("ms_setup", C.c_float), ("ms_symbolic", C.c_float),
                 ("ms_scan", C.c_float), ("ms_numeric", C.c_float), ("ms_total", C.c_float),
@@ -93,6 +102,19 @@ def lib():
         "spws_csr_release": ([C.POINTER(CsrDev)], C.c_int),
         "spws_spgemm_csr_device": ([C.POINTER(CsrDev), C.POINTER(CsrDev), C.POINTER(CsrDev), C.c_int,
                                     C.POINTER(SpgemmStats)], C.c_int),
+        "spws_csr_set_values": ([C.POINTER(CsrDev), C.c_void_p], C.c_int),
+        "spws_spgemm_csr_device_tuned": ([C.POINTER(CsrDev), C.POINTER(CsrDev), C.POINTER(CsrDev),
+                                          C.POINTER(Tuning), C.POINTER(SpgemmStats)], C.c_int),
+        "spws_spgemm_batched_tuned": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p),
+                                       C.POINTER(Tuning), C.POINTER(BatchStats)], C.c_int),
+        "spws_autotune_spgemm": ([C.POINTER(CsrDev), C.POINTER(CsrDev), C.c_int32, C.POINTER(Tuning),
+                                  C.POINTER(C.c_float)], C.c_int),
+        "spws_autotune_batched": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(Tuning),
+                                   C.POINTER(C.c_float)], C.c_int),
+        "spws_batch_plan_create": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Tuning),
+                                    C.POINTER(C.c_void_p), C.POINTER(BatchStats)], C.c_int),
+        "spws_batch_plan_execute": ([C.c_void_p, C.POINTER(C.c_float)], C.c_int),
+        "spws_batch_plan_release": ([C.c_void_p], C.c_int),
     }
     for name, (argt, rest) in sig.items():
         f = getattr(L, name)
@@ -217,6 +239,13 @@ class DeviceCsr:
         check(L.spws_csr_upload(pos.ctypes.data, crd.ctypes.data, vals.ctypes.data, nrows, ncols, C.byref(d.m)))
         return d
 
+    def set_values(self, vals):
+        """Overwrite the values (same structure)."""
+        vals = np.ascontiguousarray(vals, np.float64)
+        if len(vals) != self.m.nnz:
+            raise ValueError("need one value per stored entry")
+        check(lib().spws_csr_set_values(C.byref(self.m), vals.ctypes.data))
+
     def download(self):
         L = lib()
         pos = np.empty(self.m.nrows + 1, np.int32)
@@ -237,13 +266,39 @@ class DeviceCsr:
             pass
 
 
-def spgemm_device(A, B, accum_mode=0):
+def spgemm_device(A, B, accum_mode=0, tuning=None):
     """C = A*B for DeviceCsr operands; returns (DeviceCsr C, SpgemmStats)."""
     L = lib()
     Cd = DeviceCsr()
     st = SpgemmStats()
-    check(L.spws_spgemm_csr_device(C.byref(A.m), C.byref(B.m), C.byref(Cd.m), accum_mode, C.byref(st)))
+    if tuning is None:
+        check(L.spws_spgemm_csr_device(C.byref(A.m), C.byref(B.m), C.byref(Cd.m), accum_mode, C.byref(st)))
+    else:
+        check(L.spws_spgemm_csr_device_tuned(C.byref(A.m), C.byref(B.m), C.byref(Cd.m), C.byref(tuning),
+                                             C.byref(st)))
     return Cd, st
+
+
+def autotune(A, B, repeats=1):
+    """The fastest Tuning for C = A*B (DeviceCsr operands) and its time in ms."""
+    t = Tuning()
+    ms = C.c_float()
+    check(lib().spws_autotune_spgemm(C.byref(A.m), C.byref(B.m), repeats, C.byref(t), C.byref(ms)))
+    return t, ms.value
+
+
+def _csr_array(ms):
+    return (CsrDev * max(len(ms), 1))(*[m.m for m in ms])
+
+
+def autotune_batched(As, Bs, sample=0, repeats=1):
+    """The fastest Tuning for the batched product of DeviceCsr lists, timed on
+    at most `sample` instances spread over the batch (0 = all)."""
+    t = Tuning()
+    ms = C.c_float()
+    check(lib().spws_autotune_batched(len(As), C.cast(_csr_array(As), C.c_void_p), C.cast(_csr_array(Bs), C.c_void_p),
+                                      sample, repeats, C.byref(t), C.byref(ms)))
+    return t, ms.value
 
 
 class Batch:
@@ -271,16 +326,60 @@ class Batch:
             pass
 
 
-def spgemm_batched(As, Bs):
+def spgemm_batched(As, Bs, tuning=None):
     """C_i = A_i * B_i for lists of DeviceCsr in one batched launch set."""
     L = lib()
     n = len(As)
-    Aarr = (CsrDev * max(n, 1))(*[a.m for a in As])
-    Barr = (CsrDev * max(n, 1))(*[b.m for b in Bs])
+    Aarr, Barr = _csr_array(As), _csr_array(Bs)
     Carr = (CsrDev * max(n, 1))()
     h = C.c_void_p()
     st = BatchStats()
-    check(L.spws_spgemm_batched(n, C.cast(Aarr, C.c_void_p), C.cast(Barr, C.c_void_p), C.cast(Carr, C.c_void_p),
-                                C.byref(h), C.byref(st)))
+    if tuning is None:
+        check(L.spws_spgemm_batched(n, C.cast(Aarr, C.c_void_p), C.cast(Barr, C.c_void_p),
+                                    C.cast(Carr, C.c_void_p), C.byref(h), C.byref(st)))
+    else:
+        check(L.spws_spgemm_batched_tuned(n, C.cast(Aarr, C.c_void_p), C.cast(Barr, C.c_void_p),
+                                          C.cast(Carr, C.c_void_p), C.byref(h), C.byref(tuning), C.byref(st)))
     views = [CsrDev(Carr[i].nrows, Carr[i].ncols, Carr[i].nnz, Carr[i].pos, Carr[i].crd, Carr[i].vals) for i in range(n)]
     return Batch(h, views, st)
+
+
+class BatchPlan:
+    """A batch kept for re-solving with new values (spws_batch_plan_*):
+    execute() replays the captured numeric graph and rewrites the views'
+    values from the instances' current values."""
+
+    def __init__(self, As, Bs, tuning=None):
+        L = lib()
+        n = len(As)
+        self.As, self.Bs = As, Bs  # the plan reads their arrays on every execute
+        Carr = (CsrDev * max(n, 1))()
+        self.h = C.c_void_p()
+        self.stats = BatchStats()
+        check(L.spws_batch_plan_create(n, C.cast(_csr_array(As), C.c_void_p), C.cast(_csr_array(Bs), C.c_void_p),
+                                       C.cast(Carr, C.c_void_p), C.byref(tuning) if tuning is not None else None,
+                                       C.byref(self.h), C.byref(self.stats)))
+        self.views = [CsrDev(Carr[i].nrows, Carr[i].ncols, Carr[i].nnz, Carr[i].pos, Carr[i].crd, Carr[i].vals)
+                      for i in range(n)]
+
+    def execute(self):
+        """Replay; returns the device time in ms."""
+        ms = C.c_float()
+        check(lib().spws_batch_plan_execute(self.h, C.byref(ms)))
+        return ms.value
+
+    def download(self, i):
+        if not self.h:
+            raise RuntimeError("plan already released")
+        return DeviceCsr(self.views[i], owns=False).download()
+
+    def release(self):
+        if self.h:
+            lib().spws_batch_plan_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass

@@ -237,9 +237,6 @@ int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double*
   return SPWS_OK;
 }
 
-struct spws_batch {
-  spws::BatchBlocks blocks;
-};
 
 int spws_spgemm_batched(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
                         spws_batch** batch, spws_batch_stats* stats) {
@@ -265,6 +262,20 @@ int spws_batch_release(spws_batch* batch) {
   if (!batch) return SPWS_OK;
   for (void* p : batch->blocks.blocks) dfree(p, batch->blocks.stream);
   delete batch;
+  return SPWS_OK;
+}
+
+int spws_csr_set_values(const spws_csr_dev* m, const double* vals) {
+  clear_error();
+  if (!m || m->nnz < 0 || (m->nnz > 0 && (!m->vals || !vals))) {
+    set_error("spws_csr_set_values: bad arguments");
+    return SPWS_ERR_INVALID;
+  }
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  if (m->nnz > 0)
+    SPWS_CUDA(cudaMemcpyAsync(m->vals, vals, sizeof(double) * (size_t)m->nnz, cudaMemcpyHostToDevice, ds->stream));
+  SPWS_CUDA(cudaStreamSynchronize(ds->stream));
   return SPWS_OK;
 }
 

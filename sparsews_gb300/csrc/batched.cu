@@ -9,11 +9,13 @@
 // launches. Instances are grouped so that a group's output positions fit
 // int32, the position type of taco_tensor_t; a group is a row range of A*.
 // The product of a group is split back into per-instance CSR views whose
-// positions start at 0 and whose columns are the instance's own.
+// positions start at 0; the kernels write each row's columns shifted back by
+// its instance's column offset, so the columns are the instance's own.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <climits>
+#include <string>
 #include <vector>
 
 #include "sort.h"
@@ -91,20 +93,14 @@ __global__ void k_split_pos(int count, const Inst* __restrict__ ia, const long l
   if (lr == 0 && t.rows == 0) inst_nnz_off[i] = base;
 }
 
-// Columns of a group's product back to each instance's own range.
-__global__ void k_split_crd(int count, const Inst* __restrict__ ib, const long long* __restrict__ row_offs,
-                            int first, int last, const long long* __restrict__ inst_nnz_off,
-                            long long group_nnz, int32_t* __restrict__ crd) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= group_nnz) return;
-  int lo = first, hi = last - 1;  // last instance of the group whose output starts at or before e
-  while (lo < hi) {
-    const int m = (lo + hi + 1) >> 1;
-    if (inst_nnz_off[m] <= e) lo = m; else hi = m - 1;
-  }
-  crd[e] -= ib[lo].col_off;
-  (void)row_offs;
-  (void)count;
+// Column shift of every super-matrix row: the column offset of its
+// instance's B block, which the row-wise kernels subtract from every column
+// they write, so each instance's product comes out in its own columns.
+__global__ void k_row_shift(int count, const Inst* __restrict__ ib, const long long* __restrict__ row_offs,
+                            int32_t total_rows, int32_t* __restrict__ shift) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= total_rows) return;
+  shift[r] = ib[find_inst(row_offs, count, r)].col_off;
 }
 
 // Products of each A row, summed per instance (an upper bound of the
@@ -140,8 +136,54 @@ __global__ void k_zero_rows(int count, const Inst* __restrict__ ia, int first, i
 
 }  // namespace
 
+struct BatchReplay {
+  cudaStream_t s = nullptr;
+  std::vector<void*> owned;  // assembled operands and instance tables
+  std::vector<RowwisePlan> plans;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int kernels = 0;  // kernel nodes per replay
+  ~BatchReplay() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& p : plans) rowwise_plan_free(&p);
+    for (void* p : owned) dfree(p, s);
+    if (s) cudaStreamSynchronize(s);
+  }
+};
+
+int batch_replay_execute(BatchReplay* r, float* ms) {
+  cudaEvent_t e0, e1;
+  SPWS_CUDA(cudaEventCreate(&e0));
+  SPWS_CUDA(cudaEventCreate(&e1));
+  SPWS_CUDA(cudaEventRecord(e0, r->s));
+  SPWS_CUDA(cudaGraphLaunch(r->exec, r->s));
+  SPWS_CUDA(cudaEventRecord(e1, r->s));
+  count_launch(r->kernels);
+  std::vector<int> errs(r->plans.size(), 0);
+  for (size_t g = 0; g < r->plans.size(); g += 16) {  // readback batches of at most 16
+    Readback rb(r->s);
+    for (size_t k = g; k < std::min(r->plans.size(), g + 16); k++)
+      if (const int* e = rowwise_plan_err(&r->plans[k])) SPWS_TRY(rb.get(&errs[k], e, sizeof(int)));
+    SPWS_TRY(rb.wait());
+  }
+  if (ms) cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (int e : errs)
+    if (e) {
+      set_error("numeric pass wrote a different number of entries than the symbolic pass counted");
+      return SPWS_ERR_CUDA;
+    }
+  return SPWS_OK;
+}
+
+void batch_replay_free(BatchReplay* r) { delete r; }
+
 int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
-                   spws_batch_stats* stats, BatchBlocks* owner, cudaStream_t s) {
+                   spws_batch_stats* stats, BatchBlocks* owner, cudaStream_t s, const SpgemmOpts& opt,
+                   BatchReplay** replay) {
+  if (replay) *replay = nullptr;
   if (count <= 0) return SPWS_OK;
   std::vector<Inst> ia(count), ib(count);
   std::vector<long long> arow(count), annz(count), bnnz(count), brow(count);
@@ -177,6 +219,7 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
   // device copies of the instance tables
   Inst *dia = nullptr, *dib = nullptr;
   long long *darow = nullptr, *dannz = nullptr, *dbrow = nullptr, *dbnnz = nullptr, *dnnzoff = nullptr;
+  int32_t* dshift = nullptr;
   SPWS_TRY(dalloc((void**)&dia, sizeof(Inst) * count, s));
   SPWS_TRY(dalloc((void**)&dib, sizeof(Inst) * count, s));
   SPWS_TRY(dalloc((void**)&darow, sizeof(long long) * count, s));
@@ -205,6 +248,11 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
   SPWS_TRY(dalloc((void**)&Bb.pos, sizeof(int32_t) * ((size_t)br + 1), s));
   SPWS_TRY(dalloc((void**)&Bb.crd, sizeof(int32_t) * (size_t)std::max(bz, 1LL), s));
   SPWS_TRY(dalloc((void**)&Bb.vals, sizeof(double) * (size_t)std::max(bz, 1LL), s));
+  SPWS_TRY(dalloc((void**)&dshift, sizeof(int32_t) * (size_t)std::max(ar, 1LL), s));
+  if (ar > 0) {
+    k_row_shift<<<(unsigned)((ar + 255) / 256), 256, 0, s>>>(count, dib, darow, (int32_t)ar, dshift);
+    count_launch(1);
+  }
   k_cat_pos<<<(unsigned)((ar + 256) / 256), 256, 0, s>>>(count, dia, darow, (int32_t)ar, az, Ab.pos);
   k_cat_pos<<<(unsigned)((br + 256) / 256), 256, 0, s>>>(count, dib, dbrow, (int32_t)br, bz, Bb.pos);
   if (az > 0) k_cat_ent<<<(unsigned)((az + 255) / 256), 256, 0, s>>>(count, dia, dannz, az, Ab.crd, Ab.vals);
@@ -250,6 +298,7 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
   int32_t* opos = nullptr;
   SPWS_TRY(dalloc((void**)&opos, sizeof(int32_t) * ((size_t)ar + count), s));
   std::vector<spws_csr_dev> parts;
+  std::vector<RowwisePlan> plans;
   long long total_nnz = 0, total_products = 0;
   float ms_kernels = 0.f;
   for (size_t g = 0; rc == SPWS_OK && g + 1 < gstart.size(); g++) {
@@ -272,9 +321,22 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
     Bv.vals = Bb.vals;
     spws_csr_dev Cg{};
     spws_spgemm_stats st{};
-    SpgemmOpts opt;
-    rc = spgemm_rowwise(Av, Bv, &Cg, opt, &st, s);
-    if (rc != SPWS_OK) break;
+    RowwisePlan plan;
+    SpgemmOpts gopt = opt;
+    gopt.col_shift = dshift + row0;  // columns come out per instance
+    rc = rowwise_plan_symbolic(Av, Bv, &Cg, gopt, &plan, s);
+    if (rc == SPWS_OK) rc = rowwise_plan_numeric(&plan, &Cg, &st);
+    if (rc != SPWS_OK || !replay) {
+      rowwise_plan_free(&plan);
+    } else {
+      plans.push_back(plan);
+    }
+    if (rc != SPWS_OK) {
+      dfree(Cg.pos, s);
+      dfree(Cg.crd, s);
+      dfree(Cg.vals, s);
+      break;
+    }
     total_nnz += Cg.nnz;
     total_products += st.products;
     ms_kernels += st.ms_total;
@@ -286,11 +348,6 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
     k_zero_rows<<<(unsigned)((last - first + 255) / 256), 256, 0, s>>>(count, dia, first, last, dnnzoff, row0, Cg.pos,
                                                                       opos + row0 + first);
     count_launch(1);
-    if (Cg.nnz > 0) {
-      k_split_crd<<<(unsigned)((Cg.nnz + 255) / 256), 256, 0, s>>>(count, dib, darow, first, last, dnnzoff, Cg.nnz,
-                                                                   Cg.crd);
-      count_launch(1);
-    }
     SPWS_CUDA(cudaGetLastError());
     parts.push_back(Cg);
   }
@@ -313,7 +370,7 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
         const long long end = (i + 1 < last) ? nnzoff[i + 1] : parts[g].nnz;
         C[i].nnz = end - nnzoff[i];
       }
-      dfree(parts[g].pos, s);
+      if (!replay) dfree(parts[g].pos, s);  // a replay's numeric kernels read the group positions again
     }
   } else {
     for (auto& p : parts) {
@@ -333,7 +390,62 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (rc == SPWS_OK && replay) {
+    // Capture the numeric work of the whole batch: gather the instances'
+    // current values into the super-operands and rerun every group's numeric
+    // kernels into the same C arrays.
+    auto* r = new BatchReplay();
+    r->s = s;
+    r->plans = plans;
+    plans.clear();
+    r->owned = {dia, dib, darow, dannz, dbrow, dbnnz, dnnzoff, dshift, Ab.pos, Ab.crd, Ab.vals,
+                Bb.pos, Bb.crd, Bb.vals};
+    for (auto& p : parts) r->owned.push_back(p.pos);
+    cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    int crc = ce == cudaSuccess ? SPWS_OK : SPWS_ERR_CUDA;
+    if (crc == SPWS_OK) {
+      if (az > 0) {
+        k_cat_ent<<<(unsigned)((az + 255) / 256), 256, 0, s>>>(count, dia, dannz, az, Ab.crd, Ab.vals);
+        r->kernels++;
+      }
+      if (bz > 0) {
+        k_cat_ent<<<(unsigned)((bz + 255) / 256), 256, 0, s>>>(count, dib, dbnnz, bz, Bb.crd, Bb.vals);
+        r->kernels++;
+      }
+      for (size_t g = 0; crc == SPWS_OK && g + 1 < gstart.size(); g++) {
+        crc = rowwise_plan_launch_numeric(&r->plans[g], s);
+        r->kernels += 2;
+      }
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+    r->graph = graph;
+    if (crc == SPWS_OK && ee == cudaSuccess && graph)
+      ce = cudaGraphInstantiate(&r->exec, graph, 0);
+    else
+      ce = ee != cudaSuccess ? ee : cudaErrorUnknown;
+    if (crc != SPWS_OK || ce != cudaSuccess) {
+      (void)cudaGetLastError();
+      if (crc == SPWS_OK) set_error(std::string("capturing the batch's numeric graph failed: ") + cudaGetErrorString(ce));
+      delete r;  // frees the group positions and operands with it
+      for (auto& p : parts) {
+        dfree(p.crd, s);
+        dfree(p.vals, s);
+      }
+      dfree(opos, s);
+      rc = crc != SPWS_OK ? crc : SPWS_ERR_CUDA;
+    } else {
+      *replay = r;
+    }
+    dia = dib = nullptr;
+    darow = dannz = dbrow = dbnnz = dnnzoff = nullptr;
+    dshift = nullptr;
+    Ab.pos = Ab.crd = Bb.pos = Bb.crd = nullptr;
+    Ab.vals = Bb.vals = nullptr;
+  }
+  for (auto& p : plans) rowwise_plan_free(&p);
   dfree(dia, s); dfree(dib, s); dfree(darow, s); dfree(dannz, s); dfree(dbrow, s); dfree(dbnnz, s); dfree(dnnzoff, s);
+  dfree(dshift, s);
   dfree(Ab.pos, s); dfree(Ab.crd, s); dfree(Ab.vals, s);
   dfree(Bb.pos, s); dfree(Bb.crd, s); dfree(Bb.vals, s);
   if (rc == SPWS_OK && owner) {

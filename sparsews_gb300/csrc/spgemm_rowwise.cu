@@ -42,11 +42,12 @@ constexpr int kSpanBits = 1 << 18;            // columns one bitmap covers
 constexpr int kSpanWords = kSpanBits / 32;    // 8192
 constexpr int kGroupWords = 2048;             // words per 32-bit prefix base (65536 bits)
 constexpr int kGroups = kSpanWords / kGroupWords;
-constexpr int kAcc = 5120;                    // ranks per numeric window (40 KB of FP64)
+constexpr int kAcc = 5120;                    // ranks per numeric window (40 KB of FP64), 2 CTAs per SM
+constexpr int kAccWide = 18432;               // the wide-window variant (144 KB), 1 CTA per SM
 constexpr int kBoundInts = 2048;              // shared table of per-(j, window) slice bounds
 constexpr int kMaxWin = 64;                   // windows per span with precomputed bounds
 constexpr int kBuckets = 66;                  // cost buckets: 0 = no products, b = 1 + floor(log2(P))
-constexpr int kLightBucket = 9;               // rows with bucket <= 9 (fewer than 512 products) go to k_light
+constexpr int kLightBucket = 9;               // default: rows with bucket <= 9 (fewer than 512 products) go to k_light
 constexpr int kLightMax = 512;                // staging entries per warp in k_light
 constexpr int kLightWarps = 8;                // warps per CTA in k_light
 
@@ -110,11 +111,11 @@ __global__ void k_row_info(int32_t nA, const int32_t* __restrict__ Ap, const int
 
 // Single thread: bucket offsets in descending cost order (bucket 0 excluded).
 __global__ void k_order_offsets(const int* __restrict__ hist, int* __restrict__ cursor, int* __restrict__ nwork,
-                                int* __restrict__ nheavy) {
+                                int* __restrict__ nheavy, int light_bucket) {
   if (threadIdx.x == 0) {
     int run = 0;
     for (int b = kBuckets - 1; b >= 1; b--) {
-      if (b == kLightBucket) *nheavy = run;
+      if (b == light_bucket) *nheavy = run;
       cursor[b] = run;
       run += hist[b];
     }
@@ -139,12 +140,13 @@ __global__ void k_order_scatter(int32_t nA, const RowInfo* __restrict__ info, in
 }
 
 // Words of bitmap a heavy row keeps between the passes (0: rebuilt instead).
-__global__ void k_bitmap_words(int32_t nA, const RowInfo* __restrict__ info, int32_t* __restrict__ words) {
+__global__ void k_bitmap_words(int32_t nA, const RowInfo* __restrict__ info, int32_t* __restrict__ words,
+                               int light_bucket) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nA) return;
   const RowInfo r = info[i];
   const long long span = (long long)r.hi - r.lo + 1;
-  words[i] = (cost_bucket(r.products) > kLightBucket && span <= kSpanBits) ? (int32_t)((span + 31) >> 5) : 0;
+  words[i] = (cost_bucket(r.products) > light_bucket && span <= kSpanBits) ? (int32_t)((span + 31) >> 5) : 0;
 }
 
 struct PassArgs {
@@ -174,6 +176,8 @@ struct PassArgs {
   // runs until the queue is empty.
   long long yield_ns;
   int yield_ctas;
+  int long_min;  // B-row slices at least this long are cut into pieces; shorter ones are packed (<= 256)
+  const int32_t* col_shift;  // per A row, subtracted from the written columns (nullptr: none)
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -190,7 +194,8 @@ __device__ __forceinline__ int claim_or_yield(int* counter, const PassArgs& a, u
 }
 
 constexpr int kPieceLen = 256;   // B entries per warp work piece of a long slice
-constexpr int kLongMin = 128;    // slices this long are cut into pieces; shorter ones are packed
+constexpr int kLongMin = 128;    // default: slices this long are cut into pieces; shorter ones are packed
+constexpr int kLongMinMax = 256; // packed stream length < 512 * 256 fits the 17-bit field of fill_batch
 constexpr int kChunkLen = 128;   // packed entries per warp work item (4 rounds of 32 lanes)
 
 // Shared staging of one batch of j's. Every thread t loads one B-row slice
@@ -248,25 +253,26 @@ __device__ __forceinline__ int32_t span_end(int32_t wlo) {
 
 // Stores thread t's slice into the batch, classifies it long or short and
 // builds both work lists. Ends with a barrier.
-__device__ __forceinline__ BatchWork fill_batch(int32_t s, int32_t len, double av, Batch& b, int* wsum) {
+__device__ __forceinline__ BatchWork fill_batch(int32_t s, int32_t len, double av, int long_min, Batch& b,
+                                                int* wsum) {
   const int t = threadIdx.x;
-  const bool is_long = len >= kLongMin;
+  const bool is_long = len >= long_min;
   const bool is_short = len > 0 && !is_long;
   BatchWork w;
   const int pex = block_excl_scan(is_long ? (len + kPieceLen - 1) / kPieceLen : 0, wsum, &w.pieces);
-  // count of short slices (high bits) and their entries (low 16 bits: at most 512 * 127)
+  // count of short slices (high bits) and their entries (low 17 bits: under 512 * 256)
   int packed;
-  const int ex = block_excl_scan(is_short ? (len | (1 << 16)) : 0, wsum, &packed);
+  const int ex = block_excl_scan(is_short ? (len | (1 << 17)) : 0, wsum, &packed);
   b.s[t] = s;
   b.len[t] = len;
   b.pexcl[t] = pex;
   b.a[t] = av;
   if (is_short) {
-    b.E[ex >> 16] = ex & 0xffff;
-    b.slot[ex >> 16] = (int16_t)t;
+    b.E[ex >> 17] = ex & 0x1ffff;
+    b.slot[ex >> 17] = (int16_t)t;
   }
-  w.nshort = packed >> 16;
-  w.short_total = packed & 0xffff;
+  w.nshort = packed >> 17;
+  w.short_total = packed & 0x1ffff;
   if (t == 0) {
     b.pexcl[kThreads] = w.pieces;
     b.E[w.nshort] = w.short_total;
@@ -305,7 +311,7 @@ __device__ __forceinline__ BatchWork load_batch(const PassArgs& a, int32_t qb, i
     len = e - s;
     if (want_a) av = __ldg(a.Av + q);
   }
-  return fill_batch(s, len, av, b, wsum);
+  return fill_batch(s, len, av, a.long_min, b, wsum);
 }
 
 // Calls f(column, B value, A value) for every entry of the batch. Warps take
@@ -461,11 +467,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_symbolic(PassArgs a) {
   }
 }
 
-// Numeric pass (see the file comment).
-__global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
+// Numeric pass (see the file comment), with windows of ACC ranks.
+template <int ACC>
+__global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  double* acc = reinterpret_cast<double*>(smem);                             // kAcc
-  uint32_t* bm = reinterpret_cast<uint32_t*>(smem + sizeof(double) * kAcc);  // kSpanWords
+  double* acc = reinterpret_cast<double*>(smem);                             // ACC
+  uint32_t* bm = reinterpret_cast<uint32_t*>(smem + sizeof(double) * ACC);   // kSpanWords
   uint16_t* wpre = reinterpret_cast<uint16_t*>(bm + kSpanWords);             // kSpanWords
   Batch& b = *reinterpret_cast<Batch*>(reinterpret_cast<unsigned char*>(wpre + kSpanWords));
   int32_t* bnd = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(&b) + sizeof(Batch));  // kBoundInts
@@ -474,7 +481,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
   __shared__ int s_idx;
   __shared__ int32_t s_cols[2];
   __shared__ int32_t s_wcol[kMaxWin + 1];
-  for (int q = threadIdx.x; q < kAcc; q += kThreads) acc[q] = 0.0;
+  for (int q = threadIdx.x; q < ACC; q += kThreads) acc[q] = 0.0;
   const int nwork = *a.nheavy;
   const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
@@ -485,6 +492,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
     const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
     const bool multi = (long long)ri.hi - ri.lo + 1 > kSpanBits;
     const int32_t row_end = a.Cp[i + 1];
+    const int32_t shift = a.col_shift ? a.col_shift[i] : 0;
     int32_t out = a.Cp[i];
     for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
       const int32_t wlo = (int32_t)wl;
@@ -548,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
           while (word) {
             const int bit = __ffs(word) - 1;
             word &= word - 1;
-            a.Ck[out + r] = wlo + w * 32 + bit;
+            a.Ck[out + r] = wlo + w * 32 + bit - shift;
             r++;
           }
         }
@@ -565,7 +573,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
         while (need-- > 0) word &= word - 1;
         return wlo + lo * 32 + (__ffs(word) - 1);
       };
-      const int nwin = (nnz_w + kAcc - 1) / kAcc;
+      const int nwin = (nnz_w + ACC - 1) / ACC;
       const int nj = q1 - q0;
       const int32_t span_hi = multi ? span_end(wlo) : INT_MAX;
       // Several windows and one batch of j's: find every (j, window) slice
@@ -574,7 +582,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
       const bool prebound = nwin > 1 && nwin <= kMaxWin && nj <= kThreads && nj * (nwin + 1) <= kBoundInts;
       if (prebound) {
         for (int w = threadIdx.x; w <= nwin; w += kThreads)
-          s_wcol[w] = w == 0 ? wlo : (w == nwin ? span_hi : col_of_rank(w * kAcc));
+          s_wcol[w] = w == 0 ? wlo : (w == nwin ? span_hi : col_of_rank(w * ACC));
         __syncthreads();
         for (int it = threadIdx.x; it < nj * (nwin + 1); it += kThreads) {
           const int t = it / (nwin + 1), w = it - t * (nwin + 1);
@@ -598,9 +606,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
         }
         __syncthreads();
       }
-      // values, one window of kAcc ranks at a time
-      for (int r0 = 0, win = 0; r0 < nnz_w; r0 += kAcc, win++) {
-        const int r1 = min(nnz_w, r0 + kAcc);
+      // values, one window of ACC ranks at a time
+      for (int r0 = 0, win = 0; r0 < nnz_w; r0 += ACC, win++) {
+        const int r1 = min(nnz_w, r0 + ACC);
         const bool whole = r0 == 0 && r1 == nnz_w;
         int32_t clo = wlo, chi = span_hi;
         if (!whole && !prebound) {  // columns of ranks r0 and r1 bound the window
@@ -624,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_numeric(PassArgs a) {
               len = bnd[t * (nwin + 1) + win + 1] - s0;
               av = __ldg(a.Av + q0 + t);
             }
-            bw = fill_batch(s0, len, av, b, wsum);
+            bw = fill_batch(s0, len, av, a.long_min, b, wsum);
           } else {
             bw = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
           }
@@ -696,9 +704,9 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
     for (int t = n + lane; t < S; t += 32) key[t] = ~0ull;
     __syncwarp();
     for (int k = 2; k <= S; k <<= 1) {
-      for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int j = k >> 1, lj = __ffs(k) - 2; j > 0; j >>= 1, lj--) {
         for (int t = lane; t < (S >> 1); t += 32) {
-          const int x = (t / j) * (j << 1) + (t % j), y = x + j;
+          const int x = ((t >> lj) << (lj + 1)) + (t & (j - 1)), y = x + j;
           const unsigned long long kx = key[x], ky = key[y];
           if ((kx > ky) == ((x & k) == 0)) {  // values stay put: a key's low bits index them
             key[x] = ky;
@@ -721,7 +729,7 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
         for (int q = p + 1; q < n && (uint32_t)(key[q] >> 32) == col; q++) v = __dadd_rn(v, val[(int)(uint32_t)key[q]]);
         const int r = rank + __popc(hm & ((1u << lane) - 1u));
         if (out + r < a.Cp[i + 1]) {  // never write past the row the symbolic pass sized
-          a.Ck[out + r] = (int32_t)col;
+          a.Ck[out + r] = (int32_t)col - (a.col_shift ? a.col_shift[i] : 0);
           a.Cv[out + r] = v;
         }
       }
@@ -736,17 +744,30 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
 constexpr size_t kLightSymSmem = sizeof(unsigned long long) * kLightMax * kLightWarps;
 constexpr size_t kLightNumSmem = (sizeof(unsigned long long) + sizeof(double)) * kLightMax * kLightWarps;
 constexpr size_t kSymSmem = sizeof(uint32_t) * kSpanWords + sizeof(Batch);
+constexpr size_t num_smem(int acc) {
+  return sizeof(double) * acc + sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords + sizeof(Batch) +
+         sizeof(int32_t) * kBoundInts;
+}
+constexpr size_t kNumSmemWide = num_smem(kAccWide);
 constexpr size_t kNumSmem = sizeof(double) * kAcc + sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords +
                             sizeof(Batch) + sizeof(int32_t) * kBoundInts;
 
 }  // namespace
+
+// Cost bucket below which rows go to k_light: rows with fewer than
+// `light_max` products (a power of two, at most kLightMax).
+int light_bucket_of(int light_max) {
+  int b = 0;
+  while ((1 << b) < light_max && b < 30) b++;
+  return std::min(b, kLightBucket);
+}
 
 // Launch shapes of the row kernels on one device. The shared-memory opt-in
 // and occupancy queries run once per device: setting a kernel's attribute
 // while that kernel runs in another stream can wait for it, which would tie a
 // small product's latency to a large one's.
 struct RowKernelCfg {
-  int per_sym = 1, per_num = 1, per_ls = 1, per_ln = 1;
+  int per_sym = 1, per_num = 1, per_num_wide = 1, per_ls = 1, per_ln = 1;
   bool init = false;
 };
 
@@ -761,17 +782,22 @@ int row_kernel_cfg(int device, RowKernelCfg* out) {
   RowKernelCfg& c = cfg[device];
   if (!c.init) {
     SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
-    SPWS_CUDA(cudaFuncSetAttribute(k_numeric, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
+    SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAcc>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
+    SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAccWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kNumSmemWide));
     SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
     SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
     SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sym, k_symbolic, kThreads, kSymSmem));
-    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num, k_numeric, kThreads, kNumSmem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num, k_numeric<kAcc>, kThreads, kNumSmem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num_wide, k_numeric<kAccWide>, kThreads,
+                                                            kNumSmemWide));
     SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_ls, k_light<false>, kLightWarps * 32,
                                                             kLightSymSmem));
     SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_ln, k_light<true>, kLightWarps * 32,
                                                             kLightNumSmem));
     c.per_sym = std::max(c.per_sym, 1);
     c.per_num = std::max(c.per_num, 1);
+    c.per_num_wide = std::max(c.per_num_wide, 1);
     c.per_ls = std::max(c.per_ls, 1);
     c.per_ln = std::max(c.per_ln, 1);
     c.init = true;
@@ -810,6 +836,8 @@ struct RowwisePlanImpl {
   bool empty = false;
   long long yield_ns = 0;
   int waves_sym = 1, waves_num = 1;
+  int light_bucket = kLightBucket;
+  bool wide = false;
 
   // CTA waves for a pass that runs `rate` products per microsecond, so that
   // each wave lasts about one time slice (1 = persistent launch).
@@ -884,7 +912,9 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
 
   k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A.pos, A.crd, B.pos, B.crd, P->info, sm->hist,
                                                       &sm->products, &sm->err);
-  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy);
+  P->light_bucket = light_bucket_of(opt.light_max);
+  P->wide = opt.wide_windows;
+  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy, P->light_bucket);
   k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, sm->cursor, P->order);
   count_launch(3);
   SPWS_CUDA(cudaGetLastError());
@@ -894,7 +924,7 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   // instead of going over the row's products a second time.
   SPWS_TRY(dalloc((void**)&P->bmwords, sizeof(int32_t) * (size_t)nA, s));
   SPWS_TRY(dalloc((void**)&P->bmoff, sizeof(long long) * (size_t)nA, s));
-  k_bitmap_words<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, P->bmwords);
+  k_bitmap_words<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, P->bmwords, P->light_bucket);
   count_launch(1);
   SPWS_TRY(scan_i32_to_i64(P->bmwords, P->bmoff, nA, &sm->nnz, s));
   long long words = 0;
@@ -934,10 +964,12 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   pa.light_counter = &sm->counter[2];
   pa.rowcnt = P->rowcnt;
   pa.err = &sm->err;
+  pa.long_min = opt.long_min;
+  pa.col_shift = opt.col_shift;
   RowKernelCfg kc;
   SPWS_TRY(row_kernel_cfg(ds->device, &kc));
   const int per_sym = kc.per_sym, per_ls = kc.per_ls;
-  P->per_num = kc.per_num;
+  P->per_num = P->wide ? kc.per_num_wide : kc.per_num;
   P->per_ln = kc.per_ln;
   // products per microsecond of the whole GPU, R-MAT-like rows: sizes the CTA waves of time-sliced launches
   constexpr double kSymRate = 5e5, kNumRate = 9e4;
@@ -996,7 +1028,10 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
   SPWS_CUDA(cudaEventRecord(P->ev[4], s));
   const int g_num = ds->sm_count * std::max(P->per_num, 1);
   const int g_ln = ds->sm_count * std::max(P->per_ln, 1);
-  k_numeric<<<g_num * P->waves_num, kThreads, kNumSmem, s>>>(P->sliced(g_num, P->waves_num));
+  if (P->wide)
+    k_numeric<kAccWide><<<g_num * P->waves_num, kThreads, kNumSmemWide, s>>>(P->sliced(g_num, P->waves_num));
+  else
+    k_numeric<kAcc><<<g_num * P->waves_num, kThreads, kNumSmem, s>>>(P->sliced(g_num, P->waves_num));
   k_light<true><<<g_ln * P->waves_num, kLightWarps * 32, kLightNumSmem, s>>>(P->sliced(g_ln, P->waves_num));
   count_launch(2);
   SPWS_CUDA(cudaGetLastError());
@@ -1013,7 +1048,7 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
     cudaEventElapsedTime(&stats->ms_scan, P->ev[2], P->ev[3]);
     cudaEventElapsedTime(&stats->ms_numeric, P->ev[4], P->ev[5]);
     stats->ms_total = stats->ms_setup + stats->ms_symbolic + stats->ms_scan + stats->ms_numeric;
-    stats->chunk_width = kAcc;
+    stats->chunk_width = P->wide ? kAccWide : kAcc;
     stats->n_chunks = (C->ncols + kSpanBits - 1) / kSpanBits;
   }
   if (err) {
@@ -1021,6 +1056,32 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
     return SPWS_ERR_CUDA;
   }
   return SPWS_OK;
+}
+
+int rowwise_plan_launch_numeric(RowwisePlan* plan, cudaStream_t s) {
+  RowwisePlanImpl* P = static_cast<RowwisePlanImpl*>(plan->impl);
+  if (P->empty) return SPWS_OK;
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  SPWS_CUDA(cudaMemsetAsync(&P->sm->counter[1], 0, sizeof(int), s));
+  SPWS_CUDA(cudaMemsetAsync(&P->sm->counter[3], 0, sizeof(int), s));
+  const int g_num = ds->sm_count * std::max(P->per_num, 1);
+  const int g_ln = ds->sm_count * std::max(P->per_ln, 1);
+  PassArgs pa = P->pa;
+  pa.counter = &P->sm->counter[1];
+  pa.light_counter = &P->sm->counter[3];
+  if (P->wide)
+    k_numeric<kAccWide><<<g_num, kThreads, kNumSmemWide, s>>>(pa);
+  else
+    k_numeric<kAcc><<<g_num, kThreads, kNumSmem, s>>>(pa);
+  k_light<true><<<g_ln, kLightWarps * 32, kLightNumSmem, s>>>(pa);
+  SPWS_CUDA(cudaGetLastError());
+  return SPWS_OK;
+}
+
+const int* rowwise_plan_err(const RowwisePlan* plan) {
+  const RowwisePlanImpl* P = static_cast<const RowwisePlanImpl*>(plan->impl);
+  return P->empty ? nullptr : &P->sm->err;
 }
 
 void rowwise_plan_free(RowwisePlan* plan) {
@@ -1149,7 +1210,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
 
   k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A->pos, A->crd, B->pos, B->crd, info, hd->hist,
                                                       &hd->products, &hd->err);
-  k_order_offsets<<<1, 32, 0, s>>>(hd->hist, hd->cursor, &hd->nwork, &hd->nheavy);
+  k_order_offsets<<<1, 32, 0, s>>>(hd->hist, hd->cursor, &hd->nwork, &hd->nheavy, kLightBucket);
   k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, hd->cursor, order);
   count_launch(3);
   SPWS_CUDA(cudaGetLastError());
@@ -1169,6 +1230,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.light_counter = &hd->counter[2];
   pa.rowcnt = rowcnt;
   pa.err = &hd->err;
+  pa.long_min = kLongMin;
   RowKernelCfg kc;
   SPWS_TRY(row_kernel_cfg(dev, &kc));
   const int per_sym = kc.per_sym, per_num = kc.per_num, per_ls = kc.per_ls, per_ln = kc.per_ln;
@@ -1197,7 +1259,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.Cp = C_pos;
   pa.Ck = C_crd;
   pa.Cv = C_vals;
-  k_numeric<<<sms * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
+  k_numeric<kAcc><<<sms * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
   k_light<true><<<sms * std::max(per_ln, 1), kLightWarps * 32, kLightNumSmem, s>>>(pa);
   count_launch(2);
   SPWS_CUDA(cudaGetLastError());

@@ -64,6 +64,13 @@ struct SpgemmOpts {
   // many nanoseconds, so that kernels of higher-priority streams get SMs in
   // between (the served form); 0: persistent CTAs (fastest alone).
   long long yield_ns = 0;
+  // Tunables (the autotuner picks them per workload):
+  int light_max = 512;        // rows with fewer products go to the warp-per-row kernel (power of two <= 512)
+  int long_min = 128;         // B-row slices this long are cut into pieces, shorter ones packed (<= 256)
+  bool wide_windows = false;  // numeric windows of 18432 ranks at 1 CTA/SM instead of 5120 at 2 CTAs/SM
+  // Per A row, an amount subtracted from every column written for that row
+  // (the batched form writes each instance's own columns); nullptr: none.
+  const int32_t* col_shift = nullptr;
 };
 
 // Device CSR view used by the kernels (pointers on the device).
@@ -113,6 +120,12 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
                           RowwisePlan* plan, cudaStream_t s);
 int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* stats);
 void rowwise_plan_free(RowwisePlan* plan);
+// After rowwise_plan_numeric: launch the numeric kernels again on `s` into the
+// same C arrays (new values, same structure). Allocates nothing and does not
+// synchronise, so it can be captured in a CUDA graph; 2 kernels.
+int rowwise_plan_launch_numeric(RowwisePlan* plan, cudaStream_t s);
+// Device flag the numeric kernels set on an inconsistency (nullptr: empty plan).
+const int* rowwise_plan_err(const RowwisePlan* plan);
 // Scratch bound of a plan before its bitmaps (bytes), for admission.
 size_t rowwise_scratch_bytes(int32_t nrows);
 
@@ -131,11 +144,29 @@ struct BatchBlocks {
   cudaStream_t stream = nullptr;
 };
 
+}  // namespace spws
+
+// Owner of a batch's results (the opaque handle of spws_device.h).
+struct spws_batch {
+  spws::BatchBlocks blocks;
+};
+
+namespace spws {
+
 // C_i = A_i * B_i for `count` instances in one row-wise pipeline per group
 // (block-diagonal super-operands); C receives per-instance views whose memory
 // is recorded in `owner`.
 int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
-                   spws_batch_stats* stats, BatchBlocks* owner, cudaStream_t s);
+                   spws_batch_stats* stats, BatchBlocks* owner, cudaStream_t s, const SpgemmOpts& opt = SpgemmOpts(),
+                   struct BatchReplay** replay = nullptr);
+
+// A batch kept for re-solving with new values and the same structure: the
+// assembled operands, every group's symbolic plan and a CUDA graph of the
+// numeric work (value gather, numeric kernels, column split), replayed by
+// batch_replay_execute with one graph launch.
+struct BatchReplay;
+int batch_replay_execute(BatchReplay* r, float* ms);
+void batch_replay_free(BatchReplay* r);
 
 // Exclusive scan of `n` int32 counts into `out[0..n]` (out[n] = total), with
 // the total also returned through `total_dev` (int64, device) so callers can

@@ -18,6 +18,7 @@ def mirrors():
         "spws_csr_dev": sp.CsrDev,
         "spws_spgemm_stats": sp.SpgemmStats,
         "spws_batch_stats": sp.BatchStats,
+        "spws_tuning": sp.Tuning,
         "taco_tensor_t": taco.TacoTensor,
         "spws_csf3_dev": served.Csf3Dev,
         "spws_factor_dev": served.FactorDev,
