@@ -212,6 +212,7 @@ struct Batch {
   double a[kThreads];
   int32_t E[kThreads + 1];
   int16_t slot[kThreads];
+  unsigned long long wsum[kWarps];  // per-warp totals of fill_batch's scan
 };
 
 // Work of one loaded batch: pieces of long slices, then chunks of the
@@ -247,6 +248,30 @@ __device__ __forceinline__ int block_excl_scan(int v, int* wsum, int* total) {
   return before + incl - v;
 }
 
+// Block exclusive scan of one 64-bit value per thread (two barriers).
+__device__ __forceinline__ unsigned long long block_excl_scan64(unsigned long long v, unsigned long long* wsum,
+                                                                unsigned long long* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  unsigned long long before = 0, t = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    const unsigned long long x = wsum[w];
+    before += w < warp ? x : 0;
+    t += x;
+  }
+  __syncthreads();
+  *total = t;
+  return before + incl - v;
+}
+
 __device__ __forceinline__ int32_t span_end(int32_t wlo) {
   return (int32_t)min((long long)wlo + kSpanBits, (long long)INT_MAX);
 }
@@ -258,21 +283,27 @@ __device__ __forceinline__ BatchWork fill_batch(int32_t s, int32_t len, double a
   const int t = threadIdx.x;
   const bool is_long = len >= long_min;
   const bool is_short = len > 0 && !is_long;
+  // One scan of three fields: long-slice pieces (bits 0-23: at most
+  // 2^31 / kPieceLen + kThreads), short slices (bits 24-33) and their
+  // entries (bits 34-50: under kThreads * kLongMinMax).
+  const unsigned long long v = is_long ? (unsigned long long)((len + kPieceLen - 1) / kPieceLen)
+                                       : (is_short ? ((1ull << 24) | ((unsigned long long)len << 34)) : 0ull);
+  unsigned long long tot;
+  const unsigned long long ex = block_excl_scan64(v, b.wsum, &tot);
+  (void)wsum;
   BatchWork w;
-  const int pex = block_excl_scan(is_long ? (len + kPieceLen - 1) / kPieceLen : 0, wsum, &w.pieces);
-  // count of short slices (high bits) and their entries (low 17 bits: under 512 * 256)
-  int packed;
-  const int ex = block_excl_scan(is_short ? (len | (1 << 17)) : 0, wsum, &packed);
+  w.pieces = (int)(tot & 0xffffffull);
+  w.nshort = (int)((tot >> 24) & 0x3ffull);
+  w.short_total = (int)(tot >> 34);
   b.s[t] = s;
   b.len[t] = len;
-  b.pexcl[t] = pex;
+  b.pexcl[t] = (int)(ex & 0xffffffull);
   b.a[t] = av;
   if (is_short) {
-    b.E[ex >> 17] = ex & 0x1ffff;
-    b.slot[ex >> 17] = (int16_t)t;
+    const int c = (int)((ex >> 24) & 0x3ffull);
+    b.E[c] = (int)(ex >> 34);
+    b.slot[c] = (int16_t)t;
   }
-  w.nshort = packed >> 17;
-  w.short_total = packed & 0x1ffff;
   if (t == 0) {
     b.pexcl[kThreads] = w.pieces;
     b.E[w.nshort] = w.short_total;
@@ -520,9 +551,15 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
       int nnz_w;
       int run = block_excl_scan(lane == 0 ? wc : 0, wsum, &nnz_w);  // prefix of warp totals
       run = __shfl_sync(0xffffffffu, run, 0);
+      if (out + nnz_w > row_end) {  // never write past the row the symbolic pass sized (uniform)
+        if (threadIdx.x == 0) atomicExch(a.err, 1);
+        break;
+      }
+      // The same walk stores each word's prefix and writes its columns, in
+      // order, at their ranks.
       for (int wb = c0; wb < c1; wb += 32) {
         const int w = wb + lane;
-        const uint32_t word = w < c1 ? bm[w] : 0u;
+        uint32_t word = w < c1 ? bm[w] : 0u;
         const int pc = __popc(word);
         int incl = pc;
 #pragma unroll
@@ -530,37 +567,26 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
           const int y = __shfl_up_sync(0xffffffffu, incl, o);
           if (lane >= o) incl += y;
         }
-        const int pre = run + incl - pc;
+        int r = run + incl - pc;
         if (w < c1) {
-          if ((w & (kGroupWords - 1)) == 0) gbase[w / kGroupWords] = (uint32_t)pre;
-          wpre[w] = (uint16_t)pre;
+          if ((w & (kGroupWords - 1)) == 0) gbase[w / kGroupWords] = (uint32_t)r;
+          wpre[w] = (uint16_t)r;
+        }
+        const int32_t col0 = wlo + w * 32 - shift;
+        while (word) {
+          const int bit = __ffs(word) - 1;
+          word &= word - 1;
+          a.Ck[out + r] = col0 + bit;
+          r++;
         }
         run += __shfl_sync(0xffffffffu, incl, 31);
       }
       __syncthreads();
-      if (out + nnz_w > row_end) {  // never write past the row the symbolic pass sized
-        if (threadIdx.x == 0) atomicExch(a.err, 1);
-        break;
-      }
       // prefix of word w: the group's 32-bit base plus the 16-bit difference
       auto word_prefix = [&](int w) -> int {
         const uint32_t base = gbase[w / kGroupWords];
         return (int)base + (int)(uint16_t)(wpre[w] - (uint16_t)base);
       };
-      // columns, in order: word-interleaved per warp as above
-      for (int wb = c0; wb < c1; wb += 32) {
-        const int w = wb + lane;
-        if (w < c1) {
-          uint32_t word = bm[w];
-          int r = word_prefix(w);
-          while (word) {
-            const int bit = __ffs(word) - 1;
-            word &= word - 1;
-            a.Ck[out + r] = wlo + w * 32 + bit - shift;
-            r++;
-          }
-        }
-      }
       // column of output rank `target` (< nnz_w) in this span
       auto col_of_rank = [&](int target) -> int32_t {
         int lo = 0, hi = nw - 1;  // last word whose prefix <= target
