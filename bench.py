@@ -207,26 +207,49 @@ def cpu_baseline(A, target_products, threads):
 
 
 # ------------------------------------------------------------------ dist
-def dist_init():
+def dist_init(backend=None):
+    """Rank set-up under torchrun (RANK/LOCAL_RANK/WORLD_SIZE/MASTER_* from the
+    environment). NCCL on GPUs; gloo where there is no GPU (the CPU tests)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group("gloo")
         return ws, rank, local, dist
     return 1, 0, local, None
 
 
-def reduce_max(dist, x):
+def _reduce(dist, x, op):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def reduce_max(dist, x):
+    """Max over ranks (the slowest rank's time)."""
+    return x if dist is None else _reduce(dist, x, dist.ReduceOp.MAX)
+
+
+def reduce_sum(dist, x):
+    return x if dist is None else _reduce(dist, x, dist.ReduceOp.SUM)
+
+
+def job_rate(dist, units, secs):
+    """Whole-job throughput: the units every rank processed over the slowest
+    rank's time."""
+    return reduce_sum(dist, units) / reduce_max(dist, secs)
 
 
 def barrier(dist):
@@ -301,8 +324,7 @@ def bench_spws(args, ws, rank, local, dist):
     wall = sum(walls) / len(walls)
     wall_max = reduce_max(dist, wall)
     products = stats[0].products
-    flops_job = 2.0 * products * ws
-    value = flops_job / wall_max / 1e9
+    value = job_rate(dist, 2.0 * products, wall) / 1e9
 
     ms_num = sum(s.ms_numeric for s in stats) / len(stats)
     ms_sym = sum(s.ms_symbolic for s in stats) / len(stats)
@@ -340,7 +362,7 @@ def bench_spws(args, ws, rank, local, dist):
     for arr in pinned:
         L.spws_host_unpin(arr.ctypes.data)
     e2e_wall = reduce_max(dist, sum(e2e_walls) / len(e2e_walls)) if e2e_walls else float("nan")
-    e2e_value = flops_job / e2e_wall / 1e9 if e2e_walls else None
+    e2e_value = job_rate(dist, 2.0 * products, e2e_wall) / 1e9 if e2e_walls else None
 
     if rank != 0:
         return
