@@ -146,7 +146,9 @@ __global__ void k_bitmap_words(int32_t nA, const RowInfo* __restrict__ info, int
   if (i >= nA) return;
   const RowInfo r = info[i];
   const long long span = (long long)r.hi - r.lo + 1;
-  words[i] = (cost_bucket(r.products) > light_bucket && span <= kSpanBits) ? (int32_t)((span + 31) >> 5) : 0;
+  // padded to 4 words, so every row's stored bitmap starts on a 16-byte boundary
+  words[i] = (cost_bucket(r.products) > light_bucket && span <= kSpanBits) ? (int32_t)((((span + 31) >> 5) + 3) & ~3)
+                                                                            : 0;
 }
 
 struct PassArgs {
@@ -481,15 +483,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_symbolic(PassArgs a) {
     int total = 0;
     for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
       const int nw = words_in(wl, ri.hi);
-      for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = 0;
+      const int nq = (nw + 3) >> 2;  // 16-byte groups of words (the stored bitmaps are padded to them)
+      uint4* bm4 = reinterpret_cast<uint4*>(bm);
+      for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = make_uint4(0u, 0u, 0u, 0u);
       __syncthreads();
       build_bitmap(a, q0, q1, (int32_t)wl, multi, bm, b, wsum);
-      if (a.bmstore && !multi) {
-        uint32_t* dst = a.bmstore + a.bmoff[i];
-        for (int w = threadIdx.x; w < nw; w += kThreads) dst[w] = bm[w];
-      }
+      uint4* dst = (a.bmstore && !multi) ? reinterpret_cast<uint4*>(a.bmstore + a.bmoff[i]) : nullptr;
       int c = 0;
-      for (int w = threadIdx.x; w < nw; w += kThreads) c += __popc(bm[w]);
+      for (int w = threadIdx.x; w < nq; w += kThreads) {
+        const uint4 v = bm4[w];
+        if (dst) dst[w] = v;
+        c += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+      }
       int t;
       block_excl_scan(c, wsum, &t);
       total += t;
@@ -528,12 +533,15 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
     for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
       const int32_t wlo = (int32_t)wl;
       const int nw = words_in(wl, ri.hi);
+      const int nq = (nw + 3) >> 2;
+      uint4* bm4 = reinterpret_cast<uint4*>(bm);
       if (a.bmstore && !multi) {  // the symbolic pass left this row's bitmap
-        const uint32_t* src = a.bmstore + a.bmoff[i];
-        for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = src[w];
+        const uint4* src = reinterpret_cast<const uint4*>(a.bmstore + a.bmoff[i]);
+#pragma unroll 4
+        for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = src[w];
         __syncthreads();
       } else {
-        for (int w = threadIdx.x; w < nw; w += kThreads) bm[w] = 0;
+        for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = make_uint4(0u, 0u, 0u, 0u);
         __syncthreads();
         build_bitmap(a, q0, q1, wlo, multi, bm, b, wsum);
       }
