@@ -383,3 +383,87 @@ class BatchPlan:
             self.release()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------ file loaders
+def _loaders():
+    L = lib()
+    if not getattr(L, "_spws_loaders", False):
+        I32P, DP = C.POINTER(C.c_int32), C.POINTER(C.c_double)
+        L.spws_read_mtx_csr.argtypes = [C.c_char_p, C.c_int32, C.c_int32, I32P, I32P, C.POINTER(C.c_int64),
+                                        C.POINTER(I32P), C.POINTER(I32P), C.POINTER(DP)]
+        L.spws_read_mtx_csc.argtypes = [C.c_char_p, I32P, I32P, C.POINTER(C.c_int64), C.POINTER(I32P),
+                                        C.POINTER(I32P), C.POINTER(DP)]
+        L.spws_read_tns_coo3.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(I32P),
+                                         C.POINTER(I32P), C.POINTER(I32P), C.POINTER(DP)]
+        L.spws_read_tns_csf.argtypes = [C.c_char_p, I32P, C.POINTER(taco.TacoTensor)]
+        L.spws_csf_release.argtypes = [C.POINTER(taco.TacoTensor)]
+        for f in (L.spws_read_mtx_csr, L.spws_read_mtx_csc, L.spws_read_tns_coo3, L.spws_read_tns_csf,
+                  L.spws_csf_release):
+            f.restype = C.c_int
+        L._spws_loaders = True
+    return L
+
+
+def _take(ptr, n, dtype):
+    """Copy n elements of a malloc'd array into numpy and free it."""
+    out = np.ctypeslib.as_array(ptr, shape=(max(n, 1),))[:n].astype(dtype, copy=True) if n else np.zeros(0, dtype)
+    lib().spws_free(C.cast(ptr, C.c_void_p))
+    return out
+
+
+def read_mtx(path, keep_values=False, one_based=True):
+    """Matrix Market file -> CSR (pos, crd, vals, nrow, ncol), read_mtx_csr /
+    read_mtx_csr_keep_value semantics (include/spws/spws_loaders.h)."""
+    L = _loaders()
+    nr, nc, nz = C.c_int32(), C.c_int32(), C.c_int64()
+    p, c = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    v = C.POINTER(C.c_double)()
+    check(L.spws_read_mtx_csr(os.fsencode(path), int(keep_values), int(one_based), C.byref(nr), C.byref(nc),
+                              C.byref(nz), C.byref(p), C.byref(c), C.byref(v)))
+    return (_take(p, nr.value + 1, np.int32), _take(c, nz.value, np.int32), _take(v, nz.value, np.float64),
+            nr.value, nc.value)
+
+
+def read_mtx_csc(path):
+    """Matrix Market file -> (pos, crd, vals, nrow, ncol) with read_mtx_csc's
+    grouping (over the first coordinate, ncol outer positions)."""
+    L = _loaders()
+    nr, nc, nz = C.c_int32(), C.c_int32(), C.c_int64()
+    p, c = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    v = C.POINTER(C.c_double)()
+    check(L.spws_read_mtx_csc(os.fsencode(path), C.byref(nr), C.byref(nc), C.byref(nz), C.byref(p), C.byref(c),
+                              C.byref(v)))
+    return (_take(p, nc.value + 1, np.int32), _take(c, nz.value, np.int32), _take(v, nz.value, np.float64),
+            nr.value, nc.value)
+
+
+def read_tns(path, one_based=True):
+    """.tns file -> sorted COO (c0, c1, c2, vals), read_txt_coo3 semantics."""
+    L = _loaders()
+    nz = C.c_int64()
+    a, b, c = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    v = C.POINTER(C.c_double)()
+    check(L.spws_read_tns_coo3(os.fsencode(path), int(one_based), C.byref(nz), C.byref(a), C.byref(b), C.byref(c),
+                               C.byref(v)))
+    n = nz.value
+    return _take(a, n, np.int32), _take(b, n, np.int32), _take(c, n, np.int32), _take(v, n, np.float64)
+
+
+def read_tns_csf(path, dims):
+    """.tns file -> order-3 CSF levels (roots, pos1, crd1, pos2, crd2, vals),
+    read_tns_csf's layout in file mode order."""
+    L = _loaders()
+    t = taco.TacoTensor()
+    d = (C.c_int32 * 3)(*dims)
+    check(L.spws_read_tns_csf(os.fsencode(path), d, C.byref(t)))
+    try:
+        nr = t.indices[0][0][1]
+        nf = t.indices[1][0][nr]
+        nz = t.indices[2][0][nf]
+        arr = lambda p, n: np.ctypeslib.as_array(p, shape=(max(n, 1),))[:n].copy()
+        return (arr(t.indices[0][1], nr), arr(t.indices[1][0], nr + 1), arr(t.indices[1][1], nf),
+                arr(t.indices[2][0], nf + 1), arr(t.indices[2][1], nz), arr(t.vals, nz))
+    finally:
+        L.spws_csf_release(C.byref(t))
+
