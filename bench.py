@@ -505,6 +505,84 @@ def bench_batched(args):
     print(json.dumps(line), flush=True)
 
 
+TENSOR = dict(dims=(50000, 40000, 20000), nnz=20_000_000, zipf_s=1.1, seed=42)
+
+
+def bench_tensor(args):
+    """The tensor config: a 50,000 x 40,000 x 20,000 COO tensor with 20M
+    nonzeros (mode-1 slices Zipf s=1.1, other modes uniform, values U(0,1]),
+    seeded synthetic. mttkrp: A(i,j) = sum B(k,l,i) C(k,j) D(l,j) on mode 1
+    with dense rank-R factors (CSF order mode2, mode3, mode1);
+    ttm: A(k,j,l) = sum_i B(k,i,j) C(i,l) on mode 3 with a dense 20,000 x R
+    matrix (CSF order mode1, mode3, mode2). One step = one device-resident
+    call (sort, bucket sums, output assembly), L2 flushed between steps."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import build, gen, served, taco
+    build.build()
+    L = sp.lib()
+    sp.check(L.spws_set_device(0))
+    t0 = time.perf_counter()
+    d0, d1, d2 = TENSOR["dims"]
+    i0, i1, i2, tv = gen.tensor3(TENSOR["dims"], TENSOR["nnz"], zipf_s=TENSOR["zipf_s"], seed=TENSOR["seed"])
+    R = args.rank
+    if args.workload == "mttkrp":
+        coo, dims = (i1, i2, i0, tv), (d1, d2, d0)
+        facs = [gen.dense_factor(d1, R, seed=43), gen.dense_factor(d2, R, seed=44)]
+    else:
+        coo, dims = (i0, i2, i1, tv), (d0, d2, d1)
+        facs = [gen.dense_factor(d2, R, seed=45)]
+    gen_s = time.perf_counter() - t0
+    B = served.DeviceCsf3(coo, dims)
+    F = [served.DeviceFactor(f) for f in facs]
+    nnz = int(B.t.nnz)
+    nslices, nfibers = int(B.t.nroots), int(B.t.nfibers)
+
+    def step():
+        if args.workload == "mttkrp":
+            out, ms = served.mttkrp_device(B, F[0], F[1], keep=True)
+        else:
+            out, ms = served.ttm_device(B, F[0], keep=True)
+        n_out = int(out.nnz)
+        served.coo_release(out)
+        return ms, n_out
+
+    for _ in range(args.warmup):
+        step()
+    walls, mss = [], []
+    l0 = L.spws_launch_count()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+            t0 = time.perf_counter()
+            ms, n_out = step()
+            walls.append(time.perf_counter() - t0)
+            mss.append(ms)
+    launches = (L.spws_launch_count() - l0) // args.steps
+    wall = sum(walls) / len(walls)
+    ms_dev = sum(mss) / len(mss)
+    if args.workload == "mttkrp":
+        flops = 2.0 * R * nnz + R * nfibers
+        alg = 12 * nnz + 8 * (nslices + nfibers + 2) + 8 * R * (d1 + d2) + 12 * n_out
+    else:
+        flops = 2.0 * R * nnz
+        alg = 12 * nnz + 8 * (nslices + nfibers + 2) + 8 * R * d2 + 20 * n_out
+    bw, peak_src = measured_peaks()
+    achieved = alg / (ms_dev * 1e-3) / 1e9
+    line = {"metric": f"{args.workload}_gflops", "value": flops / wall / 1e9, "unit": "GFLOP/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zipf tensor)",
+            "config": {"workload": f"{args.workload}_tensor_config", "dims": list(TENSOR["dims"]), "nnz": nnz,
+                       "rank": R, "zipf_s": TENSOR["zipf_s"], "slices": nslices, "fibers": nfibers,
+                       "output_nnz": n_out, "l2": "flushed between timed steps (512 MiB write)"},
+            "device_ms_per_step": ms_dev,
+            "roofline": {"bound": "hbm", "kernel": "tensor_bucket (whole call: sort, bucket sums, output)",
+                         "achieved": achieved, "peak": bw, "unit": "GB/s",
+                         "frac": achieved / bw, "peak_source": peak_src,
+                         "algorithmic_bytes_per_launch": alg, "traffic": None},
+            "gpu_launches": launches, "clocks": clk.summary(), "generation_s": gen_s}
+    print(json.dumps(line), flush=True)
+
+
 SERVED_MIX = (0.90, 0.09, 0.01)  # small products, R-MAT 2^18 products, TTM requests
 
 
@@ -687,7 +765,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spws", choices=["spws", "reference"])
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched", "served"])
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched", "served", "mttkrp", "ttm"])
     ap.add_argument("--instances", type=int, default=1024,
                     help="batched workload: number of products (4096 holds ~220 GB of output at once)")
     ap.add_argument("--plain-sample", type=int, default=512, help="batched workload: one-at-a-time ABI sample")
@@ -697,6 +775,7 @@ def main():
     ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
                     help="products per step of the reference arm (all cores)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rank", type=int, default=32, help="mttkrp/ttm workloads: factor rank R")
     ap.add_argument("--served-requests", type=int, default=400, help="served workload: requests per run")
     ap.add_argument("--served-pool", type=int, default=512, help="served workload: distinct small products")
     ap.add_argument("--served-workers", type=int, default=8)
@@ -711,6 +790,9 @@ def main():
     elif args.workload == "served":
         if rank == 0 and args.impl != "reference":
             bench_served(args)
+    elif args.workload in ("mttkrp", "ttm"):
+        if rank == 0 and args.impl != "reference":
+            bench_tensor(args)
     elif args.impl == "reference":
         bench_reference(args, ws, rank, dist)
     else:

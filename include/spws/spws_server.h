@@ -92,9 +92,15 @@ int spws_factor_release(spws_factor_dev* f);
  * COO_CSF_DCSR_hash_il.h:247 `compute`; A is a sorted order-3 COO allocated by
  * the library. `ms` (may be NULL) receives the device time. */
 int spws_ttm_device(const spws_csf3_dev* B, const spws_factor_dev* F, spws_coo_dev* A, float* ms);
+/* MTTKRP A(i,j) = sum_{k,l} B(k,l,i) C(k,j) D(l,j) on device operands, the
+ * computation of COO_CSF_DCSR_DCSR_hash_free.h:233 `compute`; A is a sorted
+ * order-2 COO allocated by the library (release with spws_coo_release). */
+int spws_mttkrp_device(const spws_csf3_dev* B, const spws_factor_dev* C, const spws_factor_dev* D, spws_coo_dev* A,
+                       float* ms);
 /* Copy a device COO into caller host arrays (crd[d] for d < order, vals). */
 int spws_coo_download(const spws_coo_dev* A, int32_t* crd0, int32_t* crd1, int32_t* crd2, double* vals);
-/* Release a COO allocated by spws_ttm_device (not a server result). */
+/* Release a COO allocated by spws_ttm_device / spws_mttkrp_device (not a
+ * server result). */
 int spws_coo_release(spws_coo_dev* A);
 
 typedef struct spws_server spws_server;

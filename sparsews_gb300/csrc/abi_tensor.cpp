@@ -450,6 +450,44 @@ int spws_ttm_device(const spws_csf3_dev* B, const spws_factor_dev* F, spws_coo_d
   return rc;
 }
 
+int spws_mttkrp_device(const spws_csf3_dev* B, const spws_factor_dev* C, const spws_factor_dev* D, spws_coo_dev* A,
+                       float* ms) {
+  clear_error();
+  if (!A) {
+    set_error("A is NULL");
+    return SPWS_ERR_INVALID;
+  }
+  *A = spws_coo_dev{};
+  SPWS_TRY(check_csf3(B));
+  SPWS_TRY(check_factor(C));
+  SPWS_TRY(check_factor(D));
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  const cudaStream_t s = ds->stream;
+  cudaEvent_t e0, e1;
+  SPWS_CUDA(cudaEventCreate(&e0));
+  SPWS_CUDA(cudaEventCreate(&e1));
+  cudaEventRecord(e0, s);
+  CooOut o;
+  const FactorDense fc = factor_view(*C), fd = factor_view(*D);
+  int rc = tensor_bucket(0, csf3_view(*B), fc, &fd, &o, s);
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  if (ms) cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != SPWS_OK) {
+    for (auto& c : o.crd) dfree(c, s);
+    dfree(o.vals, s);
+    return rc;
+  }
+  A->order = 2;
+  A->nnz = o.n;
+  for (int d = 0; d < 3; d++) A->crd[d] = o.crd[d];
+  A->vals = o.vals;
+  return SPWS_OK;
+}
+
 int spws_coo_download(const spws_coo_dev* A, int32_t* crd0, int32_t* crd1, int32_t* crd2, double* vals) {
   clear_error();
   if (!A || A->order < 1 || A->order > 3 || A->nnz < 0) {

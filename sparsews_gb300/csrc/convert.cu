@@ -28,27 +28,23 @@ int bits_for(unsigned long long max_key_exclusive) {
 __global__ void k_validate_cc(int32_t nq, int32_t outer_dim, int32_t inner_dim, int64_t nnz,
                               const int32_t* __restrict__ oc, const int32_t* __restrict__ pos,
                               const int32_t* __restrict__ ic, int* __restrict__ bad) {
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // warp per outer entry, so a long fiber list (a heavy Zipf slice) is
+  // checked by 32 lanes instead of one thread
+  const int lane = threadIdx.x & 31;
+  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= nq) return;
   const int32_t o = oc[q];
-  if (o < 0 || o >= outer_dim || (q > 0 && oc[q - 1] >= o)) {
-    atomicExch(bad, 1);
-    return;
-  }
   const int32_t s = pos[q], e = pos[q + 1];
-  if (s < 0 || e < s || (int64_t)e > nnz) {
-    atomicExch(bad, 1);
+  if (o < 0 || o >= outer_dim || (q > 0 && oc[q - 1] >= o) || s < 0 || e < s || (int64_t)e > nnz) {
+    if (lane == 0) atomicExch(bad, 1);
     return;
   }
-  int prev = -1;
-  for (int32_t p = s; p < e; p++) {
+  bool ok = true;
+  for (int32_t p = s + lane; p < e; p += 32) {
     const int k = ic[p];
-    if (k <= prev || k >= inner_dim) {
-      atomicExch(bad, 1);
-      return;
-    }
-    prev = k;
+    ok &= k >= 0 && k < inner_dim && (p == s || ic[p - 1] < k);
   }
+  if (!__all_sync(0xffffffffu, ok) && lane == 0) atomicExch(bad, 1);
 }
 
 // keys[p] = row(p) * ncols + col(p) for a compressed-outer matrix whose outer
@@ -139,7 +135,7 @@ int validate_cc_device(const int32_t* oc, const int32_t* pos, const int32_t* ic,
   SPWS_TRY(dalloc((void**)&bad, sizeof(int), s));
   SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (nq > 0) {
-    k_validate_cc<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(nq, outer_dim, inner_dim, nnz, oc, pos, ic, bad);
+    k_validate_cc<<<(unsigned)((nq + 7) / 8), 256, 0, s>>>(nq, outer_dim, inner_dim, nnz, oc, pos, ic, bad);
     count_launch(1);
     SPWS_CUDA(cudaGetLastError());
   }

@@ -70,6 +70,8 @@ def _lib():
         "spws_factor_release": ([C.POINTER(FactorDev)], C.c_int),
         "spws_ttm_device": ([C.POINTER(Csf3Dev), C.POINTER(FactorDev), C.POINTER(CooDev), C.POINTER(C.c_float)],
                             C.c_int),
+        "spws_mttkrp_device": ([C.POINTER(Csf3Dev), C.POINTER(FactorDev), C.POINTER(FactorDev), C.POINTER(CooDev),
+                                C.POINTER(C.c_float)], C.c_int),
         "spws_coo_download": ([C.POINTER(CooDev), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "spws_coo_release": ([C.POINTER(CooDev)], C.c_int),
         "spws_server_create": ([C.POINTER(ServerConfig), C.POINTER(C.c_void_p)], C.c_int),
@@ -142,17 +144,39 @@ class DeviceFactor:
             pass
 
 
-def ttm_device(B, F):
+def ttm_device(B, F, keep=False):
     """TTM on device operands (one call, the plain path). Returns
-    (([k, j, l], vals), ms); the device COO is released after the copy."""
+    (([k, j, l], vals), ms) with the device COO released after the copy, or
+    with keep=True (CooDev, ms) left on the device (release with coo_release)."""
     L = _lib()
     out = CooDev()
     ms = C.c_float()
     check(L.spws_ttm_device(C.byref(B.t), C.byref(F.f), C.byref(out), C.byref(ms)))
+    if keep:
+        return out, ms.value
     try:
         return _download_coo(out), ms.value
     finally:
         L.spws_coo_release(C.byref(out))
+
+
+def mttkrp_device(B, Cf, Df, keep=False):
+    """MTTKRP on device operands. Returns (([i, j], vals), ms), or with
+    keep=True (CooDev, ms) left on the device (release with coo_release)."""
+    L = _lib()
+    out = CooDev()
+    ms = C.c_float()
+    check(L.spws_mttkrp_device(C.byref(B.t), C.byref(Cf.f), C.byref(Df.f), C.byref(out), C.byref(ms)))
+    if keep:
+        return out, ms.value
+    try:
+        return _download_coo(out), ms.value
+    finally:
+        L.spws_coo_release(C.byref(out))
+
+
+def coo_release(out):
+    _lib().spws_coo_release(C.byref(out))
 
 
 class Server:

@@ -117,3 +117,22 @@ def test_tensor_empty_and_invalid(spws_lib):
     bad[2][0] = 25  # leaf coordinate beyond its dimension
     with pytest.raises(sp.SpwsError):
         sp.mttkrp(bad, (10, 8, 20), gen.dense_factor(10, 4), gen.dense_factor(8, 4))
+
+
+def test_device_resident_mttkrp_and_ttm_match_taco_entry_points(spws_lib):
+    """spws_mttkrp_device / spws_ttm_device (device operands) give the same
+    COO as the TACO entry points on the same tensor, bit for bit (same kernel)."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import served
+    i0, i1, i2, tv = gen.tensor3((600, 300, 200), 30000, zipf_s=1.1, seed=81)
+    Cf, Df = gen.dense_factor(300, 32, seed=82), gen.dense_factor(200, 32, seed=83)
+    Bc, dims = (i1, i2, i0, tv), (300, 200, 600)
+    (ri, rj), rv = sp.mttkrp(Bc, dims, Cf, Df)
+    B = served.DeviceCsf3(Bc, dims)
+    ((gi, gj), gv), ms = served.mttkrp_device(B, served.DeviceFactor(Cf), served.DeviceFactor(Df))
+    assert ms > 0 and np.array_equal(gi, ri) and np.array_equal(gj, rj) and np.array_equal(gv, rv)
+    Bt, dt = (i0, i2, i1, tv), (600, 200, 300)
+    Ft = gen.dense_factor(200, 16, seed=84)
+    (rk, rj2, rl), rv2 = sp.ttm(Bt, dt, Ft)
+    ((gk, gj2, gl), gv2), _ = served.ttm_device(served.DeviceCsf3(Bt, dt), served.DeviceFactor(Ft))
+    assert np.array_equal(gk, rk) and np.array_equal(gl, rl) and np.array_equal(gv2, rv2)
