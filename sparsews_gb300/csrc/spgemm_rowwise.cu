@@ -547,13 +547,17 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
       }
 
       // Per-word prefix of set bits and the row's columns in order. Warp w
-      // owns a contiguous chunk of words and walks it 32 words at a time, one
-      // word per lane, so its C.crd stores are contiguous across the warp.
+      // owns a contiguous chunk of 16-byte groups of words and walks it 32
+      // groups at a time, one group (four words) per lane: one warp scan per
+      // 128 words, and the lanes' C.crd stores are contiguous across the warp.
       const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      const int chunk = (nw + kWarps - 1) / kWarps;
-      const int c0 = min(nw, warp * chunk), c1 = min(nw, c0 + chunk);
+      const int chunk = (nq + kWarps - 1) / kWarps;
+      const int c0 = min(nq, warp * chunk), c1 = min(nq, c0 + chunk);
       int wc = 0;
-      for (int w = c0 + lane; w < c1; w += 32) wc += __popc(bm[w]);
+      for (int g = c0 + lane; g < c1; g += 32) {
+        const uint4 v = bm4[g];
+        wc += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, o);
       int nnz_w;
@@ -564,28 +568,37 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
         break;
       }
       // The same walk stores each word's prefix and writes its columns, in
-      // order, at their ranks.
-      for (int wb = c0; wb < c1; wb += 32) {
-        const int w = wb + lane;
-        uint32_t word = w < c1 ? bm[w] : 0u;
-        const int pc = __popc(word);
-        int incl = pc;
+      // order, at their ranks. Words past nw inside the last group are zero.
+      for (int gb = c0; gb < c1; gb += 32) {
+        const int g = gb + lane;
+        const uint4 v = g < c1 ? bm4[g] : make_uint4(0u, 0u, 0u, 0u);
+        const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+        const int tot = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+        int incl = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const int y = __shfl_up_sync(0xffffffffu, incl, o);
           if (lane >= o) incl += y;
         }
-        int r = run + incl - pc;
-        if (w < c1) {
-          if ((w & (kGroupWords - 1)) == 0) gbase[w / kGroupWords] = (uint32_t)r;
-          wpre[w] = (uint16_t)r;
+        int r = run + incl - tot;
+        if (g < c1) {
+          if (((4 * g) & (kGroupWords - 1)) == 0) gbase[(4 * g) / kGroupWords] = (uint32_t)r;
+          const int p1 = r + __popc(v.x), p2 = p1 + __popc(v.y), p3 = p2 + __popc(v.z);
+          // the four 16-bit prefixes in one 8-byte store (4g is a multiple of 4)
+          *reinterpret_cast<uint2*>(wpre + 4 * g) =
+              make_uint2((uint32_t)(uint16_t)r | ((uint32_t)(uint16_t)p1 << 16),
+                         (uint32_t)(uint16_t)p2 | ((uint32_t)(uint16_t)p3 << 16));
         }
-        const int32_t col0 = wlo + w * 32 - shift;
-        while (word) {
-          const int bit = __ffs(word) - 1;
-          word &= word - 1;
-          a.Ck[out + r] = col0 + bit;
-          r++;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          uint32_t word = words[k];
+          const int32_t col0 = wlo + (4 * g + k) * 32 - shift;
+          while (word) {
+            const int bit = __ffs(word) - 1;
+            word &= word - 1;
+            a.Ck[out + r] = col0 + bit;
+            r++;
+          }
         }
         run += __shfl_sync(0xffffffffu, incl, 31);
       }
