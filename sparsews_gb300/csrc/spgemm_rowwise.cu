@@ -653,6 +653,15 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
         }
         __syncthreads();
       }
+      // Other rows with several windows keep, per j, where the previous
+      // window's slice of B row j ended (in the bound table's space): the next
+      // slice starts there, and only its end needs a search (none for the last
+      // window, which runs to the end of the row).
+      const bool cursors = !prebound && !multi && nwin > 1 && nj <= kBoundInts;
+      if (cursors) {
+        for (int t = threadIdx.x; t < nj; t += kThreads) bnd[t] = __ldg(a.Bp + __ldg(a.Aj + q0 + t));
+        __syncthreads();
+      }
       // values, one window of ACC ranks at a time
       for (int r0 = 0, win = 0; r0 < nnz_w; r0 += ACC, win++) {
         const int r1 = min(nnz_w, r0 + ACC);
@@ -678,6 +687,26 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
               s0 = bnd[t * (nwin + 1) + win];
               len = bnd[t * (nwin + 1) + win + 1] - s0;
               av = __ldg(a.Av + q0 + t);
+            }
+            bw = fill_batch(s0, len, av, a.long_min, b, wsum);
+          } else if (cursors) {
+            const int32_t q = qb + threadIdx.x;
+            int32_t s0 = 0, len = 0;
+            double av = 0.0;
+            if (q < q1) {
+              s0 = bnd[q - q0];
+              int32_t lo = s0, hi = __ldg(a.Bp + __ldg(a.Aj + q) + 1);  // first position with column >= chi
+              if (chi != INT_MAX) {
+                while (lo < hi) {
+                  const int32_t m = (lo + hi) >> 1;
+                  if (__ldg(a.Bk + m) < chi) lo = m + 1; else hi = m;
+                }
+              } else {
+                lo = hi;
+              }
+              bnd[q - q0] = lo;
+              len = lo - s0;
+              av = __ldg(a.Av + q);
             }
             bw = fill_batch(s0, len, av, a.long_min, b, wsum);
           } else {
