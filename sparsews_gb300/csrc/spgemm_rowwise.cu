@@ -44,6 +44,7 @@ constexpr int kGroupWords = 2048;             // words per 32-bit prefix base (6
 constexpr int kGroups = kSpanWords / kGroupWords;
 constexpr int kAcc = 5120;                    // ranks per numeric window (40 KB of FP64), 2 CTAs per SM
 constexpr int kAccWide = 18432;               // the wide-window variant (144 KB), 1 CTA per SM
+static_assert(kAcc < 65536 && kAccWide < 65536, "window offsets are computed modulo 2^16");
 constexpr int kBoundInts = 2048;              // shared table of per-(j, window) slice bounds
 constexpr int kMaxWin = 64;                   // windows per span with precomputed bounds
 constexpr int kBuckets = 66;                  // cost buckets: 0 = no products, b = 1 + floor(log2(P))
@@ -712,11 +713,15 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
           } else {
             bw = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
           }
+          // The window offset rank - r0 lies in [0, ACC), below 2^16, so it
+          // follows from the 16-bit word prefixes alone, modulo 2^16 (no
+          // group base needed).
+          const uint16_t r0_16 = (uint16_t)r0;
           for_batch_entries<true>(b, bw, a.Bk, a.Bv, [&](int32_t col, double bv, double av) {
             const int k = col - wlo;
             const int w = k >> 5;
-            const int rank = word_prefix(w) + __popc(bm[w] & ((1u << (k & 31)) - 1u));
-            atomicAdd(&acc[rank - r0], __dmul_rn(av, bv));
+            const uint16_t off = (uint16_t)(wpre[w] + __popc(bm[w] & ((1u << (k & 31)) - 1u)) - r0_16);
+            atomicAdd(&acc[off], __dmul_rn(av, bv));
           });
           __syncthreads();
         }
