@@ -76,6 +76,30 @@ def test_wide_columns_many_chunks(spws_lib):
     assert_csr_close(got, ref, scale_of(A, B), "wide")
 
 
+def test_rows_spanning_several_bitmap_spans(spws_lib):
+    """Heavy rows whose columns spread over 1,000,000 columns (several 2^18-column
+    bitmap spans) and whose outputs need several rank windows per span."""
+    import sparsews_gb300 as sp
+    n, m = 300, 1_000_000
+
+    def rand_csr(nrow, ncol, per_row, seed):
+        r = np.random.default_rng(seed)
+        rows = np.repeat(np.arange(nrow), per_row)
+        cols = r.integers(0, ncol, len(rows))
+        key = np.unique(rows.astype(np.int64) * ncol + cols)
+        rr, cc = key // ncol, (key % ncol).astype(np.int32)
+        pos = np.zeros(nrow + 1, np.int64)
+        np.add.at(pos, rr + 1, 1)
+        return np.cumsum(pos).astype(np.int32), cc, r.uniform(-1, 1, len(cc)), nrow, ncol
+
+    A = rand_csr(n, n, 40, 48)
+    B = rand_csr(n, m, 2000, 49)
+    got = sp.spgemm(A, B)
+    ref = oracle.spgemm("taco", A, B)
+    assert np.diff(ref[0]).max() > 3 * 5120  # several windows per span
+    assert_csr_close(got, ref, scale_of(A, B), "multi-span")
+
+
 def test_empty_operands(spws_lib):
     import sparsews_gb300 as sp
     Z = (np.zeros(6, np.int32), np.zeros(0, np.int32), np.zeros(0), 5, 7)
