@@ -148,6 +148,16 @@ int spws_dcsc_dcsr_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor
  * reported through spws_last_error() since the reference returns void. */
 void DCSC_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print);
 
+/* Replaces `int compute(C, A, B)` of benchmark/DCSC_DCSR/DCSC_DCSR_taco.h:4, the
+ * TACO outer product with a dense A1 x B2 workspace: each output entry is the
+ * j-ascending sum, which the coordinate engine reproduces bit for bit. */
+int spws_dcsc_dcsr_taco_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
+
+/* Replaces `double DCSC_DCSR_taco(A, B, C, warmup, repeat, bench=false,
+ * print=false)` of benchmark/DCSC_DCSR/DCSC_DCSR_taco.h:136. */
+double DCSC_DCSR_taco(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t warmup, int32_t repeat, bool bench,
+                      bool print);
+
 /* ------------------------------------------------------------------------ */
 /* Transposed-output SpGEMM C = (A*B)^T: A in CSC (dense outer level over j),  */
 /* B in CSR, C in CSR over k. evaluate/CSC_CSR_T_hash_record.h                 */

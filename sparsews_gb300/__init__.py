@@ -78,6 +78,8 @@ def lib():
         "spws_dcsc_dcsr_hash_compute": ([P, P, P, C.c_int32], C.c_int),
         "spws_dcsc_dcsr_bucket_compute": ([P, P, P, C.c_int32], C.c_int),
         "spws_dcsc_dcsr_coord_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_dcsc_dcsr_taco_compute": ([P, P, P], C.c_int),
+        "DCSC_DCSR_taco": ([P, P, P, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
         "spws_csc_csr_t_hash_compute": ([P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
         "DCSC_DCSR_hash": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
         "DCSC_DCSR_bucket": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
@@ -166,7 +168,7 @@ def _csr_transpose_np(pos, crd, vals, nrow, ncol):
 
 def spgemm_outer(A, B, method="hash"):
     """Outer-product C = A*B with A passed as DCSC and B as DCSR (the reference's
-    DCSC_DCSR_* entry points). method: 'hash', 'bucket' or 'coord'."""
+    DCSC_DCSR_* entry points). method: 'hash', 'bucket', 'coord' or 'taco'."""
     L = lib()
     ap, ac, av, an, am = A
     bp, bc, bv, bn, bm = B
@@ -174,9 +176,12 @@ def spgemm_outer(A, B, method="hash"):
     At = taco.dcsc(tp, tc, tv, an, am)
     Bt = taco.dcsr(bp, bc, bv, bn, bm)
     Ct = taco.init_dc(an, bm)
-    fn = {"hash": L.spws_dcsc_dcsr_hash_compute, "bucket": L.spws_dcsc_dcsr_bucket_compute,
-          "coord": L.spws_dcsc_dcsr_coord_compute}[method]
-    check(fn(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
+    if method == "taco":
+        check(L.spws_dcsc_dcsr_taco_compute(Ct.ptr(), At.ptr(), Bt.ptr()))
+    else:
+        fn = {"hash": L.spws_dcsc_dcsr_hash_compute, "bucket": L.spws_dcsc_dcsr_bucket_compute,
+              "coord": L.spws_dcsc_dcsr_coord_compute}[method]
+        check(fn(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
     return taco.take_csr(Ct, an, L.spws_free)
 
 

@@ -164,6 +164,17 @@ void DCSC_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32
   spws_dcsc_dcsr_coord_compute(C, A, B, w_cap);
 }
 
+int spws_dcsc_dcsr_taco_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  return dcsc_dcsr(C, A, B, Engine::Coord);
+}
+
+double DCSC_DCSR_taco(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t warmup, int32_t repeat, bool bench,
+                      bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_dcsc_dcsr_taco_compute(C, A, B); },
+               [&] { free_csr_out(C); });
+}
+
 int spws_csr_csr_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
   (void)w_cap;
   clear_error();

@@ -55,6 +55,9 @@ def test_coord_against_oracle(spws_lib, case):
     assert np.array_equal(got[2], ref[2])
     got_o = sp.spgemm_outer(A, A, "coord")
     assert np.array_equal(got_o[2], ref[2])
+    got_t = sp.spgemm_outer(A, A, "taco")  # DCSC_DCSR_taco.h's dense workspace sums in j order too
+    assert_csr_equal_structure(got_t, ref, case)
+    assert np.array_equal(got_t[2], ref[2])
 
 
 def test_outer_against_oracle_rmat(spws_lib):
