@@ -73,6 +73,9 @@ def _load(kind):
     f = getattr(lib, prefix + "csc_csr_t_hash")
     f.argtypes = [P] * 3 + [C.c_int32, C.POINTER(C.c_int32)]
     f.restype = C.c_int
+    f = getattr(lib, prefix + "csc_csr_t_hash_nofuse")
+    f.argtypes = [P] * 4 + [C.c_int32, C.POINTER(C.c_int32)]
+    f.restype = C.c_int
     for name in ("mttkrp_hash", "mttkrp_bucket"):
         f = getattr(lib, prefix + name)
         f.argtypes = [P] * 4 + [C.c_int32]
@@ -148,6 +151,29 @@ def spgemm_t(A, B, w_cap=None, kind="port"):
     if rc != 0:
         raise RuntimeError(f"oracle t_hash failed rc={rc}")
     return taco.take_csr(Cout, bm, fr), int(coll.value)
+
+
+def spgemm_t_nofuse(A, B, w_cap=None, kind="port"):
+    """The non-fused form (evaluate/CSC_CSR_T_hash_record_nofuse.h): C_noT =
+    A*B through the (i, k)-keyed hash, then C = C_noT^T by TACO's transpose.
+    Returns (CSR of C_noT, CSR of C, collision count)."""
+    lib, pre, fr = _load(kind)
+    ap, ac, av, an, am = A
+    bp, bc, bv, bn, bm = B
+    if w_cap is None:
+        w_cap = w_cap_default(len(ac))
+    from sparsews_gb300.gen import csr_transpose
+    tp, tc, tv = csr_transpose(ap, ac, av, an, am)
+    At = taco.csc(tp, tc, tv, an, am)
+    Bt = taco.csr(bp, bc, bv, bn, bm)
+    CnoT = taco.init_dc(an, bm)
+    Cout = taco.init_dc(bm, an)
+    coll = C.c_int32(0)
+    rc = getattr(lib, pre + "csc_csr_t_hash_nofuse")(CnoT.ptr(), Cout.ptr(), At.ptr(), Bt.ptr(), w_cap,
+                                                    C.byref(coll))
+    if rc != 0:
+        raise RuntimeError(f"oracle t_hash_nofuse failed rc={rc}")
+    return taco.take_csr(CnoT, an, fr), taco.take_csr(Cout, bm, fr), int(coll.value)
 
 
 def mttkrp(method, Bcsf, dims, Cf, Df, w_cap=None, kind="port"):

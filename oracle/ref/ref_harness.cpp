@@ -28,6 +28,9 @@ namespace ref_outer_bucket {
 namespace ref_t_hash {
 #include "evaluate/CSC_CSR_T_hash_record.h"
 }
+namespace ref_t_nofuse {
+#include "evaluate/CSC_CSR_T_hash_record_nofuse.h"
+}
 namespace ns_mttkrp_hash {
 #include "benchmark/MTTKRP/COO_CSF_DCSR_DCSR_hash_free.h"
 }
@@ -67,6 +70,16 @@ int ref_csc_csr_t_hash(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int
   ref_t_hash::collison_times = 0;
   int c = 0;
   ref_t_hash::CSC_CSR_T_hash(A, B, C, w_cap, c);
+  *collisions = c;
+  return 0;
+}
+/* evaluate/CSC_CSR_T_hash_record_nofuse.h:405 (compute_nofuse, then transpose);
+   the collision counter is cleared per call as above. */
+int ref_csc_csr_t_hash_nofuse(taco_tensor_t* C_noT, taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B,
+                              int32_t w_cap, int32_t* collisions) {
+  ref_t_nofuse::collison_times = 0;
+  int c = 0;
+  ref_t_nofuse::CSC_CSR_T_hash_nonfuse(A, B, C_noT, C, w_cap, c);
   *collisions = c;
   return 0;
 }

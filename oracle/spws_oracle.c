@@ -763,6 +763,68 @@ int ora_csc_csr_t_hash(taco_tensor_t* C, const taco_tensor_t* A, const taco_tens
 }
 
 /* ------------------------------------------------------------------------ */
+/* Non-fused form of the same product: C_noT = A*B with the key (i, k),     */
+/* then C = C_noT^T by TACO's counting-sort transpose.                      */
+/* evaluate/CSC_CSR_T_hash_record_nofuse.h:234-352 (compute_nofuse) and     */
+/* :354-403 (transpose). C_noT has A's row count, C has B's column count.   */
+/* ------------------------------------------------------------------------ */
+int ora_csc_csr_t_hash_nofuse(taco_tensor_t* C_noT, taco_tensor_t* C, const taco_tensor_t* A,
+                              const taco_tensor_t* B, int32_t w_cap, int32_t* collisions) {
+  const int32_t nj = B->dimensions[0];
+  const int32_t* Ap = A->indices[1][0];
+  const int32_t* Ai = A->indices[1][1];
+  const double* Av = A->vals;
+  const int32_t* Bp = B->indices[1][0];
+  const int32_t* Bk = B->indices[1][1];
+  const double* Bv = B->vals;
+  hws_t w;
+  if (hws_init(&w, 2, w_cap, 0)) return SPWS_ORA_NOMEM;
+  int32_t key[2];
+  for (int32_t j = 0; j < nj; j++) {                       /* :271 */
+    for (int32_t pa = Ap[j]; pa < Ap[j + 1]; pa++) {       /* :272 */
+      key[0] = Ai[pa];
+      for (int32_t pb = Bp[j]; pb < Bp[j + 1]; pb++) {     /* :275 */
+        key[1] = Bk[pb];
+        if (hws_insert(&w, key, Av[pa] * Bv[pb])) { hws_free(&w); return SPWS_ORA_NOMEM; }
+      }
+    }
+  }
+  if (hws_flush(&w)) { hws_free(&w); return SPWS_ORA_NOMEM; }
+  if (collisions) *collisions = (int32_t)w.same_key_hits;
+  const int32_t ni = C_noT->dimensions[0];
+  int rc = coo2_to_csr(C_noT, &w.all, ni);
+  hws_free(&w);
+  if (rc != SPWS_ORA_OK) return rc;
+  /* transpose (:354-403): count per column, prefix, stable scatter over the
+     rows of C_noT in order, then shift the positions back by one fiber */
+  const int32_t nk = C->dimensions[0];
+  const int32_t* Tp = C_noT->indices[1][0];
+  const int32_t* Tc = C_noT->indices[1][1];
+  const double* Tv = C_noT->vals;
+  const int64_t nnz = Tp[ni];
+  int32_t* pos = (int32_t*)calloc((size_t)nk + 1, sizeof(int32_t));
+  int32_t* crd = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nnz ? nnz : 1));
+  double* vals = (double*)malloc(sizeof(double) * (size_t)(nnz ? nnz : 1));
+  if (!pos || !crd || !vals) { free(pos); free(crd); free(vals); return SPWS_ORA_NOMEM; }
+  for (int64_t p = 0; p < nnz; p++) pos[Tc[p] + 1]++;
+  for (int32_t k = 0; k < nk; k++) pos[k + 1] += pos[k];
+  for (int32_t i = 0; i < ni; i++) {
+    for (int32_t p = Tp[i]; p < Tp[i + 1]; p++) {
+      const int32_t q = pos[Tc[p]]++;
+      crd[q] = i;
+      vals[q] = Tv[p];
+    }
+  }
+  for (int32_t k = nk; k > 0; k--) pos[k] = pos[k - 1];
+  pos[0] = 0;
+  C->indices[1][0] = pos;
+  C->indices[1][1] = crd;
+  C->vals = vals;
+  C->vals_size = C_noT->vals_size;
+  return SPWS_ORA_OK;
+}
+
+/* ------------------------------------------------------------------------ */
 /* MTTKRP A(i,j) = sum_{k,l} B(k,l,i) C(k,j) D(l,j).                        */
 /* Loop nest of benchmark/MTTKRP/COO_CSF_DCSR_DCSR_hash_free.h:277-332; the */
 /* product is (B*C)*D as written at :307.                                   */

@@ -22,6 +22,8 @@ int ora_dcsc_dcsr_coord_faithful(taco_tensor_t* C, const taco_tensor_t* A, const
 int ora_dcsc_dcsr_bucket(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap);
 int ora_csc_csr_t_hash(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap,
                        int32_t* collisions);
+int ora_csc_csr_t_hash_nofuse(taco_tensor_t* C_noT, taco_tensor_t* C, const taco_tensor_t* A,
+                              const taco_tensor_t* B, int32_t w_cap, int32_t* collisions);
 int ora_mttkrp_hash(taco_tensor_t* A, const taco_tensor_t* B, const taco_tensor_t* C, const taco_tensor_t* D,
                     int32_t w_cap);
 int ora_mttkrp_bucket(taco_tensor_t* A, const taco_tensor_t* B, const taco_tensor_t* C, const taco_tensor_t* D,

@@ -98,6 +98,15 @@ def main():
     save("spgemm_t_er100", **pack("A", A), **pack("B", B), t_pos=p, t_crd=c, t_vals=v,
          t_collisions=np.array(coll), t16_pos=pb, t16_crd=cb, t16_vals=vb, t16_collisions=np.array(collb),
          meta=np.array("C^T=(A*B)^T, er n=100 per_row 5/6 seeds 15/16; t16 = w_cap 16"))
+    # its non-fused form (evaluate/CSC_CSR_T_hash_record_nofuse.h): the (i, k)
+    # hash gives C_noT = A*B, TACO's transpose then gives C
+    outs = {}
+    for tag, wc in (("n", None), ("n16", 16)):
+        (p, c, v), (tp, tc, tv), coll = oracle.spgemm_t_nofuse(A, B, w_cap=wc, kind="ref")
+        outs.update({tag + "_noT_pos": p, tag + "_noT_crd": c, tag + "_noT_vals": v, tag + "_pos": tp,
+                     tag + "_crd": tc, tag + "_vals": tv, tag + "_collisions": np.array(coll)})
+    save("spgemm_t_nofuse_er100", **pack("A", A), **pack("B", B), **outs,
+         meta=np.array("C_noT=A*B then C=C_noT^T, same A/B as spgemm_t_er100; n16 = w_cap 16"))
 
     # MTTKRP: CSF levels (k, l, i) with i the output row; factors dense rank R
     i0, i1, i2, tv = gen.tensor3((90, 60, 40), 2500, zipf_s=1.1, seed=17)

@@ -57,6 +57,22 @@ def test_port_matches_reference_golden_transposed():
         assert coll == int(z[tag + "_collisions"])
 
 
+def test_port_matches_reference_golden_transposed_nofuse():
+    z = load("spgemm_t_nofuse_er100")
+    zf = load("spgemm_t_er100")
+    A, B = csr(z, "A"), csr(z, "B")
+    for tag, wc in (("n", None), ("n16", 16)):
+        (p, c, v), (tp, tc, tv), coll = oracle.spgemm_t_nofuse(A, B, w_cap=wc, kind="port")
+        assert np.array_equal(p, z[tag + "_noT_pos"]) and np.array_equal(c, z[tag + "_noT_crd"])
+        assert np.array_equal(v, z[tag + "_noT_vals"])
+        assert np.array_equal(tp, z[tag + "_pos"]) and np.array_equal(tc, z[tag + "_crd"])
+        assert np.array_equal(tv, z[tag + "_vals"])
+        assert coll == int(z[tag + "_collisions"])
+        # the fused and non-fused forms give the same C^T structure
+        assert np.array_equal(tp, zf["t_pos"]) and np.array_equal(tc, zf["t_crd"])
+        np.testing.assert_allclose(tv, zf["t_vals"], rtol=1e-13, atol=1e-15)
+
+
 @pytest.mark.parametrize("R", [4, 16])
 def test_port_matches_reference_golden_mttkrp(R):
     z = load(f"mttkrp_R{R}_s17")
@@ -133,3 +149,17 @@ def test_port_matches_live_reference_tensors():
         g = oracle.ttm(m, (i0, i2, i1, tv), (70, 30, 50), Ct, w_cap=40, kind="port")
         r = oracle.ttm(m, (i0, i2, i1, tv), (70, 30, 50), Ct, w_cap=40, kind="ref")
         assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
+
+
+@needs_ref
+@pytest.mark.parametrize("wcap", [None, 24])
+def test_port_matches_live_reference_transposed(wcap):
+    A, B = gen.rmat(8, 5, seed=38), gen.rmat(8, 4, seed=39)
+    (g, gc) = oracle.spgemm_t(A, B, w_cap=wcap, kind="port")
+    (r, rc) = oracle.spgemm_t(A, B, w_cap=wcap, kind="ref")
+    assert gc == rc and all(np.array_equal(a, b) for a, b in zip(g, r))
+    g = oracle.spgemm_t_nofuse(A, B, w_cap=wcap, kind="port")
+    r = oracle.spgemm_t_nofuse(A, B, w_cap=wcap, kind="ref")
+    assert g[2] == r[2]
+    for x, y in ((g[0], r[0]), (g[1], r[1])):
+        assert all(np.array_equal(a, b) for a, b in zip(x, y))
