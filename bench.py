@@ -505,6 +505,155 @@ def bench_batched(args):
     print(json.dumps(line), flush=True)
 
 
+# (A*A)^T suite of the transposed-output comparison: output nnz from ~1e4 to
+# ~1e8 and collision ratios (products landing on an existing entry / products)
+# from ~0.05 to ~0.9, seeded synthetic stand-ins for the unnamed SuiteSparse
+# matrices behind the reference's fusion-speedup plots.
+TRANSPOSE_SUITE = [("er", 600, 3), ("er", 2000, 5), ("er", 30000, 8), ("er", 300000, 10), ("er", 2000000, 7),
+                   ("er", 10000, 60), ("er", 2500, 50),
+                   ("rmat", 10, 8), ("rmat", 13, 8), ("rmat", 15, 8), ("rmat", 17, 6),
+                   ("band", 10000, 8), ("band", 200000, 8), ("band", 2000000, 8), ("band", 400000, 32),
+                   ("band", 100000, 64)]
+
+
+def transpose_suite_matrix(kind, a, b, seed=42):
+    from sparsews_gb300 import gen
+    if kind == "er":
+        return gen.er(a, b, seed=seed), {"kind": "er", "n": a, "per_row": b}
+    if kind == "rmat":
+        return gen.rmat(a, b, seed=seed), {"kind": "rmat", "scale": a, "edge_draws_per_row": b}
+    return gen.band(a, b, 0.5, seed=seed), {"kind": "band", "n": a, "half_bandwidth": b, "fill": 0.5}
+
+
+def gstats(xs):
+    xs = [x for x in xs if x > 0]
+    if not xs:
+        return None
+    return {"gmean": float(np.exp(np.mean(np.log(xs)))), "min": float(min(xs)), "max": float(max(xs)), "count": len(xs)}
+
+
+def bench_transpose(args):
+    """Fused vs non-fused transposed-output SpGEMM C = (A*A)^T
+    (evaluate/CSC_CSR_T_hash_record.h against _nofuse.h), the comparison
+    behind the reference's only published figures: speedup of the fused form
+    binned by output nnz and by collision ratio (gmean / min / max per bin,
+    the statistics of scripts/draw_bars.py). Per matrix: the device form
+    (operands resident, CUDA-event times, L2 flushed) and the drop-in entry
+    points CSC_CSR_T_hash / CSC_CSR_T_hash_nonfuse with host arrays (wall
+    time, copies included); on the smaller matrices also the oracle's CPU
+    restatement of both reference functions on one host core."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import build, taco
+    build.build()
+    L = sp.lib()
+    sp.check(L.spws_set_device(0))
+    ora = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        if oracle.available("port"):
+            ora = oracle._load("port")
+    rows = []
+    with ClockSampler(0) as clk:
+        for kind, a, b in TRANSPOSE_SUITE:
+            A, desc = transpose_suite_matrix(kind, a, b)
+            n, m = A[3], A[4]
+            tp, tc, tv = sp._csr_transpose_np(*A)
+            At = sp.DeviceCsr.upload(tp, tc, tv, m, n)
+            Bd = sp.DeviceCsr.upload(*A)
+            dev = {True: [], False: []}
+            split = {}
+            for it in range(args.warmup + args.steps):
+                for fuse in (True, False):
+                    sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+                    Cd, _, st = sp.spgemm_t_device(At, Bd, fuse=fuse)
+                    Cd.release()
+                    if it >= args.warmup:
+                        dev[fuse].append(st.ms_total)
+                        split[fuse] = [st.ms_input_transpose, st.ms_spgemm, st.ms_output_transpose]
+                    products, nnz = int(st.products), int(st.nnz)
+            At.release()
+            Bd.release()
+            # drop-in entry points with host arrays
+            Ah = taco.csc(tp, tc, tv, n, m)
+            Bh = taco.csr(*A)
+            e2e = {True: [], False: []}
+            coll = C.c_int32(0)
+            for it in range(1 + args.e2e_steps):
+                for fuse in (True, False):
+                    Ct = taco.init_dc(m, n)
+                    if fuse:
+                        t = L.CSC_CSR_T_hash(Ah.ptr(), Bh.ptr(), Ct.ptr(), 0, C.byref(coll))
+                    else:
+                        Nt = taco.init_dc(n, m)
+                        t = L.CSC_CSR_T_hash_nonfuse(Ah.ptr(), Bh.ptr(), Nt.ptr(), Ct.ptr(), 0, C.byref(coll))
+                        taco.take_csr(Nt, n, L.spws_free)
+                    if t < 0:
+                        raise RuntimeError(L.spws_last_error().decode())
+                    taco.take_csr(Ct, m, L.spws_free)
+                    if it >= 1:
+                        e2e[fuse].append(t * 1e3)
+            row = dict(desc, nnz_A=int(len(A[1])), products=products, nnz_C=nnz,
+                       collision_ratio=(products - nnz) / max(products, 1),
+                       device={"fused_ms": statistics.median(dev[True]), "nofuse_ms": statistics.median(dev[False]),
+                               "fused_split_ms": split[True], "nofuse_split_ms": split[False]},
+                       e2e={"fused_ms": statistics.median(e2e[True]), "nofuse_ms": statistics.median(e2e[False])})
+            for k in ("device", "e2e"):
+                row[k]["speedup"] = row[k]["nofuse_ms"] / row[k]["fused_ms"]
+            if ora is not None and products <= args.transpose_cpu_products:
+                lib, pre, fr = ora
+                wc = 1 << max(0, int(np.floor(np.log2(max(len(A[1]), 1)))))
+                tcpu = {}
+                for fuse in (True, False):
+                    Ct, Nt = taco.init_dc(m, n), taco.init_dc(n, m)
+                    c = C.c_int32(0)
+                    t0 = time.perf_counter()
+                    if fuse:
+                        rc = getattr(lib, pre + "csc_csr_t_hash")(Ct.ptr(), Ah.ptr(), Bh.ptr(), wc, C.byref(c))
+                    else:
+                        rc = getattr(lib, pre + "csc_csr_t_hash_nofuse")(Nt.ptr(), Ct.ptr(), Ah.ptr(), Bh.ptr(), wc,
+                                                                         C.byref(c))
+                    tcpu[fuse] = (time.perf_counter() - t0) * 1e3
+                    if rc != 0:
+                        raise RuntimeError("oracle failed")
+                    taco.take_csr(Ct, m, fr)
+                    if not fuse:
+                        taco.take_csr(Nt, n, fr)
+                row["cpu_port"] = {"fused_ms": tcpu[True], "nofuse_ms": tcpu[False],
+                                   "speedup": tcpu[False] / tcpu[True], "cores": 1}
+            rows.append(row)
+            print(json.dumps({"matrix": row}), file=sys.stderr, flush=True)
+
+    def bins(key, edges, leg):
+        out = []
+        for lo, hi in zip(edges[:-1], edges[1:]):
+            xs = [r[leg]["speedup"] for r in rows if leg in r and lo <= r[key] < hi]
+            if xs:
+                out.append({"range": [lo, hi], **gstats(xs)})
+        return out
+
+    nnz_edges = [0, 1e4, 1e5, 1e6, 1e7, 1e8, 1e10]
+    coll_edges = [0.0, 0.2, 0.4, 0.6, 0.8, 1.0001]
+    dev_all = gstats([r["device"]["speedup"] for r in rows])
+    e2e_all = gstats([r["e2e"]["speedup"] for r in rows])
+    line = {"metric": "transposed_output_fusion_speedup_gmean", "value": e2e_all["gmean"], "unit": "x",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "transposed_output_AxA_fused_vs_nofuse", "matrices": len(rows),
+                       "l2": "flushed between device-timed calls"},
+            "e2e": {"what": "CSC_CSR_T_hash_nonfuse / CSC_CSR_T_hash wall time, host arrays", **e2e_all,
+                    "by_output_nnz": bins("nnz_C", nnz_edges, "e2e"),
+                    "by_collision_ratio": bins("collision_ratio", coll_edges, "e2e")},
+            "device": {"what": "spws_spgemm_t_device fuse=0 / fuse=1, CUDA-event time", **dev_all,
+                       "by_output_nnz": bins("nnz_C", nnz_edges, "device"),
+                       "by_collision_ratio": bins("collision_ratio", coll_edges, "device")},
+            "cpu_port": {"what": "the oracle's restatement of both reference functions, one core",
+                         "by_output_nnz": bins("nnz_C", nnz_edges, "cpu_port"),
+                         "by_collision_ratio": bins("collision_ratio", coll_edges, "cpu_port")},
+            "matrices": rows, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 TENSOR = dict(dims=(50000, 40000, 20000), nnz=20_000_000, zipf_s=1.1, seed=42)
 
 
@@ -765,7 +914,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spws", choices=["spws", "reference"])
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched", "served", "mttkrp", "ttm"])
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched", "served", "mttkrp", "ttm", "transpose"])
     ap.add_argument("--instances", type=int, default=1024,
                     help="batched workload: number of products (4096 holds ~220 GB of output at once)")
     ap.add_argument("--plain-sample", type=int, default=512, help="batched workload: one-at-a-time ABI sample")
@@ -775,6 +924,8 @@ def main():
     ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
                     help="products per step of the reference arm (all cores)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--transpose-cpu-products", type=int, default=30_000_000,
+                    help="transpose workload: largest product count timed on the CPU port")
     ap.add_argument("--rank", type=int, default=32, help="mttkrp/ttm workloads: factor rank R")
     ap.add_argument("--served-requests", type=int, default=400, help="served workload: requests per run")
     ap.add_argument("--served-pool", type=int, default=512, help="served workload: distinct small products")
@@ -793,6 +944,9 @@ def main():
     elif args.workload in ("mttkrp", "ttm"):
         if rank == 0 and args.impl != "reference":
             bench_tensor(args)
+    elif args.workload == "transpose":
+        if rank == 0 and args.impl != "reference":
+            bench_transpose(args)
     elif args.impl == "reference":
         bench_reference(args, ws, rank, dist)
     else:

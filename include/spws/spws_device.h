@@ -100,6 +100,29 @@ int spws_spgemm_csr_device(const spws_csr_dev* A, const spws_csr_dev* B, spws_cs
 int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev* B, int32_t* C_pos, int32_t* C_crd,
                             double* C_vals, int64_t c_cap, int64_t* c_nnz);
 
+/* Statistics of a transposed-output product (spws_spgemm_t_device). */
+typedef struct spws_spgemm_t_stats {
+  int64_t products;          /* scalar products a_ij * b_jk */
+  int64_t nnz;               /* output nonzeros */
+  float ms_input_transpose;  /* B -> B^T (fused) or A^T -> A (non-fused), device time */
+  float ms_spgemm;           /* the row-wise pipeline, device time */
+  float ms_output_transpose; /* A*B -> (A*B)^T, non-fused only */
+  float ms_total;            /* all of the above */
+} spws_spgemm_t_stats;
+
+/* C = (A*B)^T on the device, the device form of CSC_CSR_T_hash (taco_abi.h).
+ * At holds A's CSC arrays, which are the CSR arrays of A^T (At->nrows = B's
+ * row count, At->ncols = A's row count); B is CSR.
+ *  fuse = 1: C's rows are computed directly as B^T * A^T (the reference's
+ *            key swap, evaluate/CSC_CSR_T_hash_record.h:275,278);
+ *  fuse = 0: C_noT = A*B, then C = C_noT^T (its non-fused form,
+ *            evaluate/CSC_CSR_T_hash_record_nofuse.h:405-412). C_noT (may be
+ *            NULL) receives A*B; it is left empty when fuse = 1.
+ * Results are library-owned (free with spws_csr_release). `stats` may be
+ * NULL. Returns when the work has finished. */
+int spws_spgemm_t_device(const spws_csr_dev* At, const spws_csr_dev* B, int32_t fuse, spws_csr_dev* C,
+                         spws_csr_dev* C_noT, spws_spgemm_t_stats* stats);
+
 /* Make `device` current for the calling thread (cudaSetDevice). */
 int spws_set_device(int device);
 

@@ -175,6 +175,19 @@ int spws_csc_csr_t_hash_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_
  * reference; C takes a pointer). */
 double CSC_CSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t* collisions);
 
+/* The non-fused form of the same product: C_noT = A*B in CSR over i, then
+ * C = C_noT^T. Both outputs are returned (malloc'd arrays, as the reference
+ * fills both). Replaces `int compute_nofuse(C_noT, A, B, w_cap)` followed by
+ * `int transpose(C, C_noT)` of evaluate/CSC_CSR_T_hash_record_nofuse.h:234,354.
+ * `collisions` as above. */
+int spws_csc_csr_t_hash_nofuse_compute(taco_tensor_t* C_noT, taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B,
+                                       int32_t w_cap, int32_t* collisions);
+
+/* Replaces `double CSC_CSR_T_hash_nonfuse(A, B, C_noT, C, int w_cap, int&
+ * collisions)` of evaluate/CSC_CSR_T_hash_record_nofuse.h:405. */
+double CSC_CSR_T_hash_nonfuse(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C_noT, taco_tensor_t* C,
+                              int32_t w_cap, int32_t* collisions);
+
 /* ------------------------------------------------------------------------ */
 /* MTTKRP A(i,j) = sum_{k,l} B(k,l,i) * C(k,j) * D(l,j): B in CSF (k,l,i),     */
 /* C and D in DCSR, A is sorted 2-D COO.                                        */

@@ -55,6 +55,11 @@ class SpgemmStats(C.Structure):
                 ("chunk_width", C.c_int32), ("n_chunks", C.c_int32)]
 
 
+class SpgemmTStats(C.Structure):
+    _fields_ = [("products", C.c_int64), ("nnz", C.c_int64), ("ms_input_transpose", C.c_float),
+                ("ms_spgemm", C.c_float), ("ms_output_transpose", C.c_float), ("ms_total", C.c_float)]
+
+
 def lib():
     """Load libspws.so (raises if it has not been built: there is no fallback)."""
     global _lib
@@ -85,6 +90,8 @@ def lib():
         "DCSC_DCSR_bucket": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
         "DCSC_DCSR_coord": ([P, P, P, C.c_int32, C.c_bool], None),
         "CSC_CSR_T_hash": ([P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_double),
+        "spws_csc_csr_t_hash_nofuse_compute": ([P, P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+        "CSC_CSR_T_hash_nonfuse": ([P, P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_double),
         "spws_coo_csf_dcsr_dcsr_hash_compute": ([P, P, P, P, C.c_int32], C.c_int),
         "spws_coo_csf_dcsr_dcsr_bucket_compute": ([P, P, P, P, C.c_int32], C.c_int),
         "spws_coo_csf_dcsr_hash_compute": ([P, P, P, C.c_int32], C.c_int),
@@ -105,6 +112,8 @@ def lib():
         "spws_spgemm_csr_device": ([C.POINTER(CsrDev), C.POINTER(CsrDev), C.POINTER(CsrDev), C.c_int,
                                     C.POINTER(SpgemmStats)], C.c_int),
         "spws_csr_set_values": ([C.POINTER(CsrDev), C.c_void_p], C.c_int),
+        "spws_spgemm_t_device": ([C.POINTER(CsrDev), C.POINTER(CsrDev), C.c_int32, C.POINTER(CsrDev),
+                                  C.POINTER(CsrDev), C.POINTER(SpgemmTStats)], C.c_int),
         "spws_spgemm_csr_device_tuned": ([C.POINTER(CsrDev), C.POINTER(CsrDev), C.POINTER(CsrDev),
                                           C.POINTER(Tuning), C.POINTER(SpgemmStats)], C.c_int),
         "spws_spgemm_batched_tuned": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p),
@@ -185,9 +194,11 @@ def spgemm_outer(A, B, method="hash"):
     return taco.take_csr(Ct, an, L.spws_free)
 
 
-def spgemm_t(A, B):
-    """C^T = (A*B)^T with A passed as CSC and B as CSR (CSC_CSR_T_hash).
-    Returns ((pos, crd, vals) of C^T, collisions)."""
+def spgemm_t(A, B, fuse=True):
+    """C^T = (A*B)^T with A passed as CSC and B as CSR (CSC_CSR_T_hash, or with
+    fuse=False its non-fused form CSC_CSR_T_hash_nonfuse).
+    Returns ((pos, crd, vals) of C^T, collisions); with fuse=False
+    ((C_noT = A*B), (C^T), collisions)."""
     L = lib()
     ap, ac, av, an, am = A
     bp, bc, bv, bn, bm = B
@@ -196,8 +207,12 @@ def spgemm_t(A, B):
     Bt = taco.csr(bp, bc, bv, bn, bm)
     Ct = taco.init_dc(bm, an)
     coll = C.c_int32(0)
-    check(L.spws_csc_csr_t_hash_compute(Ct.ptr(), At.ptr(), Bt.ptr(), 0, C.byref(coll)))
-    return taco.take_csr(Ct, bm, L.spws_free), int(coll.value)
+    if fuse:
+        check(L.spws_csc_csr_t_hash_compute(Ct.ptr(), At.ptr(), Bt.ptr(), 0, C.byref(coll)))
+        return taco.take_csr(Ct, bm, L.spws_free), int(coll.value)
+    Nt = taco.init_dc(an, bm)
+    check(L.spws_csc_csr_t_hash_nofuse_compute(Nt.ptr(), Ct.ptr(), At.ptr(), Bt.ptr(), 0, C.byref(coll)))
+    return taco.take_csr(Nt, an, L.spws_free), taco.take_csr(Ct, bm, L.spws_free), int(coll.value)
 
 
 def mttkrp(Bcoo, dims, Cf, Df, method="bucket"):
@@ -282,6 +297,17 @@ def spgemm_device(A, B, accum_mode=0, tuning=None):
         check(L.spws_spgemm_csr_device_tuned(C.byref(A.m), C.byref(B.m), C.byref(Cd.m), C.byref(tuning),
                                              C.byref(st)))
     return Cd, st
+
+
+def spgemm_t_device(At, B, fuse=True, keep_noT=False):
+    """(A*B)^T for DeviceCsr operands, At holding A's CSC arrays (the CSR of
+    A^T). Returns (DeviceCsr C, DeviceCsr C_noT or None, SpgemmTStats)."""
+    L = lib()
+    Cd, Nd = DeviceCsr(), DeviceCsr()
+    st = SpgemmTStats()
+    check(L.spws_spgemm_t_device(C.byref(At.m), C.byref(B.m), 1 if fuse else 0, C.byref(Cd.m),
+                                 C.byref(Nd.m) if keep_noT and not fuse else None, C.byref(st)))
+    return Cd, (Nd if keep_noT and not fuse else None), st
 
 
 def autotune(A, B, repeats=1):

@@ -10,6 +10,7 @@
 #include "abi_util.h"
 #include "convert.h"
 #include "spws_internal.h"
+#include "validate.h"
 
 namespace spws {
 namespace abi {
@@ -121,6 +122,110 @@ int dcsc_dcsr(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, Engine eng) 
   return run_into(C, view(dA.m), view(dB.m), eng, nullptr, s);
 }
 
+struct Event {
+  cudaEvent_t e = nullptr;
+  ~Event() {
+    if (e) cudaEventDestroy(e);
+  }
+};
+
+float elapsed(const Event& a, const Event& b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a.e, b.e);
+  return ms;
+}
+
+// (A*B)^T from A's CSC arrays (which are the CSR arrays of A^T) and B in CSR.
+// Fused: the result's rows are the k of B, computed directly as B^T * A^T
+// row by row -- the key swap of evaluate/CSC_CSR_T_hash_record.h:275,278.
+// Non-fused: C_noT = A*B row by row, then transposed, as
+// evaluate/CSC_CSR_T_hash_record_nofuse.h:405-412 runs compute_nofuse and
+// transpose. Either way the input the row-wise pipeline needs in CSR (B^T, or
+// A) is built first by a device transpose. C_noT may be null.
+int t_product(const CsrView& At, const CsrView& B, bool fuse, spws_csr_dev* C, spws_csr_dev* C_noT,
+              spws_spgemm_t_stats* st, cudaStream_t s) {
+  Event ev[4];
+  for (auto& e : ev) SPWS_CUDA(cudaEventCreate(&e.e));
+  SPWS_CUDA(cudaEventRecord(ev[0].e, s));
+  DevCsr in_t;  // B^T (fused) or A (non-fused)
+  in_t.s = s;
+  SPWS_TRY(csr_transpose(fuse ? B : At, &in_t.m, s));
+  SPWS_CUDA(cudaEventRecord(ev[1].e, s));
+  spws_spgemm_stats sst{};
+  SpgemmOpts opt;
+  spws_csr_dev r{};
+  int rc = fuse ? spgemm_rowwise(view(in_t.m), At, &r, opt, &sst, s) : spgemm_rowwise(view(in_t.m), B, &r, opt, &sst, s);
+  if (rc != SPWS_OK) {
+    release(&r, s);
+    return rc;
+  }
+  SPWS_CUDA(cudaEventRecord(ev[2].e, s));
+  if (fuse) {
+    *C = r;
+  } else {
+    rc = csr_transpose(view(r), C, s);
+    if (rc != SPWS_OK || !C_noT) release(&r, s);
+    else *C_noT = r;
+    if (rc != SPWS_OK) {
+      release(C, s);
+      return rc;
+    }
+  }
+  SPWS_CUDA(cudaEventRecord(ev[3].e, s));
+  SPWS_CUDA(cudaEventSynchronize(ev[3].e));
+  if (st) {
+    st->products = sst.products;
+    st->nnz = sst.nnz;
+    st->ms_input_transpose = elapsed(ev[0], ev[1]);
+    st->ms_spgemm = elapsed(ev[1], ev[2]);
+    st->ms_output_transpose = elapsed(ev[2], ev[3]);
+    st->ms_total = elapsed(ev[0], ev[3]);
+  }
+  return SPWS_OK;
+}
+
+// Host entry of both forms: uploads A (CSC, outer level over j) and B (CSR),
+// runs t_product and copies C (and C_noT) back into malloc'd arrays.
+int csc_csr_t(taco_tensor_t* C_noT, taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, bool fuse,
+              int32_t* collisions) {
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  int32_t aj, ai, bn, bm;
+  int64_t annz, bnnz;
+  SPWS_TRY(check_dc(A, "A", 1, &aj, &ai, &annz));  // outer = columns j, inner = rows i
+  SPWS_TRY(check_dc(B, "B", 0, &bn, &bm, &bnnz));
+  SPWS_TRY(check_out_dc(C, "C"));
+  if (aj != bn || C->dimensions[0] != bm) {
+    set_error("shape mismatch: A is i x j (CSC), B j x k, C must have k rows");
+    return SPWS_ERR_INVALID;
+  }
+  if (!fuse) {
+    SPWS_TRY(check_out_dc(C_noT, "C_noT"));
+    if (C_noT->dimensions[0] != ai) {
+      set_error("shape mismatch: C_noT must have A's i rows");
+      return SPWS_ERR_INVALID;
+    }
+  }
+  cudaStream_t s = ds->stream;
+  DevCsr dAt, dB, rC, rN;
+  SPWS_TRY(upload(A->indices[1][0], A->indices[1][1], A->vals, aj, ai, annz, "A", &dAt, s));
+  SPWS_TRY(upload(B->indices[1][0], B->indices[1][1], B->vals, bn, bm, bnnz, "B", &dB, s));
+  rC.s = rN.s = s;
+  spws_spgemm_t_stats st{};
+  SPWS_TRY(t_product(view(dAt.m), view(dB.m), fuse, &rC.m, fuse ? nullptr : &rN.m, &st, s));
+  if (!fuse) SPWS_TRY(download_into(C_noT, rN.m, s));
+  int rc = download_into(C, rC.m, s);
+  if (rc != SPWS_OK) {
+    if (!fuse) free_csr_out(C_noT);
+    return rc;
+  }
+  // products that found their output entry already present: the reference's
+  // collision count when its buffer never refreshes
+  if (collisions) *collisions = (int32_t)(st.products - st.nnz);
+  return SPWS_OK;
+}
+
 }  // namespace
 }  // namespace abi
 }  // namespace spws
@@ -196,35 +301,42 @@ int spws_csr_csr_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t
   return run_into(C, view(dA.m), view(dB.m), Engine::Coord, nullptr, s);
 }
 
-// C = (A*B)^T with A in CSC (dense outer level over j) and B in CSR, computed
-// as B^T * A^T row by row: the rows of the result are indexed by k, the key
-// the reference swaps in (evaluate/CSC_CSR_T_hash_record.h:275,278). The
-// CSC arrays of A are the CSR arrays of A^T; B^T is built on the device.
+// C = (A*B)^T with A in CSC (dense outer level over j) and B in CSR, the
+// result's rows indexed by k (evaluate/CSC_CSR_T_hash_record.h:234).
 int spws_csc_csr_t_hash_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap,
                                 int32_t* collisions) {
   (void)w_cap;
+  return csc_csr_t(nullptr, C, A, B, true, collisions);
+}
+
+// The non-fused form: C_noT = A*B, then C = C_noT^T
+// (evaluate/CSC_CSR_T_hash_record_nofuse.h:234,354). Both are returned.
+int spws_csc_csr_t_hash_nofuse_compute(taco_tensor_t* C_noT, taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B,
+                                       int32_t w_cap, int32_t* collisions) {
+  (void)w_cap;
+  return csc_csr_t(C_noT, C, A, B, false, collisions);
+}
+
+double CSC_CSR_T_hash_nonfuse(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C_noT, taco_tensor_t* C,
+                              int32_t w_cap, int32_t* collisions) {
+  const double t0 = now_s();
+  if (spws_csc_csr_t_hash_nofuse_compute(C_noT, C, A, B, w_cap, collisions) != SPWS_OK) return -1.0;
+  return now_s() - t0;
+}
+
+int spws_spgemm_t_device(const spws_csr_dev* At, const spws_csr_dev* B, int32_t fuse, spws_csr_dev* C,
+                         spws_csr_dev* C_noT, spws_spgemm_t_stats* stats) {
   clear_error();
-  DeviceState* ds = nullptr;
-  SPWS_TRY(device_state(&ds));
-  int32_t aj, ai, bn, bm;
-  int64_t annz, bnnz;
-  SPWS_TRY(check_dc(A, "A", 1, &aj, &ai, &annz));  // outer = columns j, inner = rows i
-  SPWS_TRY(check_dc(B, "B", 0, &bn, &bm, &bnnz));
-  SPWS_TRY(check_out_dc(C, "C"));
-  if (aj != bn || C->dimensions[0] != bm) {
-    set_error("shape mismatch: A is i x j (CSC), B j x k, C must have k rows");
+  if (!At || !B || !C || At->nrows != B->nrows) {
+    set_error("spws_spgemm_t_device: bad arguments or shape mismatch (At must have B's row count)");
     return SPWS_ERR_INVALID;
   }
-  cudaStream_t s = ds->stream;
-  DevCsr dAt, dB, dBt;
-  SPWS_TRY(upload(A->indices[1][0], A->indices[1][1], A->vals, aj, ai, annz, "A", &dAt, s));
-  SPWS_TRY(upload(B->indices[1][0], B->indices[1][1], B->vals, bn, bm, bnnz, "B", &dB, s));
-  dBt.s = s;
-  SPWS_TRY(csr_transpose(view(dB.m), &dBt.m, s));
-  spws_spgemm_stats st{};
-  SPWS_TRY(run_into(C, view(dBt.m), view(dAt.m), Engine::Rowwise, &st, s));
-  if (collisions) *collisions = (int32_t)(st.products - st.nnz);
-  return SPWS_OK;
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  SPWS_TRY(validate_csr_device(At->pos, At->crd, At->nrows, At->ncols, At->nnz, "At", ds->stream));
+  if (B != At) SPWS_TRY(validate_csr_device(B->pos, B->crd, B->nrows, B->ncols, B->nnz, "B", ds->stream));
+  if (C_noT) *C_noT = spws_csr_dev{};
+  return t_product(view(*At), view(*B), fuse != 0, C, fuse ? nullptr : C_noT, stats, ds->stream);
 }
 
 double CSC_CSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t* collisions) {

@@ -47,45 +47,57 @@ __global__ void k_validate_cc(int32_t nq, int32_t outer_dim, int32_t inner_dim, 
   if (!__all_sync(0xffffffffu, ok) && lane == 0) atomicExch(bad, 1);
 }
 
-// keys[p] = row(p) * ncols + col(p) for a compressed-outer matrix whose outer
-// coordinates are columns (DCSC): row = inner crd, col = outer coordinate.
+// Transposes sort only the major coordinate. Keys are (major << minor_bits) |
+// minor, written in the input's order, which is already ascending in the
+// minor coordinate (a DCSC walks columns in order, a CSR rows in order), so a
+// stable sort of the major bits alone leaves every output fiber sorted.
+
+// keys[p] = (row(p) << col_bits) | col(p) for a compressed-outer matrix whose
+// outer coordinates are columns (DCSC): row = inner crd, col = outer coordinate.
 __global__ void k_cc_transposed_keys(int32_t nq, const int32_t* __restrict__ oc, const int32_t* __restrict__ pos,
-                                     const int32_t* __restrict__ ic, const double* __restrict__ vals, int32_t ncols,
+                                     const int32_t* __restrict__ ic, const double* __restrict__ vals, int col_bits,
                                      unsigned long long* __restrict__ keys, unsigned long long* __restrict__ pay) {
   const int lane = threadIdx.x & 31;
   const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= nq) return;
   const int32_t col = oc[q];
   for (int32_t p = pos[q] + lane; p < pos[q + 1]; p += 32) {
-    keys[p] = (unsigned long long)ic[p] * (unsigned long long)ncols + (unsigned long long)col;
+    keys[p] = ((unsigned long long)ic[p] << col_bits) | (unsigned long long)col;
     pay[p] = __double_as_longlong(vals[p]);
   }
 }
 
-// keys[p] = col(p) * nrows + row(p) for a CSR (its transpose order).
+// keys[p] = (col(p) << row_bits) | row(p) for a CSR (its transpose order).
 __global__ void k_csr_transposed_keys(int32_t nrows, const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
-                                      const double* __restrict__ vals, unsigned long long* __restrict__ keys,
-                                      unsigned long long* __restrict__ pay) {
+                                      const double* __restrict__ vals, int row_bits,
+                                      unsigned long long* __restrict__ keys, unsigned long long* __restrict__ pay) {
   const int lane = threadIdx.x & 31;
   const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= nrows) return;
   for (int32_t p = pos[i] + lane; p < pos[i + 1]; p += 32) {
-    keys[p] = (unsigned long long)crd[p] * (unsigned long long)nrows + (unsigned long long)i;
+    keys[p] = ((unsigned long long)crd[p] << row_bits) | (unsigned long long)i;
     pay[p] = __double_as_longlong(vals[p]);
   }
 }
 
-// Sorted (major * minor_dim + minor) keys -> CSR crd/vals and major counts.
+// Sorted keys -> CSR. Thread p (0 <= p <= n) writes crd/vals of entry p and
+// the positions of every major coordinate in (major(p-1), major(p)], so each
+// of out_pos[0 .. nmajor] is written exactly once, with no counts or scan;
+// thread n stands for the sentinel major nmajor.
 __global__ void k_keys_to_csr(int64_t n, const unsigned long long* __restrict__ keys,
-                              const unsigned long long* __restrict__ pay, int32_t minor_dim, int32_t* __restrict__ crd,
-                              double* __restrict__ vals, int32_t* __restrict__ counts) {
+                              const unsigned long long* __restrict__ pay, int minor_bits, int32_t nmajor,
+                              int32_t* __restrict__ crd, double* __restrict__ vals, int32_t* __restrict__ out_pos) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const unsigned long long k = keys[p];
-  const int32_t major = (int32_t)(k / (unsigned long long)minor_dim);
-  crd[p] = (int32_t)(k % (unsigned long long)minor_dim);
-  vals[p] = __longlong_as_double((long long)pay[p]);
-  atomicAdd(&counts[major], 1);
+  if (p > n) return;
+  int64_t m = nmajor;
+  if (p < n) {
+    const unsigned long long k = keys[p];
+    m = (int64_t)(k >> minor_bits);
+    crd[p] = (int32_t)(k & ((1ull << minor_bits) - 1ull));
+    vals[p] = __longlong_as_double((long long)pay[p]);
+  }
+  const int64_t prev = p == 0 ? -1 : (int64_t)(keys[p - 1] >> minor_bits);
+  for (int64_t q = prev + 1; q <= m; q++) out_pos[q] = (int32_t)p;
 }
 
 // counts[outer coordinate] = fiber length, for expanding a compressed outer level.
@@ -97,25 +109,16 @@ __global__ void k_cc_counts(int32_t nq, const int32_t* __restrict__ oc, const in
 }
 
 int keys_to_csr(int64_t nnz, unsigned long long* keys, unsigned long long* pay, unsigned long long* ktmp,
-                unsigned long long* ptmp, int key_bits, int32_t nmajor, int32_t nminor, spws_csr_dev* out,
+                unsigned long long* ptmp, int minor_bits, int major_bits, int32_t nmajor, spws_csr_dev* out,
                 cudaStream_t s) {
   bool in_tmp = false;
-  SPWS_TRY(radix_sort_pairs(keys, pay, ktmp, ptmp, nnz, key_bits, &in_tmp, s));
+  SPWS_TRY(radix_sort_pairs(keys, pay, ktmp, ptmp, nnz, minor_bits + major_bits, &in_tmp, s, minor_bits));
   const unsigned long long* k = in_tmp ? ktmp : keys;
   const unsigned long long* v = in_tmp ? ptmp : pay;
-  int32_t* counts = nullptr;
-  SPWS_TRY(dalloc((void**)&counts, sizeof(int32_t) * std::max<int64_t>(nmajor, 1), s));
-  SPWS_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * std::max<int64_t>(nmajor, 1), s));
-  if (nnz > 0) {
-    k_keys_to_csr<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, k, v, nminor, out->crd, out->vals, counts);
-    count_launch(1);
-  }
-  long long* tot = nullptr;
-  SPWS_TRY(dalloc((void**)&tot, sizeof(long long), s));
-  SPWS_TRY(scan_counts_i32(counts, out->pos, nmajor, tot, s));
+  k_keys_to_csr<<<(unsigned)((nnz + 256) / 256), 256, 0, s>>>(nnz, k, v, minor_bits, nmajor, out->crd, out->vals,
+                                                             out->pos);
+  count_launch(1);
   SPWS_CUDA(cudaGetLastError());
-  dfree(tot, s);
-  dfree(counts, s);
   return SPWS_OK;
 }
 
@@ -168,12 +171,12 @@ int dcsc_to_csr(const int32_t* oc, const int32_t* pos, const int32_t* ic, const 
   SPWS_TRY(dalloc((void**)&p, b, s));
   SPWS_TRY(dalloc((void**)&kt, b, s));
   SPWS_TRY(dalloc((void**)&pt, b, s));
+  const int col_bits = bits_for((unsigned long long)ncols);
   if (nq > 0) {
-    k_cc_transposed_keys<<<(unsigned)((nq + 7) / 8), 256, 0, s>>>(nq, oc, pos, ic, vals, ncols, k, p);
+    k_cc_transposed_keys<<<(unsigned)((nq + 7) / 8), 256, 0, s>>>(nq, oc, pos, ic, vals, col_bits, k, p);
     count_launch(1);
   }
-  const int bits = bits_for((unsigned long long)std::max(nrows, 1) * (unsigned long long)std::max(ncols, 1));
-  int rc = keys_to_csr(nnz, k, p, kt, pt, bits, nrows, ncols, out, s);
+  int rc = keys_to_csr(nnz, k, p, kt, pt, col_bits, bits_for((unsigned long long)nrows), nrows, out, s);
   dfree(k, s);
   dfree(p, s);
   dfree(kt, s);
@@ -223,12 +226,13 @@ int csr_transpose(const CsrView& m, spws_csr_dev* out, cudaStream_t s) {
   SPWS_TRY(dalloc((void**)&p, b, s));
   SPWS_TRY(dalloc((void**)&kt, b, s));
   SPWS_TRY(dalloc((void**)&pt, b, s));
+  const int row_bits = bits_for((unsigned long long)m.nrows);
   if (m.nrows > 0) {
-    k_csr_transposed_keys<<<(unsigned)((m.nrows + 7) / 8), 256, 0, s>>>(m.nrows, m.pos, m.crd, m.vals, k, p);
+    k_csr_transposed_keys<<<(unsigned)((m.nrows + 7) / 8), 256, 0, s>>>(m.nrows, m.pos, m.crd, m.vals, row_bits, k,
+                                                                          p);
     count_launch(1);
   }
-  const int bits = bits_for((unsigned long long)std::max(m.nrows, 1) * (unsigned long long)std::max(m.ncols, 1));
-  int rc = keys_to_csr(nnz, k, p, kt, pt, bits, m.ncols, m.nrows, out, s);
+  int rc = keys_to_csr(nnz, k, p, kt, pt, row_bits, bits_for((unsigned long long)m.ncols), m.ncols, out, s);
   dfree(k, s);
   dfree(p, s);
   dfree(kt, s);

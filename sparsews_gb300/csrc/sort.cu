@@ -208,16 +208,17 @@ int scan_i64(const long long* in, long long* out, int64_t n, long long* total_de
 }
 
 int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigned long long* keys_tmp,
-                     unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s) {
+                     unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s,
+                     int begin_bit) {
   *result_in_tmp = false;
-  if (n <= 1 || key_bits <= 0) return SPWS_OK;
+  if (n <= 1 || key_bits <= begin_bit) return SPWS_OK;
   const int64_t ntiles = (n + kTile - 1) / kTile;
   int* hist = nullptr;
   long long* offs = nullptr;
   SPWS_TRY(dalloc((void**)&hist, sizeof(int) * kBins * ntiles, s));
   SPWS_TRY(dalloc((void**)&offs, sizeof(long long) * kBins * ntiles, s));
   unsigned long long *ka = keys, *va = vals, *kb = keys_tmp, *vb = vals_tmp;
-  for (int shift = 0; shift < key_bits; shift += kRadixBits) {
+  for (int shift = begin_bit; shift < key_bits; shift += kRadixBits) {
     k_radix_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, hist);
     SPWS_TRY(scan_i32_to_i64(hist, offs, (int64_t)kBins * ntiles, nullptr, s));
     k_radix_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, offs);

@@ -8,9 +8,10 @@ namespace spws {
 int scan_i32_to_i64(const int32_t* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s);
 int scan_i64(const long long* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s);
 
-// Stable sort of n (key, payload) pairs by the low `key_bits` bits of key.
-// Ping-pongs between (keys, vals) and (keys_tmp, vals_tmp); *result_in_tmp
-// tells which pair holds the sorted output.
+// Stable sort of n (key, payload) pairs by bits [begin_bit, key_bits) of key
+// (bits above key_bits must be zero). Ping-pongs between (keys, vals) and
+// (keys_tmp, vals_tmp); *result_in_tmp tells which pair holds the output.
 int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigned long long* keys_tmp,
-                     unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s);
+                     unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s,
+                     int begin_bit = 0);
 }  // namespace spws

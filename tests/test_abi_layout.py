@@ -17,6 +17,7 @@ def mirrors():
     return {
         "spws_csr_dev": sp.CsrDev,
         "spws_spgemm_stats": sp.SpgemmStats,
+        "spws_spgemm_t_stats": sp.SpgemmTStats,
         "spws_batch_stats": sp.BatchStats,
         "spws_tuning": sp.Tuning,
         "taco_tensor_t": taco.TacoTensor,

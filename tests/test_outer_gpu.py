@@ -101,6 +101,71 @@ def test_transposed_against_oracle(spws_lib):
     assert np.array_equal(tp, got[0]) and np.array_equal(tc, got[1])
 
 
+def test_transposed_nofuse_golden(spws_lib):
+    """The non-fused form against the reference's own outputs
+    (evaluate/CSC_CSR_T_hash_record_nofuse.h): C_noT = A*B and C = C_noT^T."""
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, "spgemm_t_nofuse_er100.npz"))
+    A, B = csr(z, "A"), csr(z, "B")
+    noT, got, coll = sp.spgemm_t(A, B, fuse=False)
+    sN = oracle.spgemm("taco", abs_csr(A), abs_csr(B))[2]
+    sT = oracle.spgemm_t(abs_csr(A), abs_csr(B), w_cap=1 << 22)[0][2]
+    assert_csr_close(noT, (z["n_noT_pos"], z["n_noT_crd"], z["n_noT_vals"]), sN, "C_noT")
+    assert_csr_close(got, (z["n_pos"], z["n_crd"], z["n_vals"]), sT, "C")
+    fused, fcoll = sp.spgemm_t(A, B)
+    assert_csr_equal_structure(got, fused, "fused vs non-fused")
+    assert coll == fcoll
+
+
+@pytest.mark.parametrize("shape", ["rmat", "rect", "empty", "one"])
+def test_transposed_fused_and_nofuse_against_oracle(spws_lib, shape):
+    import sparsews_gb300 as sp
+    if shape == "rmat":
+        A, B = gen.rmat(11, 6, seed=68), gen.rmat(11, 7, seed=69)
+    elif shape == "rect":
+        rng = np.random.default_rng(70)
+
+        def rect(n, m, d):
+            mask = rng.random((n, m)) < d
+            mask[3] = False
+            r, c = np.nonzero(mask)
+            pos = np.zeros(n + 1, np.int32)
+            np.add.at(pos, r + 1, 1)
+            return np.cumsum(pos).astype(np.int32), c.astype(np.int32), rng.uniform(-1, 1, len(r)), n, m
+        A, B = rect(40, 70, 0.08), rect(70, 55, 0.1)
+    elif shape == "empty":
+        A = (np.zeros(31, np.int32), np.zeros(0, np.int32), np.zeros(0), 30, 20)
+        B = gen.er(20, 3, seed=71)[:3] + (20, 20)
+    else:
+        A = (np.array([0, 1], np.int32), np.array([0], np.int32), np.array([-0.75]), 1, 1)
+        B = (np.array([0, 1], np.int32), np.array([0], np.int32), np.array([2.5]), 1, 1)
+    (rn, rt, rcoll) = oracle.spgemm_t_nofuse(A, B, w_cap=1 << 22)
+    sN = oracle.spgemm("taco", abs_csr(A), abs_csr(B))[2]
+    sT = oracle.spgemm_t(abs_csr(A), abs_csr(B), w_cap=1 << 22)[0][2]
+    noT, got, coll = sp.spgemm_t(A, B, fuse=False)
+    assert_csr_close(noT, rn, sN, "C_noT")
+    assert_csr_close(got, rt, sT, "C")
+    fused, fcoll = sp.spgemm_t(A, B)
+    assert_csr_close(fused, rt, sT, "fused")
+    assert coll == fcoll == rcoll
+    # the device form: both ways give the host entry points' results, the
+    # non-fused transpose is exactly the transpose of its C_noT
+    tp, tc, tv = sp._csr_transpose_np(*A)
+    At = sp.DeviceCsr.upload(tp, tc, tv, A[4], A[3])
+    Bd = sp.DeviceCsr.upload(*B)
+    Cf, _, stf = sp.spgemm_t_device(At, Bd, fuse=True)
+    Cn, Nn, stn = sp.spgemm_t_device(At, Bd, fuse=False, keep_noT=True)
+    assert stf.products == stn.products and stf.nnz == stn.nnz == len(got[1])
+    hf, hn, hN = Cf.download(), Cn.download(), Nn.download()
+    assert_csr_equal_structure(hf, fused, "device fused")
+    assert_csr_close(hn, got, sT, "device non-fused")  # heavy rows sum with atomics: order varies per call
+    assert_csr_equal_structure(hN, noT, "device C_noT")
+    ep, ec, ev = sp._csr_transpose_np(hN[0], hN[1], hN[2], A[3], B[4])
+    assert np.array_equal(ep, hn[0]) and np.array_equal(ec, hn[1]) and np.array_equal(ev, hn[2])
+    for d in (Cf, Cn, Nn, At, Bd):
+        d.release()
+
+
 def test_outer_rejects_malformed(spws_lib):
     import sparsews_gb300 as sp
     from sparsews_gb300 import taco
