@@ -547,6 +547,21 @@ def bench_transpose(args):
     build.build()
     L = sp.lib()
     sp.check(L.spws_set_device(0))
+    bw, peak_src = measured_peaks()
+    # Both entry points return malloc'd host outputs (the non-fused one two of
+    # them). glibc serves large blocks with fresh mmap pages (page faults on
+    # the first copy into them) and moves that threshold as blocks are freed,
+    # which made single mid-size calls 5-20x slower at random. A fixed
+    # threshold (32 MiB, glibc's largest on 64-bit) and a 1 GiB trim threshold
+    # keep freed heap pages for reuse, the same for both forms; blocks above
+    # 32 MiB still come from mmap in both.
+    allocator = "glibc default"
+    try:
+        libc = C.CDLL(None)
+        if libc.mallopt(C.c_int(-3), C.c_int(32 << 20)) and libc.mallopt(C.c_int(-1), C.c_int(1 << 30)):
+            allocator = "glibc, mmap threshold fixed at 32 MiB, trim threshold 1 GiB"
+    except (OSError, AttributeError):
+        pass
     ora = None
     if not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -579,7 +594,7 @@ def bench_transpose(args):
             Bh = taco.csr(*A)
             e2e = {True: [], False: []}
             coll = C.c_int32(0)
-            for it in range(1 + args.e2e_steps):
+            for it in range(1 + max(args.e2e_steps, 5)):
                 for fuse in (True, False):
                     Ct = taco.init_dc(m, n)
                     if fuse:
@@ -600,6 +615,13 @@ def bench_transpose(args):
                        e2e={"fused_ms": statistics.median(e2e[True]), "nofuse_ms": statistics.median(e2e[False])})
             for k in ("device", "e2e"):
                 row[k]["speedup"] = row[k]["nofuse_ms"] / row[k]["fused_ms"]
+            # the non-fused form with its output transpose at the HBM copy
+            # rate (read and write 12 B per entry): the smallest speedup any
+            # transpose kernel could leave to fusion on this product
+            ideal_out = 24.0 * nnz / (bw * 1e9) * 1e3
+            nf = split[False]
+            row["device"]["speedup_vs_ideal_transpose"] = (nf[0] + nf[1] + ideal_out) / row["device"]["fused_ms"]
+            row["device"]["output_transpose_gbs"] = 24.0 * nnz / (nf[2] * 1e-3) / 1e9 if nf[2] > 0 else None
             if ora is not None and products <= args.transpose_cpu_products:
                 lib, pre, fr = ora
                 wc = 1 << max(0, int(np.floor(np.log2(max(len(A[1]), 1)))))
@@ -640,11 +662,13 @@ def bench_transpose(args):
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": "transposed_output_AxA_fused_vs_nofuse", "matrices": len(rows),
-                       "l2": "flushed between device-timed calls"},
+                       "l2": "flushed between device-timed calls", "host_allocator": allocator},
             "e2e": {"what": "CSC_CSR_T_hash_nonfuse / CSC_CSR_T_hash wall time, host arrays", **e2e_all,
                     "by_output_nnz": bins("nnz_C", nnz_edges, "e2e"),
                     "by_collision_ratio": bins("collision_ratio", coll_edges, "e2e")},
             "device": {"what": "spws_spgemm_t_device fuse=0 / fuse=1, CUDA-event time", **dev_all,
+                       "vs_ideal_transpose": gstats([r["device"]["speedup_vs_ideal_transpose"] for r in rows]),
+                       "hbm_peak_gbs": bw, "hbm_peak_source": peak_src,
                        "by_output_nnz": bins("nnz_C", nnz_edges, "device"),
                        "by_collision_ratio": bins("collision_ratio", coll_edges, "device")},
             "cpu_port": {"what": "the oracle's restatement of both reference functions, one core",

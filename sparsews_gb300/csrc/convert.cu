@@ -68,13 +68,29 @@ __global__ void k_cc_transposed_keys(int32_t nq, const int32_t* __restrict__ oc,
 }
 
 // keys[p] = (col(p) << row_bits) | row(p) for a CSR (its transpose order).
-__global__ void k_csr_transposed_keys(int32_t nrows, const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
-                                      const double* __restrict__ vals, int row_bits,
+// Work is split by entries, not rows, so one long row does not hold a warp
+// for the whole launch: warp w covers entries [256w, 256w + 256), lane l the
+// entries 256w + l + 32k (coalesced), finding its first row by one binary
+// search over pos (the last row starting at or before the entry) and later
+// rows by stepping forward.
+constexpr int kKeysPerLane = 8;
+__global__ void k_csr_transposed_keys(int32_t nrows, int64_t nnz, const int32_t* __restrict__ pos,
+                                      const int32_t* __restrict__ crd, const double* __restrict__ vals, int row_bits,
                                       unsigned long long* __restrict__ keys, unsigned long long* __restrict__ pay) {
   const int lane = threadIdx.x & 31;
-  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= nrows) return;
-  for (int32_t p = pos[i] + lane; p < pos[i + 1]; p += 32) {
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t p = w * (32 * kKeysPerLane) + lane;
+  if (p >= nnz) return;
+  int32_t lo = 0, hi = nrows - 1;
+  while (lo < hi) {
+    const int32_t mid = lo + ((hi - lo + 1) >> 1);
+    if ((int64_t)pos[mid] <= p) lo = mid;
+    else hi = mid - 1;
+  }
+  int32_t i = lo;
+  int64_t end = pos[i + 1];
+  for (int k = 0; k < kKeysPerLane && p < nnz; k++, p += 32) {
+    while (p >= end) end = pos[++i + 1];
     keys[p] = ((unsigned long long)crd[p] << row_bits) | (unsigned long long)i;
     pay[p] = __double_as_longlong(vals[p]);
   }
@@ -227,9 +243,10 @@ int csr_transpose(const CsrView& m, spws_csr_dev* out, cudaStream_t s) {
   SPWS_TRY(dalloc((void**)&kt, b, s));
   SPWS_TRY(dalloc((void**)&pt, b, s));
   const int row_bits = bits_for((unsigned long long)m.nrows);
-  if (m.nrows > 0) {
-    k_csr_transposed_keys<<<(unsigned)((m.nrows + 7) / 8), 256, 0, s>>>(m.nrows, m.pos, m.crd, m.vals, row_bits, k,
-                                                                          p);
+  if (nnz > 0) {
+    const int64_t warps = (nnz + 32 * kKeysPerLane - 1) / (32 * kKeysPerLane);
+    k_csr_transposed_keys<<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(m.nrows, nnz, m.pos, m.crd, m.vals, row_bits,
+                                                                        k, p);
     count_launch(1);
   }
   int rc = keys_to_csr(nnz, k, p, kt, pt, row_bits, bits_for((unsigned long long)m.ncols), m.ncols, out, s);

@@ -10,6 +10,8 @@
 // their input order; passes are therefore stable and the sort is stable.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "sort.h"
 #include "spws_internal.h"
 
@@ -24,47 +26,89 @@ constexpr int kRounds = 16;
 constexpr int kTile = kSortThreads * kRounds;  // 4096
 static_assert(kBins == kSortThreads, "one bin per thread");
 
+// Both kernels load a thread's kRounds items of the tile up front (all loads
+// in flight at once) before any shared-memory work, so a CTA waits for DRAM
+// once per tile rather than once per round.
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long* __restrict__ keys, int64_t n,
                                                              int shift, int64_t ntiles, int* __restrict__ hist) {
   __shared__ int h[kBins];
   h[threadIdx.x] = 0;
-  __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * kTile;
-#pragma unroll 4
+  const int64_t base = (int64_t)blockIdx.x * kTile + threadIdx.x;
+  int d[kRounds];
+#pragma unroll
   for (int r = 0; r < kRounds; r++) {
-    const int64_t idx = base + (int64_t)r * kSortThreads + threadIdx.x;
-    if (idx < n) atomicAdd(&h[(int)((keys[idx] >> shift) & (kBins - 1))], 1);
+    const int64_t idx = base + (int64_t)r * kSortThreads;
+    d[r] = idx < n ? (int)((keys[idx] >> shift) & (kBins - 1)) : -1;
   }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kRounds; r++)
+    if (d[r] >= 0) atomicAdd(&h[d[r]], 1);
   __syncthreads();
   hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
+
+// Scatter of one tile: items are ranked round by round (a warp multisplit:
+// lanes holding the same digit found with one ballot per digit bit, then a
+// prefix over the warps), placed digit-sorted into shared memory at
+// tile-local positions (the tile's own digit histogram, scanned, gives each
+// digit's start), and written out from there in slot order, so consecutive
+// threads store consecutive addresses of the same digit's run instead of one
+// scattered 8-byte store per item. Ranks follow input order within a digit:
+// the pass is stable.
+constexpr size_t kScatterSmem = 2 * sizeof(unsigned long long) * kTile;
 
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long* __restrict__ kin,
                                                                 const unsigned long long* __restrict__ vin,
                                                                 unsigned long long* __restrict__ kout,
                                                                 unsigned long long* __restrict__ vout, int64_t n,
                                                                 int shift, int64_t ntiles,
-                                                                const long long* __restrict__ offs) {
+                                                                const long long* __restrict__ offs,
+                                                                const int* __restrict__ hist) {
+  extern __shared__ unsigned long long stage[];  // keys [kTile], then payloads [kTile]
   __shared__ long long base[kBins];
+  __shared__ int lstart[kBins];
+  __shared__ int run[kBins];
   __shared__ int wcnt[kSortWarps][kBins];
-  __shared__ int rcnt[kBins];
+  __shared__ int wsum[kSortWarps];
+  unsigned long long* sk = stage;
+  unsigned long long* sv = stage + kTile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t tile0 = (int64_t)blockIdx.x * kTile;
+  unsigned long long kr[kRounds], vr[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    const int64_t idx = tile0 + (int64_t)r * kSortThreads + threadIdx.x;
+    kr[r] = idx < n ? kin[idx] : 0ull;
+    vr[r] = idx < n ? vin[idx] : 0ull;
+  }
   base[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+  {  // tile-local digit starts: exclusive scan of this tile's histogram
+    const int c = hist[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+    int v = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[warp] = v;
+    __syncthreads();
+    int before = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++)
+      if (w < warp) before += wsum[w];
+    lstart[threadIdx.x] = before + v - c;
+    run[threadIdx.x] = 0;
+  }
 #pragma unroll
   for (int w = 0; w < kSortWarps; w++) wcnt[w][threadIdx.x] = 0;
   __syncthreads();
   const unsigned lt = (1u << lane) - 1u;
-  const int64_t tile0 = (int64_t)blockIdx.x * kTile;
+#pragma unroll
   for (int r = 0; r < kRounds; r++) {
     const int64_t idx = tile0 + (int64_t)r * kSortThreads + threadIdx.x;
     const bool valid = idx < n;
-    unsigned long long k = 0, v = 0;
-    int d = 0;
-    if (valid) {
-      k = kin[idx];
-      v = vin[idx];
-      d = (int)((k >> shift) & (kBins - 1));
-    }
+    const int d = (int)((kr[r] >> shift) & (kBins - 1));
     // lanes of this warp holding the same digit
     unsigned eq = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
@@ -76,27 +120,36 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned l
     const int rank = __popc(eq & lt);
     if (valid && rank == 0) wcnt[warp][d] = __popc(eq);
     __syncthreads();
+    int rtotal;
     {  // thread t owns digit t: prefix over warps
-      int run = 0;
+      int acc = 0;
 #pragma unroll
       for (int w = 0; w < kSortWarps; w++) {
         const int c = wcnt[w][threadIdx.x];
-        wcnt[w][threadIdx.x] = run;
-        run += c;
+        wcnt[w][threadIdx.x] = acc;
+        acc += c;
       }
-      rcnt[threadIdx.x] = run;
+      rtotal = acc;
     }
     __syncthreads();
     if (valid) {
-      const long long p = base[d] + wcnt[warp][d] + rank;
-      kout[p] = k;
-      vout[p] = v;
+      const int slot = lstart[d] + run[d] + wcnt[warp][d] + rank;
+      sk[slot] = kr[r];
+      sv[slot] = vr[r];
     }
     __syncthreads();
-    base[threadIdx.x] += rcnt[threadIdx.x];
+    run[threadIdx.x] += rtotal;
 #pragma unroll
     for (int w = 0; w < kSortWarps; w++) wcnt[w][threadIdx.x] = 0;
     __syncthreads();
+  }
+  const int count = (int)(n - tile0 < kTile ? n - tile0 : kTile);
+  for (int j = threadIdx.x; j < count; j += kSortThreads) {
+    const unsigned long long k = sk[j];
+    const int d = (int)((k >> shift) & (kBins - 1));
+    const long long p = base[d] + (j - lstart[d]);
+    kout[p] = k;
+    vout[p] = sv[j];
   }
 }
 
@@ -212,6 +265,18 @@ int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigne
                      int begin_bit) {
   *result_in_tmp = false;
   if (n <= 1 || key_bits <= begin_bit) return SPWS_OK;
+  {  // the scatter's staging exceeds the default 48 KB: opt in once per device
+    static std::mutex mu;
+    static bool smem_set[64] = {};
+    int dev = 0;
+    SPWS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    if (dev >= 0 && dev < 64 && !smem_set[dev]) {
+      SPWS_CUDA(cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kScatterSmem));
+      smem_set[dev] = true;
+    }
+  }
   const int64_t ntiles = (n + kTile - 1) / kTile;
   int* hist = nullptr;
   long long* offs = nullptr;
@@ -221,7 +286,8 @@ int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigne
   for (int shift = begin_bit; shift < key_bits; shift += kRadixBits) {
     k_radix_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, hist);
     SPWS_TRY(scan_i32_to_i64(hist, offs, (int64_t)kBins * ntiles, nullptr, s));
-    k_radix_scatter<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, offs);
+    k_radix_scatter<<<(unsigned)ntiles, kSortThreads, kScatterSmem, s>>>(ka, va, kb, vb, n, shift, ntiles, offs,
+                                                                           hist);
     count_launch(2);
     SPWS_CUDA(cudaGetLastError());
     std::swap(ka, kb);

@@ -5,6 +5,7 @@ not exercise, for profiling one kernel family at a time under ncu:
     python -m sparsews_gb300.profile_cases mttkrp    # tensor bucket kernel, mode 0
     python -m sparsews_gb300.profile_cases ttm       # tensor bucket kernel, mode 1
     python -m sparsews_gb300.profile_cases outer     # DCSC x DCSR conversion + row-wise pipeline
+    python -m sparsews_gb300.profile_cases transpose # (A*A)^T fused and non-fused (device transposes)
 
 Each case runs its call `--repeat` times (default 2: one warm-up, one to
 capture) on inputs larger than the L2 cache and prints one line of sizes.
@@ -17,7 +18,8 @@ import numpy as np
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["coord", "mttkrp", "ttm", "outer"])
+    ap.add_argument("case", choices=["coord", "mttkrp", "ttm", "outer", "transpose"])
+    ap.add_argument("--scale", type=int, default=15, help="transpose case: R-MAT scale")
     ap.add_argument("--repeat", type=int, default=2)
     args = ap.parse_args()
     import sparsews_gb300 as sp
@@ -30,6 +32,18 @@ def main():
         for _ in range(args.repeat):
             C = sp.spgemm(A, A, "coord") if args.case == "coord" else sp.spgemm_outer(A, A, "hash")
         print(f"{args.case}: band 2^20, nnz(A) {len(A[1])}, nnz(C) {len(C[1])}, {time.perf_counter() - t0:.1f} s")
+        return
+    if args.case == "transpose":
+        A = gen.rmat(args.scale, 8, seed=42)
+        tp, tc, tv = sp._csr_transpose_np(*A)
+        At = sp.DeviceCsr.upload(tp, tc, tv, A[4], A[3])
+        Bd = sp.DeviceCsr.upload(*A)
+        for _ in range(args.repeat):
+            for fuse in (True, False):
+                Cd, _, st = sp.spgemm_t_device(At, Bd, fuse=fuse)
+                Cd.release()
+                print(f"transpose fuse={fuse}: in {st.ms_input_transpose:.3f} spgemm {st.ms_spgemm:.3f} "
+                      f"out {st.ms_output_transpose:.3f} total {st.ms_total:.3f} ms, nnz {st.nnz}")
         return
     i0, i1, i2, tv = gen.tensor3((50000, 40000, 20000), 2_000_000, zipf_s=1.1, seed=42)
     if args.case == "mttkrp":
