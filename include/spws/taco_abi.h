@@ -159,6 +159,31 @@ double DCSC_DCSR_taco(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int3
                       bool print);
 
 /* ------------------------------------------------------------------------ */
+/* Transposed-output outer product C = (A*B)^T: A in DCSC, B in DCSR, C in     */
+/* CSR over k. benchmark/DCSC_DCSR_T/. The reference names every wrapper there */
+/* `CSC_CSR_T_hash` / `CSC_CSR_T_coord`, clashing with the CSC x CSR one below  */
+/* (another signature); C has one namespace, so these are DCSC_DCSR_T_*.      */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces `int compute(C, A, B, w_cap)` of DCSC_DCSR_T_hash.h:232. */
+int spws_dcsc_dcsr_t_hash_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap);
+/* Replaces `int compute(C, A, B, w_cap)` of DCSC_DCSR_T_coord_bucket.h:279. */
+int spws_dcsc_dcsr_t_bucket_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap);
+/* Replaces `int compute(C, A, B)` of DCSC_DCSR_T_coord_index_chase_flex.h:191
+ * (coordinate workspace: sums in j order, bit-exact with the hash form when
+ * its buffer never refreshes). */
+int spws_dcsc_dcsr_t_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap);
+/* Replace `double CSC_CSR_T_hash(A, B, C, w_cap, warmup, repeat, bench=false,
+ * print=false)` of DCSC_DCSR_T_hash.h:361 and DCSC_DCSR_T_coord_bucket.h:404. */
+double DCSC_DCSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                        int32_t repeat, bool bench, bool print);
+double DCSC_DCSR_T_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                          int32_t repeat, bool bench, bool print);
+/* Replaces `void CSC_CSR_T_coord(A, B, C, w_cap, print=false)` of
+ * DCSC_DCSR_T_coord_index_chase_flex.h:381. */
+void DCSC_DCSR_T_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print);
+
+/* ------------------------------------------------------------------------ */
 /* Transposed-output SpGEMM C = (A*B)^T: A in CSC (dense outer level over j),  */
 /* B in CSR, C in CSR over k. evaluate/CSC_CSR_T_hash_record.h                 */
 /* ------------------------------------------------------------------------ */

@@ -60,7 +60,7 @@ def _load(kind):
         raise ValueError(kind)
     P = C.POINTER(taco.TacoTensor)
     names = [("csr_csr_hash", 3), ("dcsc_dcsr_hash", 3), ("dcsc_dcsr_coord", 3), ("dcsc_dcsr_bucket", 3),
-             ("ttm_hash", 3), ("ttm_bucket", 3)]
+             ("dcsc_dcsr_t_hash", 3), ("ttm_hash", 3), ("ttm_bucket", 3)]
     if kind == "port":
         names.append(("dcsc_dcsr_coord_faithful", 3))
     for name, nt in names:
@@ -151,6 +151,26 @@ def spgemm_t(A, B, w_cap=None, kind="port"):
     if rc != 0:
         raise RuntimeError(f"oracle t_hash failed rc={rc}")
     return taco.take_csr(Cout, bm, fr), int(coll.value)
+
+
+def spgemm_outer_t(A, B, w_cap=None, kind="port"):
+    """C = (A*B)^T with A passed as DCSC and B as DCSR, the (k, i)-keyed hash
+    of benchmark/DCSC_DCSR_T/DCSC_DCSR_T_hash.h. A and B are CSR triples.
+    Returns the CSR of C^T (rows = columns of B)."""
+    lib, pre, fr = _load(kind)
+    ap, ac, av, an, am = A
+    bp, bc, bv, bn, bm = B
+    if w_cap is None:
+        w_cap = w_cap_default(len(ac))
+    from sparsews_gb300.gen import csr_transpose
+    tp, tc, tv = csr_transpose(ap, ac, av, an, am)
+    At = taco.dcsc(tp, tc, tv, an, am)
+    Bt = taco.dcsr(bp, bc, bv, bn, bm)
+    Cout = taco.init_dc(bm, an)
+    rc = getattr(lib, pre + "dcsc_dcsr_t_hash")(Cout.ptr(), At.ptr(), Bt.ptr(), w_cap)
+    if rc != 0:
+        raise RuntimeError(f"oracle dcsc_dcsr_t_hash failed rc={rc}")
+    return taco.take_csr(Cout, bm, fr)
 
 
 def spgemm_t_nofuse(A, B, w_cap=None, kind="port"):

@@ -28,6 +28,9 @@ namespace ref_outer_bucket {
 namespace ref_t_hash {
 #include "evaluate/CSC_CSR_T_hash_record.h"
 }
+namespace ref_dcsc_t_hash {
+#include "benchmark/DCSC_DCSR_T/DCSC_DCSR_T_hash.h"
+}
 namespace ref_t_nofuse {
 #include "evaluate/CSC_CSR_T_hash_record_nofuse.h"
 }
@@ -72,6 +75,10 @@ int ref_csc_csr_t_hash(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int
   ref_t_hash::CSC_CSR_T_hash(A, B, C, w_cap, c);
   *collisions = c;
   return 0;
+}
+/* benchmark/DCSC_DCSR_T/DCSC_DCSR_T_hash.h:232 */
+int ref_dcsc_dcsr_t_hash(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  return ref_dcsc_t_hash::compute(C, A, B, w_cap);
 }
 /* evaluate/CSC_CSR_T_hash_record_nofuse.h:405 (compute_nofuse, then transpose);
    the collision counter is cleared per call as above. */

@@ -444,6 +444,22 @@ int ora_dcsc_dcsr_hash(taco_tensor_t* C, const taco_tensor_t* A, const taco_tens
   return rc;
 }
 
+static int visit_t_hash(void* ctx, int32_t i, int32_t k, double v) {
+  int32_t key[2] = {k, i};
+  return hws_insert((hws_t*)ctx, key, v);
+}
+
+/* Transposed output C = (A*B)^T, key (k, i), same co-iteration:
+   benchmark/DCSC_DCSR_T/DCSC_DCSR_T_hash.h:232-359 (:285,288 swap the key) */
+int ora_dcsc_dcsr_t_hash(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap) {
+  hws_t w;
+  if (hws_init(&w, 2, w_cap, 0)) return SPWS_ORA_NOMEM;
+  if (outer_coiterate(A, B, visit_t_hash, &w) || hws_flush(&w)) { hws_free(&w); return SPWS_ORA_NOMEM; }
+  int rc = coo2_to_csr(C, &w.all, C->dimensions[0]);
+  hws_free(&w);
+  return rc;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Coordinate workspace: append triples, and when the buffer is full sort   */
 /* an index array by key, then reduce and merge into a ping-pong all-array. */

@@ -19,6 +19,7 @@ int ora_dcsc_dcsr_hash(taco_tensor_t* C, const taco_tensor_t* A, const taco_tens
 int ora_dcsc_dcsr_coord(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap);
 /* Reproduces the reference's first-flush behaviour; pinning tests only. */
 int ora_dcsc_dcsr_coord_faithful(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap);
+int ora_dcsc_dcsr_t_hash(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap);
 int ora_dcsc_dcsr_bucket(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap);
 int ora_csc_csr_t_hash(taco_tensor_t* C, const taco_tensor_t* A, const taco_tensor_t* B, int32_t w_cap,
                        int32_t* collisions);

@@ -90,6 +90,12 @@ def lib():
         "DCSC_DCSR_bucket": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
         "DCSC_DCSR_coord": ([P, P, P, C.c_int32, C.c_bool], None),
         "CSC_CSR_T_hash": ([P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_double),
+        "spws_dcsc_dcsr_t_hash_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_dcsc_dcsr_t_bucket_compute": ([P, P, P, C.c_int32], C.c_int),
+        "spws_dcsc_dcsr_t_coord_compute": ([P, P, P, C.c_int32], C.c_int),
+        "DCSC_DCSR_T_hash": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "DCSC_DCSR_T_bucket": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
+        "DCSC_DCSR_T_coord": ([P, P, P, C.c_int32, C.c_bool], None),
         "spws_csc_csr_t_hash_nofuse_compute": ([P, P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
         "CSC_CSR_T_hash_nonfuse": ([P, P, P, P, C.c_int32, C.POINTER(C.c_int32)], C.c_double),
         "spws_coo_csf_dcsr_dcsr_hash_compute": ([P, P, P, P, C.c_int32], C.c_int),
@@ -192,6 +198,22 @@ def spgemm_outer(A, B, method="hash"):
               "coord": L.spws_dcsc_dcsr_coord_compute}[method]
         check(fn(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
     return taco.take_csr(Ct, an, L.spws_free)
+
+
+def spgemm_outer_t(A, B, method="hash"):
+    """C^T = (A*B)^T with A passed as DCSC and B as DCSR (the DCSC_DCSR_T
+    entry points). method: 'hash', 'bucket' or 'coord'. Returns the CSR of C^T."""
+    L = lib()
+    ap, ac, av, an, am = A
+    bp, bc, bv, bn, bm = B
+    tp, tc, tv = _csr_transpose_np(ap, ac, av, an, am)
+    At = taco.dcsc(tp, tc, tv, an, am)
+    Bt = taco.dcsr(bp, bc, bv, bn, bm)
+    Ct = taco.init_dc(bm, an)
+    fn = {"hash": L.spws_dcsc_dcsr_t_hash_compute, "bucket": L.spws_dcsc_dcsr_t_bucket_compute,
+          "coord": L.spws_dcsc_dcsr_t_coord_compute}[method]
+    check(fn(Ct.ptr(), At.ptr(), Bt.ptr(), 0))
+    return taco.take_csr(Ct, bm, L.spws_free)
 
 
 def spgemm_t(A, B, fuse=True):

@@ -61,8 +61,11 @@ int up(const T* h, size_t n, DevBuf* b, cudaStream_t s) {
 }
 
 // Uploads a CC matrix, validates it on the device and converts it to CSR.
-// outer_mode 1 = DCSC (outer level over columns), 0 = DCSR.
-int cc_to_dev_csr(const taco_tensor_t* t, const char* what, int outer_mode, DevCsr* out, cudaStream_t s) {
+// outer_mode 1 = DCSC (outer level over columns), 0 = DCSR. With transposed
+// set, a DCSC's arrays are read as the DCSR of its transpose (no sort), so
+// the result is the CSR of the transpose.
+int cc_to_dev_csr(const taco_tensor_t* t, const char* what, int outer_mode, DevCsr* out, cudaStream_t s,
+                  bool transposed = false) {
   int32_t nq;
   int64_t nnz;
   SPWS_TRY(check_cc(t, what, outer_mode, &nq, &nnz));
@@ -81,6 +84,9 @@ int cc_to_dev_csr(const taco_tensor_t* t, const char* what, int outer_mode, DevC
   SPWS_TRY(validate_cc_device((int32_t*)oc.p, (int32_t*)pos.p, (int32_t*)ic.p, nq, outer_dim, inner_dim, nnz, what,
                               s));
   out->s = s;
+  if (outer_mode == 1 && transposed)
+    return dcsr_to_csr((int32_t*)oc.p, (int32_t*)pos.p, (int32_t*)ic.p, (double*)vals.p, nq, ncols, nrows, nnz,
+                       &out->m, s);
   if (outer_mode == 1)
     return dcsc_to_csr((int32_t*)oc.p, (int32_t*)pos.p, (int32_t*)ic.p, (double*)vals.p, nq, nrows, ncols, nnz,
                        &out->m, s);
@@ -120,6 +126,28 @@ int dcsc_dcsr(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, Engine eng) 
     return SPWS_ERR_INVALID;
   }
   return run_into(C, view(dA.m), view(dB.m), eng, nullptr, s);
+}
+
+// Transposed output C = (A*B)^T with A in DCSC and B in DCSR
+// (benchmark/DCSC_DCSR_T: the key (k, i) at DCSC_DCSR_T_hash.h:285,288):
+// A's DCSC arrays are the DCSR of A^T, B^T comes from B's CSR by a device
+// transpose, and C's rows k are B^T * A^T row by row.
+int dcsc_dcsr_t(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, Engine eng) {
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  SPWS_TRY(check_out_dc(C, "C"));
+  cudaStream_t s = ds->stream;
+  DevCsr dAt, dB, dBt;
+  SPWS_TRY(cc_to_dev_csr(A, "A", 1, &dAt, s, true));
+  SPWS_TRY(cc_to_dev_csr(B, "B", 0, &dB, s));
+  if (dAt.m.nrows != dB.m.nrows || C->dimensions[0] != dB.m.ncols) {
+    set_error("shape mismatch: A is n x m, B must be m x k and C k x n");
+    return SPWS_ERR_INVALID;
+  }
+  dBt.s = s;
+  SPWS_TRY(csr_transpose(view(dB.m), &dBt.m, s));
+  return run_into(C, view(dBt.m), view(dAt.m), eng, nullptr, s);
 }
 
 struct Event {
@@ -278,6 +306,40 @@ double DCSC_DCSR_taco(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int3
   (void)print;
   return timed(warmup, repeat, bench, [&] { return spws_dcsc_dcsr_taco_compute(C, A, B); },
                [&] { free_csr_out(C); });
+}
+
+int spws_dcsc_dcsr_t_hash_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  (void)w_cap;
+  return dcsc_dcsr_t(C, A, B, Engine::Rowwise);
+}
+
+int spws_dcsc_dcsr_t_bucket_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  (void)w_cap;
+  return dcsc_dcsr_t(C, A, B, Engine::Rowwise);
+}
+
+int spws_dcsc_dcsr_t_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {
+  (void)w_cap;
+  return dcsc_dcsr_t(C, A, B, Engine::Coord);
+}
+
+double DCSC_DCSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                        int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_dcsc_dcsr_t_hash_compute(C, A, B, w_cap); },
+               [&] { free_csr_out(C); });
+}
+
+double DCSC_DCSR_T_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                          int32_t repeat, bool bench, bool print) {
+  (void)print;
+  return timed(warmup, repeat, bench, [&] { return spws_dcsc_dcsr_t_bucket_compute(C, A, B, w_cap); },
+               [&] { free_csr_out(C); });
+}
+
+void DCSC_DCSR_T_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print) {
+  (void)print;
+  spws_dcsc_dcsr_t_coord_compute(C, A, B, w_cap);
 }
 
 int spws_csr_csr_coord_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B, int32_t w_cap) {

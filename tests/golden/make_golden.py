@@ -107,6 +107,13 @@ def main():
                      tag + "_crd": tc, tag + "_vals": tv, tag + "_collisions": np.array(coll)})
     save("spgemm_t_nofuse_er100", **pack("A", A), **pack("B", B), **outs,
          meta=np.array("C_noT=A*B then C=C_noT^T, same A/B as spgemm_t_er100; n16 = w_cap 16"))
+    # the DCSC x DCSR form with the same (k, i) key (benchmark/DCSC_DCSR_T/DCSC_DCSR_T_hash.h)
+    outs = {}
+    for tag, wc in (("d", None), ("d16", 16)):
+        p, c, v = oracle.spgemm_outer_t(A, B, w_cap=wc, kind="ref")
+        outs.update({tag + "_pos": p, tag + "_crd": c, tag + "_vals": v})
+    save("spgemm_t_outer_er100", **pack("A", A), **pack("B", B), **outs,
+         meta=np.array("C=(A*B)^T, A as DCSC, B as DCSR, same A/B as spgemm_t_er100; d16 = w_cap 16"))
 
     # MTTKRP: CSF levels (k, l, i) with i the output row; factors dense rank R
     i0, i1, i2, tv = gen.tensor3((90, 60, 40), 2500, zipf_s=1.1, seed=17)

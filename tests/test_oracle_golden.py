@@ -73,6 +73,18 @@ def test_port_matches_reference_golden_transposed_nofuse():
         np.testing.assert_allclose(tv, zf["t_vals"], rtol=1e-13, atol=1e-15)
 
 
+def test_port_matches_reference_golden_outer_transposed():
+    z = load("spgemm_t_outer_er100")
+    zf = load("spgemm_t_er100")
+    A, B = csr(z, "A"), csr(z, "B")
+    for tag, wc in (("d", None), ("d16", 16)):
+        p, c, v = oracle.spgemm_outer_t(A, B, w_cap=wc, kind="port")
+        assert np.array_equal(p, z[tag + "_pos"]) and np.array_equal(c, z[tag + "_crd"])
+        assert np.array_equal(v, z[tag + "_vals"])
+    # same product as the CSC x CSR form: same structure
+    assert np.array_equal(z["d_pos"], zf["t_pos"]) and np.array_equal(z["d_crd"], zf["t_crd"])
+
+
 @pytest.mark.parametrize("R", [4, 16])
 def test_port_matches_reference_golden_mttkrp(R):
     z = load(f"mttkrp_R{R}_s17")
@@ -158,6 +170,9 @@ def test_port_matches_live_reference_transposed(wcap):
     (g, gc) = oracle.spgemm_t(A, B, w_cap=wcap, kind="port")
     (r, rc) = oracle.spgemm_t(A, B, w_cap=wcap, kind="ref")
     assert gc == rc and all(np.array_equal(a, b) for a, b in zip(g, r))
+    g = oracle.spgemm_outer_t(A, B, w_cap=wcap, kind="port")
+    r = oracle.spgemm_outer_t(A, B, w_cap=wcap, kind="ref")
+    assert all(np.array_equal(a, b) for a, b in zip(g, r))
     g = oracle.spgemm_t_nofuse(A, B, w_cap=wcap, kind="port")
     r = oracle.spgemm_t_nofuse(A, B, w_cap=wcap, kind="ref")
     assert g[2] == r[2]

@@ -101,6 +101,28 @@ def test_transposed_against_oracle(spws_lib):
     assert np.array_equal(tp, got[0]) and np.array_equal(tc, got[1])
 
 
+@pytest.mark.parametrize("method", ["hash", "bucket", "coord"])
+def test_outer_transposed_golden_and_oracle(spws_lib, method):
+    """The DCSC x DCSR transposed-output entry points (benchmark/DCSC_DCSR_T)
+    against the reference's own outputs and, on an R-MAT pair, the oracle;
+    the coordinate form sums in j order and is bit-exact."""
+    import sparsews_gb300 as sp
+    z = np.load(os.path.join(GOLD, "spgemm_t_outer_er100.npz"))
+    A, B = csr(z, "A"), csr(z, "B")
+    sT = oracle.spgemm_outer_t(abs_csr(A), abs_csr(B), w_cap=1 << 22)[2]
+    got = sp.spgemm_outer_t(A, B, method)
+    assert_csr_close(got, (z["d_pos"], z["d_crd"], z["d_vals"]), sT, method)
+    A, B = gen.rmat(11, 6, seed=72), gen.rmat(11, 5, seed=73)
+    ref = oracle.spgemm_outer_t(A, B, w_cap=1 << 22)
+    sT = oracle.spgemm_outer_t(abs_csr(A), abs_csr(B), w_cap=1 << 22)[2]
+    got = sp.spgemm_outer_t(A, B, method)
+    assert_csr_close(got, ref, sT, method)
+    if method == "coord":
+        assert np.array_equal(got[2], ref[2])
+    fused, _ = sp.spgemm_t(A, B)
+    assert_csr_equal_structure(got, fused, "DCSC x DCSR vs CSC x CSR")
+
+
 def test_transposed_nofuse_golden(spws_lib):
     """The non-fused form against the reference's own outputs
     (evaluate/CSC_CSR_T_hash_record_nofuse.h): C_noT = A*B and C = C_noT^T."""
