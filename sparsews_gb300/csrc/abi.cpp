@@ -89,15 +89,12 @@ int download_into(taco_tensor_t* C, const spws_csr_dev& r, cudaStream_t s) {
     set_error("host allocation of the output failed");
     return SPWS_ERR_NOMEM;
   }
-  cudaError_t e = cudaMemcpyAsync(pos, r.pos, sizeof(int32_t) * npos, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && nnz) e = cudaMemcpyAsync(crd, r.crd, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && nnz) e = cudaMemcpyAsync(vals, r.vals, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) {
-    (void)cudaGetLastError();
+  int rc = copy_to_host(pos, r.pos, sizeof(int32_t) * npos, s);
+  if (rc == SPWS_OK && nnz) rc = copy_to_host(crd, r.crd, sizeof(int32_t) * nnz, s);
+  if (rc == SPWS_OK && nnz) rc = copy_to_host(vals, r.vals, sizeof(double) * nnz, s);
+  if (rc != SPWS_OK) {
     free(pos); free(crd); free(vals);
-    set_error(std::string("copying the output to the host failed: ") + cudaGetErrorString(e));
-    return SPWS_ERR_CUDA;
+    return rc;
   }
   C->indices[1][0] = pos;
   C->indices[1][1] = crd;
@@ -228,12 +225,11 @@ int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double*
     }
   }
   cudaStream_t s = ds->stream;
-  SPWS_CUDA(cudaMemcpyAsync(pos, m->pos, sizeof(int32_t) * ((size_t)m->nrows + 1), cudaMemcpyDeviceToHost, s));
+  SPWS_TRY(copy_to_host(pos, m->pos, sizeof(int32_t) * ((size_t)m->nrows + 1), s));
   if (m->nnz > 0) {
-    SPWS_CUDA(cudaMemcpyAsync(crd, m->crd, sizeof(int32_t) * (size_t)m->nnz, cudaMemcpyDeviceToHost, s));
-    SPWS_CUDA(cudaMemcpyAsync(vals, m->vals, sizeof(double) * (size_t)m->nnz, cudaMemcpyDeviceToHost, s));
+    SPWS_TRY(copy_to_host(crd, m->crd, sizeof(int32_t) * (size_t)m->nnz, s));
+    SPWS_TRY(copy_to_host(vals, m->vals, sizeof(double) * (size_t)m->nnz, s));
   }
-  SPWS_CUDA(cudaStreamSynchronize(s));
   return SPWS_OK;
 }
 

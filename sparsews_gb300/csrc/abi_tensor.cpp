@@ -140,22 +140,18 @@ int download_coo(taco_tensor_t* A, CooOut& o, int order, cudaStream_t s) {
     c[d] = (int32_t*)malloc(sizeof(int32_t) * std::max<size_t>(n, 1));
     ok = ok && c[d];
   }
-  cudaError_t e = cudaSuccess;
+  int rc = SPWS_OK;
   if (ok && n) {
-    for (int d = 0; d < order && e == cudaSuccess; d++)
-      e = cudaMemcpyAsync(c[d], o.crd[d], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(v, o.vals, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (int d = 0; d < order && rc == SPWS_OK; d++) rc = copy_to_host(c[d], o.crd[d], sizeof(int32_t) * n, s);
+    if (rc == SPWS_OK) rc = copy_to_host(v, o.vals, sizeof(double) * n, s);
   }
   for (int d = 0; d < 3; d++) dfree(o.crd[d], s);
   dfree(o.vals, s);
-  if (!ok || e != cudaSuccess) {
-    (void)cudaGetLastError();
+  if (!ok || rc != SPWS_OK) {
     free(v);
     for (int d = 0; d < order; d++) free(c[d]);
-    set_error(ok ? std::string("copying the output failed: ") + cudaGetErrorString(e)
-                 : std::string("host allocation of the output failed"));
-    return ok ? SPWS_ERR_CUDA : SPWS_ERR_NOMEM;
+    if (!ok) set_error("host allocation of the output failed");
+    return ok ? rc : SPWS_ERR_NOMEM;
   }
   for (int d = 0; d < order; d++) A->indices[d + 1][0] = c[d];
   A->vals = v;
@@ -504,13 +500,13 @@ int spws_coo_download(const spws_coo_dev* A, int32_t* crd0, int32_t* crd1, int32
         set_error("coordinate array is NULL");
         return SPWS_ERR_INVALID;
       }
-      SPWS_CUDA(cudaMemcpyAsync(dst[d], A->crd[d], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ds->stream));
+      SPWS_TRY(copy_to_host(dst[d], A->crd[d], sizeof(int32_t) * n, ds->stream));
     }
     if (!vals || !A->vals) {
       set_error("vals is NULL");
       return SPWS_ERR_INVALID;
     }
-    SPWS_CUDA(cudaMemcpyAsync(vals, A->vals, sizeof(double) * n, cudaMemcpyDeviceToHost, ds->stream));
+    SPWS_TRY(copy_to_host(vals, A->vals, sizeof(double) * n, ds->stream));
   }
   SPWS_CUDA(cudaStreamSynchronize(ds->stream));
   return SPWS_OK;

@@ -55,6 +55,11 @@ void dfree(void* p, cudaStream_t s);
 // dalloc on the calling thread draws from `pool` (nullptr: the device's
 // default pool). The served form gives its workers their own pool.
 void set_thread_pool(cudaMemPool_t pool);
+// Device -> host copy into any host memory (typically pageable), ordered
+// after the work already on `s`; returns when the bytes have landed. Large
+// copies are staged through page-locked chunks and copied out by a pool of
+// host threads (host_copy.cpp).
+int copy_to_host(void* dst, const void* src, size_t bytes, cudaStream_t s);
 
 // ---- SpGEMM (row-wise, column-chunked dense workspace) ----
 struct SpgemmOpts {

@@ -158,3 +158,21 @@ def test_timing_wrapper_frees_like_reference(spws_lib):
     got = taco.take_csr(Ct, 400, L.spws_free)  # the last repeat's output is left for the caller
     ref = oracle.spgemm("taco", A, A)
     assert_csr_close(got, ref, scale_of(A, A), "wrapper")
+
+
+def test_large_output_copied_to_host(spws_lib):
+    """An output of 1.4e7 entries (115 MB of values, 58 MB of coordinates):
+    both arrays go to the host through the staged multi-chunk copy, through
+    the TACO entry point (malloc'd outputs) and spws_csr_download (caller
+    arrays); both must equal the oracle's structure and values."""
+    import sparsews_gb300 as sp
+    A = gen.er(400000, 6, seed=61)
+    got = sp.spgemm(A, A)
+    ref = oracle.spgemm("taco", A, A)
+    assert len(got[1]) > 12_000_000
+    assert_csr_close(got, ref, scale_of(A, A), "taco abi")
+    d = sp.DeviceCsr.upload(*A)
+    Cd, _ = sp.spgemm_device(d, d)
+    assert_csr_close(Cd.download(), ref, scale_of(A, A), "download")
+    Cd.release()
+    d.release()

@@ -94,6 +94,43 @@ def test_mttkrp_sparse_factors(spws_lib):
     assert_vals_close(gv, rv, scale, "mttkrp sparse")
 
 
+def sparse_factor(rows, rank, density, seed):
+    """A DCSR factor with about density * rows * rank entries, sorted, no duplicates."""
+    rng = np.random.default_rng(seed)
+    mask = rng.random((rows, rank)) < density
+    r, c = np.nonzero(mask)
+    pos = np.zeros(rows + 1, np.int64)
+    np.add.at(pos, r + 1, 1)
+    return np.cumsum(pos).astype(np.int32), c.astype(np.int32), rng.uniform(-1, 1, len(r)), rows, rank
+
+
+@pytest.mark.parametrize("perm", [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)])
+def test_tensor_mode_permutations_sparse_factors(spws_lib, perm):
+    """The reference's native setting: any CSF level order of the same tensor
+    and DCSR factors with missing entries. MTTKRP contracts the first two
+    levels against C and D (output = the leaf mode); TTM contracts the middle
+    level against C."""
+    import sparsews_gb300 as sp
+    shape = (300, 200, 120)
+    c = gen.tensor3(shape, 12000, zipf_s=1.1, seed=79)
+    coo = (c[perm[0]], c[perm[1]], c[perm[2]], c[3])
+    dims = tuple(shape[m] for m in perm)
+    R = 24
+    Cf = sparse_factor(dims[0], R, 0.6, seed=80 + perm[0])
+    Df = sparse_factor(dims[1], R, 0.5, seed=90 + perm[1])
+    (gi, gj), gv = sp.mttkrp(coo, dims, Cf, Df)
+    (ri, rj), rv = oracle.mttkrp("hash", coo, dims, Cf, Df, w_cap=BIG)
+    assert np.array_equal(gi, ri) and np.array_equal(gj, rj)
+    (_, _), scale = oracle.mttkrp("hash", coo[:3] + (np.abs(coo[3]),), dims, abs_f(Cf), abs_f(Df), w_cap=BIG)
+    assert_vals_close(gv, rv, scale, f"mttkrp {perm}")
+    Tf = sparse_factor(dims[1], R, 0.4, seed=100 + perm[1])
+    (gk, gj, gl), gv = sp.ttm(coo, dims, Tf)
+    (rk, rj, rl), rv = oracle.ttm("hash", coo, dims, Tf, w_cap=BIG)
+    assert np.array_equal(gk, rk) and np.array_equal(gj, rj) and np.array_equal(gl, rl)
+    (_, _, _), scale = oracle.ttm("hash", coo[:3] + (np.abs(coo[3]),), dims, abs_f(Tf), w_cap=BIG)
+    assert_vals_close(gv, rv, scale, f"ttm {perm}")
+
+
 @pytest.mark.parametrize("R", [8, 32])
 def test_ttm_against_oracle(spws_lib, R):
     import sparsews_gb300 as sp
