@@ -140,9 +140,13 @@ struct Factor {
 };
 
 // Warp per piece: left-to-right FP64 sums of the piece's leaves for output
-// columns [j0, j0 + kTileR) (lane handles j0 + lane + 32u). MTTKRP forms
-// (b * C(k,j)) * D(l,j) (hash_free.h:307), TTM forms b * C(i,l) (hash_il.h:317).
-template <int MODE>
+// columns [j0, j0 + 32 * JPL) (lane handles j0 + lane + 32u, u < JPL). MTTKRP
+// forms (b * C(k,j)) * D(l,j) (hash_free.h:307), TTM forms b * C(i,l)
+// (hash_il.h:317). JPL is the smallest power of two covering the rank (at
+// most kJpl): a rank-32 factor needs one accumulator per lane, and the
+// registers the other seven would hold are what limits how many warps (each
+// waiting on its factor-row loads) an SM keeps in flight.
+template <int MODE, int JPL>
 __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, const long long* __restrict__ pstart,
                          const long long* __restrict__ starts, const int32_t* __restrict__ r0,
                          const int32_t* __restrict__ r1, const double* __restrict__ bv, Factor F0, Factor F1, int32_t R,
@@ -153,10 +157,10 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   if (w >= npieces) return;
   const long long q0 = pstart[w];
   const long long q1 = min(q0 + (long long)kPiece, starts[pseg[w] + 1]);
-  double acc[kJpl];
+  double acc[JPL];
   unsigned started = 0;
 #pragma unroll
-  for (int u = 0; u < kJpl; u++) acc[u] = 0.0;
+  for (int u = 0; u < JPL; u++) acc[u] = 0.0;
   for (long long qb = q0; qb < q1; qb += 32) {
     const long long q = qb + lane;
     int32_t a0 = -1, a1 = -1;
@@ -173,7 +177,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
       const double bb = __shfl_sync(0xffffffffu, b, t);
       if (x0 >= F0.rows || (MODE == 0 && x1 >= F1.rows)) continue;  // factor row absent
 #pragma unroll
-      for (int u = 0; u < kJpl; u++) {
+      for (int u = 0; u < JPL; u++) {
         const int j = j0 + lane + 32 * u;
         if (j >= R) break;
         const bool have0 = (F0.mask[(int64_t)x0 * F0.mw + (j >> 5)] >> (j & 31)) & 1u;
@@ -188,7 +192,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
     }
   }
 #pragma unroll
-  for (int u = 0; u < kJpl; u++) {
+  for (int u = 0; u < JPL; u++) {
     const int j = j0 + lane + 32 * u;
     const bool in = j < R;
     if (in) partial[w * (int64_t)(32 * pw) + (j - j0)] = acc[u];
@@ -415,14 +419,23 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   for (int32_t j0 = 0; j0 < R; j0 += kTileR) {
     if (npieces > 0) {
       const unsigned gp = (unsigned)((npieces + 7) / 8);
-      if (mode == 0)
-        k_pieces<0><<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
-                                       r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw,
-                                       pw, partial.as<double>(), pmask.as<uint32_t>());
-      else
-        k_pieces<1><<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
-                                       r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw,
-                                       pw, partial.as<double>(), pmask.as<uint32_t>());
+      const int jpl = mw >= 5 ? 8 : (mw >= 3 ? 4 : mw);  // power of two >= min(mw, 8)
+      auto launch = [&](auto kernel) {
+        kernel<<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
+                                  r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw, pw,
+                                  partial.as<double>(), pmask.as<uint32_t>());
+      };
+      if (mode == 0) {
+        if (jpl <= 1) launch(k_pieces<0, 1>);
+        else if (jpl == 2) launch(k_pieces<0, 2>);
+        else if (jpl == 4) launch(k_pieces<0, 4>);
+        else launch(k_pieces<0, 8>);
+      } else {
+        if (jpl <= 1) launch(k_pieces<1, 1>);
+        else if (jpl == 2) launch(k_pieces<1, 2>);
+        else if (jpl == 4) launch(k_pieces<1, 4>);
+        else launch(k_pieces<1, 8>);
+      }
       k_combine<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, poff.as<long long>(), partial.as<double>(),
                                                            pmask.as<uint32_t>(), R, j0, mw, pw, segval.as<double>(),
                                                            segmask.as<uint32_t>());
