@@ -62,12 +62,13 @@ __global__ void k_fiber_root(int32_t nk, const int32_t* __restrict__ roots, cons
   for (int32_t f = pos1[r] + lane; f < pos1[r + 1]; f += 32) fib_root[f] = roots[r];
 }
 
-// leaf_fib[p] = level-1 fiber that owns leaf p
+// leaf_fib[p] = level-1 fiber that owns leaf p. Thread per fiber: level-1
+// fibers are mostly one or two leaves long, so a warp per fiber left 30 of
+// its lanes idle (1.7 ms for 15M fibers).
 __global__ void k_leaf_fiber(int32_t nf, const int32_t* __restrict__ pos2, int32_t* __restrict__ leaf_fib) {
-  const int lane = threadIdx.x & 31;
-  const int64_t f = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
-  for (int32_t p = pos2[f] + lane; p < pos2[f + 1]; p += 32) leaf_fib[p] = (int32_t)f;
+  for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) leaf_fib[p] = (int32_t)f;
 }
 
 // Bucket keys: MTTKRP buckets by the leaf coordinate, TTM by (root, leaf).
@@ -151,7 +152,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
                          const long long* __restrict__ starts, const int32_t* __restrict__ r0,
                          const int32_t* __restrict__ r1, const double* __restrict__ bv, Factor F0, Factor F1, int32_t R,
                          int32_t j0, int32_t mw, int32_t pw, double* __restrict__ partial,
-                         uint32_t* __restrict__ pmask) {
+                         uint32_t* __restrict__ pmask, double* __restrict__ segval, uint32_t* __restrict__ segmask) {
   const int lane = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= npieces) return;
@@ -180,26 +181,43 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
       for (int u = 0; u < JPL; u++) {
         const int j = j0 + lane + 32 * u;
         if (j >= R) break;
-        const bool have0 = (F0.mask[(int64_t)x0 * F0.mw + (j >> 5)] >> (j & 31)) & 1u;
-        bool have = have0;
-        if (MODE == 0) have = have && ((F1.mask[(int64_t)x1 * F1.mw + (j >> 5)] >> (j & 31)) & 1u);
-        if (!have) continue;
-        double t0 = __dmul_rn(bb, F0.dense[(int64_t)x0 * F0.R + j]);
-        if (MODE == 0) t0 = __dmul_rn(t0, F1.dense[(int64_t)x1 * F1.R + j]);
+        // presence words and values are loaded together (an absent entry's
+        // dense value is a stored 0.0, never used), so a leaf costs one
+        // round trip to L2 rather than a mask load and then a value load
+        const uint32_t m0 = F0.mask[(int64_t)x0 * F0.mw + (j >> 5)];
+        const double d0 = F0.dense[(int64_t)x0 * F0.R + j];
+        uint32_t m1 = 0xffffffffu;
+        double d1 = 0.0;
+        if (MODE == 0) {
+          m1 = F1.mask[(int64_t)x1 * F1.mw + (j >> 5)];
+          d1 = F1.dense[(int64_t)x1 * F1.R + j];
+        }
+        if (!(((m0 & m1) >> (j & 31)) & 1u)) continue;
+        double t0 = __dmul_rn(bb, d0);
+        if (MODE == 0) t0 = __dmul_rn(t0, d1);
         acc[u] = ((started >> u) & 1u) ? __dadd_rn(acc[u], t0) : t0;
         started |= 1u << u;
       }
     }
   }
+  // A segment that is this one piece is final here: write its values and
+  // presence straight into the segment arrays (what k_combine would copy);
+  // k_combine handles only segments of several pieces.
+  const int64_t sg = pseg[w];
+  const bool single = q0 == starts[sg] && starts[sg + 1] - q0 <= (long long)kPiece;
 #pragma unroll
   for (int u = 0; u < JPL; u++) {
     const int j = j0 + lane + 32 * u;
     const bool in = j < R;
-    if (in) partial[w * (int64_t)(32 * pw) + (j - j0)] = acc[u];
     const unsigned m = __ballot_sync(0xffffffffu, in && ((started >> u) & 1u));  // all lanes, one call site
-    if (lane == 0 && u < pw) pmask[w * (int64_t)pw + u] = m;
+    if (single) {
+      if (in) segval[sg * (int64_t)R + j] = acc[u];
+      if (lane == 0 && (j0 / 32 + u) < mw) segmask[sg * (int64_t)mw + j0 / 32 + u] = m;
+    } else {
+      if (in) partial[w * (int64_t)(32 * pw) + (j - j0)] = acc[u];
+      if (lane == 0 && u < pw) pmask[w * (int64_t)pw + u] = m;
+    }
   }
-  (void)mw;
 }
 
 // Warp per segment: add the pieces' partials in piece order into the
@@ -210,7 +228,7 @@ __global__ void k_combine(int64_t nseg, const long long* __restrict__ poff, cons
                           double* __restrict__ segval, uint32_t* __restrict__ segmask) {
   const int lane = threadIdx.x & 31;
   const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (s >= nseg) return;
+  if (s >= nseg || poff[s + 1] - poff[s] == 1) return;  // one piece: k_pieces wrote it
   for (int u = 0; u < kJpl; u++) {
     const int j = j0 + lane + 32 * u;
     double v = 0.0;
@@ -344,7 +362,7 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
     count_launch(1);
   }
   if (B.nf > 0) {
-    k_leaf_fiber<<<(unsigned)((B.nf + 7) / 8), 256, 0, s>>>(B.nf, B.pos2, leaf_fib.as<int32_t>());
+    k_leaf_fiber<<<(unsigned)((B.nf + 255) / 256), 256, 0, s>>>(B.nf, B.pos2, leaf_fib.as<int32_t>());
     count_launch(1);
   }
   const size_t kb = sizeof(unsigned long long) * (size_t)std::max<int64_t>(nnz, 1);
@@ -423,7 +441,8 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
       auto launch = [&](auto kernel) {
         kernel<<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
                                   r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw, pw,
-                                  partial.as<double>(), pmask.as<uint32_t>());
+                                  partial.as<double>(), pmask.as<uint32_t>(), segval.as<double>(),
+                                  segmask.as<uint32_t>());
       };
       if (mode == 0) {
         if (jpl <= 1) launch(k_pieces<0, 1>);
