@@ -125,24 +125,42 @@ int store_i64(long long* dst, long long v, cudaStream_t s) {
 
 namespace {
 
-// Warp per row: 0 <= pos[i] <= pos[i+1] <= nnz, columns in [0, ncols) and
-// strictly increasing within the row. Any violation sets *bad.
+// L lanes per row: 0 <= pos[i] <= pos[i+1] <= nnz, columns in [0, ncols)
+// and strictly increasing within the row. Any violation sets *bad. L follows
+// the average row length (launch_validate_csr): a warp per row for long rows,
+// one thread per row for the one- or two-entry rows of a CSF level.
+template <int L>
 __global__ void k_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int32_t* __restrict__ pos,
                                const int32_t* __restrict__ crd, int* __restrict__ bad) {
-  const int lane = threadIdx.x & 31;
-  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= n) return;
-  const int32_t s = pos[i], e = pos[i + 1];
-  if (s < 0 || e < s || (int64_t)e > nnz) {
-    if (lane == 0) atomicExch(bad, 1);
-    return;
-  }
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = t / L;
+  const int sub = (int)(t % L);
   bool ok = true;
-  for (int32_t p = s + lane; p < e; p += 32) {
-    const int k = crd[p];
-    ok &= k >= 0 && k < ncols && (p == s || crd[p - 1] < k);
+  if (i < n) {
+    const int32_t s = pos[i], e = pos[i + 1];
+    if (s < 0 || e < s || (int64_t)e > nnz) {
+      ok = false;
+    } else {
+      for (int32_t p = s + sub; p < e; p += L) {
+        const int k = crd[p];
+        ok &= k >= 0 && k < ncols && (p == s || crd[p - 1] < k);
+      }
+    }
   }
-  if (!__all_sync(0xffffffffu, ok) && lane == 0) atomicExch(bad, 1);
+  if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicExch(bad, 1);
+}
+
+void launch_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int32_t* pos, const int32_t* crd, int* bad,
+                         cudaStream_t s) {
+  const int64_t avg = n > 0 ? nnz / n : 0;
+  if (avg <= 2) {
+    k_validate_csr<1><<<(unsigned)(((int64_t)n + 255) / 256), 256, 0, s>>>(n, nnz, ncols, pos, crd, bad);
+  } else if (avg <= 24) {
+    k_validate_csr<4><<<(unsigned)(((int64_t)n * 4 + 255) / 256), 256, 0, s>>>(n, nnz, ncols, pos, crd, bad);
+  } else {
+    k_validate_csr<32><<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, s>>>(n, nnz, ncols, pos, crd, bad);
+  }
+  count_launch(1);
 }
 
 }  // namespace
@@ -161,8 +179,7 @@ int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, i
   SPWS_TRY(dalloc((void**)&bad, sizeof(int), s));
   SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (nrows > 0) {
-    k_validate_csr<<<(unsigned)((nrows + 7) / 8), 256, 0, s>>>(nrows, nnz, ncols, pos, crd, bad);
-    count_launch(1);
+    launch_validate_csr(nrows, nnz, ncols, pos, crd, bad, s);
     SPWS_CUDA(cudaGetLastError());
   }
   int hbad = 0;
@@ -259,8 +276,7 @@ int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nro
   SPWS_TRY(rb.get(&ends[1], pos + nrows, sizeof(int32_t)));
   SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (nrows > 0) {
-    k_validate_csr<<<(unsigned)((nrows + 7) / 8), 256, 0, s>>>(nrows, nnz, ncols, pos, crd, bad);
-    count_launch(1);
+    launch_validate_csr(nrows, nnz, ncols, pos, crd, bad, s);
     SPWS_CUDA(cudaGetLastError());
   }
   int hbad = 0;
