@@ -49,8 +49,14 @@ constexpr int kBoundInts = 2048;              // shared table of per-(j, window)
 constexpr int kMaxWin = 64;                   // windows per span with precomputed bounds
 constexpr int kBuckets = 66;                  // cost buckets: 0 = no products, b = 1 + floor(log2(P))
 constexpr int kLightBucket = 9;               // default: rows with bucket <= 9 (fewer than 512 products) go to k_light
-constexpr int kLightMax = 512;                // staging entries per warp in k_light
+constexpr int kLightMax = 512;                // staging entries per warp in k_light's largest tier
 constexpr int kLightWarps = 8;                // warps per CTA in k_light
+// k_light runs as three launches over the light rows' cost tiers (rows of
+// 256-511, 128-255 and under 128 products), each staging only as many entries
+// per warp as its longest row can have: short rows then fit 4x more warps on
+// an SM than with one staging size for all.
+constexpr int kLightTiers = 3;
+constexpr int kLightStage[kLightTiers] = {512, 256, 128};
 
 struct RowInfo {
   long long products;  // sum over j in A(i,:) of nnz(B(j,:)) (upper bound of the row's nnz)
@@ -111,17 +117,26 @@ __global__ void k_row_info(int32_t nA, const int32_t* __restrict__ Ap, const int
 }
 
 // Single thread: bucket offsets in descending cost order (bucket 0 excluded).
+// tier[0..3] bound the light rows' three cost tiers in order: tier[0] =
+// nheavy, tier[1] = first row under 256 products, tier[2] = first row under
+// 128, tier[3] = nwork (a tier is empty when light_bucket excludes it).
 __global__ void k_order_offsets(const int* __restrict__ hist, int* __restrict__ cursor, int* __restrict__ nwork,
-                                int* __restrict__ nheavy, int light_bucket) {
+                                int* __restrict__ nheavy, int light_bucket, int* __restrict__ tier) {
   if (threadIdx.x == 0) {
     int run = 0;
     for (int b = kBuckets - 1; b >= 1; b--) {
-      if (b == light_bucket) *nheavy = run;
+      if (b == light_bucket) {
+        *nheavy = run;
+        tier[0] = run;
+      }
+      if (b == min(light_bucket, 8)) tier[1] = run;
+      if (b == min(light_bucket, 7)) tier[2] = run;
       cursor[b] = run;
       run += hist[b];
     }
     cursor[0] = run;
     *nwork = run;
+    tier[3] = run;
   }
 }
 
@@ -744,13 +759,13 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
 // with a bitonic network (keys are unique, so the order of equal columns is
 // their visiting order), and each run of equal columns is summed left to
 // right: the value is the reference's sequential sum bit for bit.
-template <bool NUMERIC>
+template <bool NUMERIC, int STAGE>
 __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long* key = reinterpret_cast<unsigned long long*>(smem) + (size_t)warp * kLightMax;
-  double* val = reinterpret_cast<double*>(smem + sizeof(unsigned long long) * kLightMax * kLightWarps) +
-                (size_t)warp * kLightMax;
+  unsigned long long* key = reinterpret_cast<unsigned long long*>(smem) + (size_t)warp * STAGE;
+  double* val = reinterpret_cast<double*>(smem + sizeof(unsigned long long) * STAGE * kLightWarps) +
+                (size_t)warp * STAGE;
   const int lo_idx = *a.nheavy, hi_idx = *a.nwork;
   const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
@@ -775,7 +790,7 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
       }
       const int base = n;
       n += warp_expand_indexed(sl, [&](int f, int32_t p, double av) {
-        const int at = base + f;  // < kLightMax: the row has fewer than 512 products
+        const int at = base + f;  // < STAGE: the tier's rows have fewer products
         key[at] = ((unsigned long long)(uint32_t)__ldg(a.Bk + p) << 32) | (unsigned)at;
         if (NUMERIC) val[at] = __dmul_rn(av, __ldg(a.Bv + p));
       });
@@ -822,8 +837,10 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
   }
 }
 
-constexpr size_t kLightSymSmem = sizeof(unsigned long long) * kLightMax * kLightWarps;
-constexpr size_t kLightNumSmem = (sizeof(unsigned long long) + sizeof(double)) * kLightMax * kLightWarps;
+constexpr size_t light_smem(bool numeric, int stage) {
+  return (numeric ? sizeof(unsigned long long) + sizeof(double) : sizeof(unsigned long long)) * (size_t)stage *
+         kLightWarps;
+}
 constexpr size_t kSymSmem = sizeof(uint32_t) * kSpanWords + sizeof(Batch);
 constexpr size_t num_smem(int acc) {
   return sizeof(double) * acc + sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords + sizeof(Batch) +
@@ -848,9 +865,58 @@ int light_bucket_of(int light_max) {
 // while that kernel runs in another stream can wait for it, which would tie a
 // small product's latency to a large one's.
 struct RowKernelCfg {
-  int per_sym = 1, per_num = 1, per_num_wide = 1, per_ls = 1, per_ln = 1;
+  int per_sym = 1, per_num = 1, per_num_wide = 1;
+  int per_ls[kLightTiers] = {1, 1, 1}, per_ln[kLightTiers] = {1, 1, 1};  // k_light CTAs per SM, per tier
   bool init = false;
 };
+
+template <bool NUMERIC, int STAGE>
+int light_cfg_one(int* per) {
+  const size_t smem = light_smem(NUMERIC, STAGE);
+  SPWS_CUDA(cudaFuncSetAttribute(k_light<NUMERIC, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, k_light<NUMERIC, STAGE>, kLightWarps * 32, smem));
+  *per = std::max(*per, 1);
+  return SPWS_OK;
+}
+
+template <bool NUMERIC>
+int light_cfg(RowKernelCfg* c) {
+  int* per = NUMERIC ? c->per_ln : c->per_ls;
+  SPWS_TRY((light_cfg_one<NUMERIC, kLightStage[0]>(&per[0])));
+  SPWS_TRY((light_cfg_one<NUMERIC, kLightStage[1]>(&per[1])));
+  SPWS_TRY((light_cfg_one<NUMERIC, kLightStage[2]>(&per[2])));
+  return SPWS_OK;
+}
+
+// Launches k_light over the three cost tiers of the light rows (tier[0..3],
+// from k_order_offsets), each with its own claim counter (counters[0..2])
+// and as many CTAs per SM as its staging size allows. `waves` > 1 time-slices
+// each launch like the CTA kernels (see PassArgs::yield_ns).
+template <bool NUMERIC>
+int launch_light(const PassArgs& base, const int* tier, int* counters, const RowKernelCfg& kc, int sms, int waves,
+                 long long yield_ns, cudaStream_t s) {
+  const int* per = NUMERIC ? kc.per_ln : kc.per_ls;
+  for (int t = 0; t < kLightTiers; t++) {
+    PassArgs p = base;
+    p.nheavy = tier + t;
+    p.nwork = tier + t + 1;
+    p.light_counter = counters + t;
+    const int g = sms * std::max(per[t], 1);
+    p.yield_ns = yield_ns;
+    p.yield_ctas = waves > 1 ? g * (waves - 1) : 0;
+    const unsigned grid = (unsigned)(g * waves);
+    const size_t smem = light_smem(NUMERIC, kLightStage[t]);
+    if (t == 0)
+      k_light<NUMERIC, kLightStage[0]><<<grid, kLightWarps * 32, smem, s>>>(p);
+    else if (t == 1)
+      k_light<NUMERIC, kLightStage[1]><<<grid, kLightWarps * 32, smem, s>>>(p);
+    else
+      k_light<NUMERIC, kLightStage[2]><<<grid, kLightWarps * 32, smem, s>>>(p);
+  }
+  count_launch(kLightTiers);
+  SPWS_CUDA(cudaGetLastError());
+  return SPWS_OK;
+}
 
 int row_kernel_cfg(int device, RowKernelCfg* out) {
   static std::mutex mu;
@@ -866,21 +932,15 @@ int row_kernel_cfg(int device, RowKernelCfg* out) {
     SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAcc>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
     SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAccWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kNumSmemWide));
-    SPWS_CUDA(cudaFuncSetAttribute(k_light<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightSymSmem));
-    SPWS_CUDA(cudaFuncSetAttribute(k_light<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLightNumSmem));
+    SPWS_TRY(light_cfg<false>(&c));
+    SPWS_TRY(light_cfg<true>(&c));
     SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sym, k_symbolic, kThreads, kSymSmem));
     SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num, k_numeric<kAcc>, kThreads, kNumSmem));
     SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num_wide, k_numeric<kAccWide>, kThreads,
                                                             kNumSmemWide));
-    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_ls, k_light<false>, kLightWarps * 32,
-                                                            kLightSymSmem));
-    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_ln, k_light<true>, kLightWarps * 32,
-                                                            kLightNumSmem));
     c.per_sym = std::max(c.per_sym, 1);
     c.per_num = std::max(c.per_num, 1);
     c.per_num_wide = std::max(c.per_num_wide, 1);
-    c.per_ls = std::max(c.per_ls, 1);
-    c.per_ln = std::max(c.per_ln, 1);
     c.init = true;
   }
   *out = c;
@@ -893,7 +953,10 @@ struct RowwisePlanImpl {
     int cursor[kBuckets];
     int nwork;
     int nheavy;
-    int counter[4];
+    int tier[kLightTiers + 1];
+    // claims: [0] heavy symbolic, [1] heavy numeric, [2..4] light symbolic
+    // tiers, [5..7] light numeric tiers
+    int counter[8];
     int err;
     unsigned long long products;
     long long nnz;
@@ -911,7 +974,8 @@ struct RowwisePlanImpl {
   uint32_t* bmstore = nullptr;
   size_t bmstore_bytes = 0;
   PassArgs pa{};
-  int per_num = 1, per_ln = 1;
+  int per_num = 1;
+  RowKernelCfg kc;
   long long nnz = 0;
   unsigned long long products = 0;
   bool empty = false;
@@ -995,7 +1059,7 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
                                                       &sm->products, &sm->err);
   P->light_bucket = light_bucket_of(opt.light_max);
   P->wide = opt.wide_windows;
-  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy, P->light_bucket);
+  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy, P->light_bucket, sm->tier);
   k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, sm->cursor, P->order);
   count_launch(3);
   SPWS_CUDA(cudaGetLastError());
@@ -1042,26 +1106,23 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   pa.nwork = &sm->nwork;
   pa.nheavy = &sm->nheavy;
   pa.counter = &sm->counter[0];
-  pa.light_counter = &sm->counter[2];
   pa.rowcnt = P->rowcnt;
   pa.err = &sm->err;
   pa.long_min = opt.long_min;
   pa.col_shift = opt.col_shift;
-  RowKernelCfg kc;
+  RowKernelCfg& kc = P->kc;
   SPWS_TRY(row_kernel_cfg(ds->device, &kc));
-  const int per_sym = kc.per_sym, per_ls = kc.per_ls;
+  const int per_sym = kc.per_sym;
   P->per_num = P->wide ? kc.per_num_wide : kc.per_num;
-  P->per_ln = kc.per_ln;
   // products per microsecond of the whole GPU, R-MAT-like rows: sizes the CTA waves of time-sliced launches
   constexpr double kSymRate = 5e5, kNumRate = 9e4;
   P->waves_sym = P->waves(kSymRate);
   P->waves_num = P->waves(kNumRate);
   const int g_sym = ds->sm_count * std::max(per_sym, 1);
   k_symbolic<<<g_sym * P->waves_sym, kThreads, kSymSmem, s>>>(P->sliced(g_sym, P->waves_sym));
-  const int g_ls = ds->sm_count * std::max(per_ls, 1);
-  k_light<false><<<g_ls * P->waves_sym, kLightWarps * 32, kLightSymSmem, s>>>(P->sliced(g_ls, P->waves_sym));
-  count_launch(2);
+  count_launch(1);
   SPWS_CUDA(cudaGetLastError());
+  SPWS_TRY(launch_light<false>(pa, sm->tier, &sm->counter[2], kc, ds->sm_count, P->waves_sym, P->yield_ns, s));
   SPWS_CUDA(cudaEventRecord(P->ev[2], s));
 
   SPWS_TRY(scan_counts_i32(P->rowcnt, C->pos, nA, &sm->nnz, s));
@@ -1102,20 +1163,19 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
   SPWS_TRY(dalloc((void**)&C->vals, sizeof(double) * (size_t)std::max<long long>(nnz, 1), s));
   PassArgs& pa = P->pa;
   pa.counter = &P->sm->counter[1];
-  pa.light_counter = &P->sm->counter[3];
   pa.Cp = C->pos;
   pa.Ck = C->crd;
   pa.Cv = C->vals;
   SPWS_CUDA(cudaEventRecord(P->ev[4], s));
   const int g_num = ds->sm_count * std::max(P->per_num, 1);
-  const int g_ln = ds->sm_count * std::max(P->per_ln, 1);
   if (P->wide)
     k_numeric<kAccWide><<<g_num * P->waves_num, kThreads, kNumSmemWide, s>>>(P->sliced(g_num, P->waves_num));
   else
     k_numeric<kAcc><<<g_num * P->waves_num, kThreads, kNumSmem, s>>>(P->sliced(g_num, P->waves_num));
-  k_light<true><<<g_ln * P->waves_num, kLightWarps * 32, kLightNumSmem, s>>>(P->sliced(g_ln, P->waves_num));
-  count_launch(2);
+  count_launch(1);
   SPWS_CUDA(cudaGetLastError());
+  SPWS_TRY(launch_light<true>(pa, P->sm->tier, &P->sm->counter[5], P->kc, ds->sm_count, P->waves_num, P->yield_ns,
+                              s));
   SPWS_CUDA(cudaEventRecord(P->ev[5], s));
   int err = 0;
   Readback rb(s);
@@ -1145,19 +1205,16 @@ int rowwise_plan_launch_numeric(RowwisePlan* plan, cudaStream_t s) {
   DeviceState* ds = nullptr;
   SPWS_TRY(device_state(&ds));
   SPWS_CUDA(cudaMemsetAsync(&P->sm->counter[1], 0, sizeof(int), s));
-  SPWS_CUDA(cudaMemsetAsync(&P->sm->counter[3], 0, sizeof(int), s));
+  SPWS_CUDA(cudaMemsetAsync(&P->sm->counter[5], 0, sizeof(int) * kLightTiers, s));
   const int g_num = ds->sm_count * std::max(P->per_num, 1);
-  const int g_ln = ds->sm_count * std::max(P->per_ln, 1);
   PassArgs pa = P->pa;
   pa.counter = &P->sm->counter[1];
-  pa.light_counter = &P->sm->counter[3];
   if (P->wide)
     k_numeric<kAccWide><<<g_num, kThreads, kNumSmemWide, s>>>(pa);
   else
     k_numeric<kAcc><<<g_num, kThreads, kNumSmem, s>>>(pa);
-  k_light<true><<<g_ln, kLightWarps * 32, kLightNumSmem, s>>>(pa);
   SPWS_CUDA(cudaGetLastError());
-  return SPWS_OK;
+  return launch_light<true>(pa, P->sm->tier, &P->sm->counter[5], P->kc, ds->sm_count, 1, 0, s);
 }
 
 const int* rowwise_plan_err(const RowwisePlan* plan) {
@@ -1204,7 +1261,8 @@ struct NoAllocHead {
   int cursor[kBuckets];
   int nwork;
   int nheavy;
-  int counter[4];
+  int tier[kLightTiers + 1];
+  int counter[8];  // as RowwisePlanImpl::Small::counter
   int err;
   int bad;
   unsigned long long products;
@@ -1291,7 +1349,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
 
   k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A->pos, A->crd, B->pos, B->crd, info, hd->hist,
                                                       &hd->products, &hd->err);
-  k_order_offsets<<<1, 32, 0, s>>>(hd->hist, hd->cursor, &hd->nwork, &hd->nheavy, kLightBucket);
+  k_order_offsets<<<1, 32, 0, s>>>(hd->hist, hd->cursor, &hd->nwork, &hd->nheavy, kLightBucket, hd->tier);
   k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, hd->cursor, order);
   count_launch(3);
   SPWS_CUDA(cudaGetLastError());
@@ -1308,17 +1366,16 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.nwork = &hd->nwork;
   pa.nheavy = &hd->nheavy;
   pa.counter = &hd->counter[0];
-  pa.light_counter = &hd->counter[2];
   pa.rowcnt = rowcnt;
   pa.err = &hd->err;
   pa.long_min = kLongMin;
   RowKernelCfg kc;
   SPWS_TRY(row_kernel_cfg(dev, &kc));
-  const int per_sym = kc.per_sym, per_num = kc.per_num, per_ls = kc.per_ls, per_ln = kc.per_ln;
+  const int per_sym = kc.per_sym, per_num = kc.per_num;
   k_symbolic<<<sms * std::max(per_sym, 1), kThreads, kSymSmem, s>>>(pa);
-  k_light<false><<<sms * std::max(per_ls, 1), kLightWarps * 32, kLightSymSmem, s>>>(pa);
-  count_launch(2);
+  count_launch(1);
   SPWS_CUDA(cudaGetLastError());
+  SPWS_TRY(launch_light<false>(pa, hd->tier, &hd->counter[2], kc, sms, 1, 0, s));
   SPWS_TRY(scan_counts_i32_into(rowcnt, C_pos, nA, &hd->nnz, tiles, s));
 
   long long nnz = 0;
@@ -1336,14 +1393,13 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
     return SPWS_ERR_CAPACITY;
   }
   pa.counter = &hd->counter[1];
-  pa.light_counter = &hd->counter[3];
   pa.Cp = C_pos;
   pa.Ck = C_crd;
   pa.Cv = C_vals;
   k_numeric<kAcc><<<sms * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
-  k_light<true><<<sms * std::max(per_ln, 1), kLightWarps * 32, kLightNumSmem, s>>>(pa);
-  count_launch(2);
+  count_launch(1);
   SPWS_CUDA(cudaGetLastError());
+  SPWS_TRY(launch_light<true>(pa, hd->tier, &hd->counter[5], kc, sms, 1, 0, s));
   SPWS_CUDA(cudaMemcpyAsync(&err, &hd->err, sizeof(int), cudaMemcpyDeviceToHost, s));
   SPWS_CUDA(cudaStreamSynchronize(s));
   if (err) {
