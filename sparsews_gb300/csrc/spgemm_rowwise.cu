@@ -49,12 +49,12 @@ constexpr int kBoundInts = 2048;              // shared table of per-(j, window)
 constexpr int kMaxWin = 64;                   // windows per span with precomputed bounds
 constexpr int kBuckets = 66;                  // cost buckets: 0 = no products, b = 1 + floor(log2(P))
 constexpr int kLightBucket = 9;               // default: rows with bucket <= 9 (fewer than 512 products) go to k_light
-constexpr int kLightMax = 512;                // staging entries per warp in k_light's largest tier
 constexpr int kLightWarps = 8;                // warps per CTA in k_light
-// k_light runs as three launches over the light rows' cost tiers (rows of
-// 256-511, 128-255 and under 128 products), each staging only as many entries
-// per warp as its longest row can have: short rows then fit 4x more warps on
-// an SM than with one staging size for all.
+// Light rows run as three launches over their cost tiers (rows of 256-511,
+// 128-255 and under 128 products): k_light for the first two, each staging
+// only as many entries per warp as its longest row can have, and
+// k_light_hash (a per-warp hash table, no sort of the products) for the
+// shortest rows, the bulk of a uniform matrix's rows.
 constexpr int kLightTiers = 3;
 constexpr int kLightStage[kLightTiers] = {512, 256, 128};
 
@@ -837,6 +837,193 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
   }
 }
 
+// Bitonic sort by column of the first E*32 of a warp's (column, value) pairs,
+// entry e of lane l at position e*32 + l: partners 32 or more apart sit in
+// the same lane's registers, closer ones are exchanged by shuffles.
+template <int E>
+__device__ __forceinline__ void warp_sort_pairs(int32_t (&kc)[4], double (&kv)[4]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32 * E; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int p = e * 32 + lane;
+        const bool up = (p & k) == 0;
+        if (j >= 32) {
+          const int e2 = e ^ (j >> 5);
+          if (e2 > e && ((kc[e] > kc[e2]) == up)) {
+            const int32_t tk = kc[e];
+            kc[e] = kc[e2];
+            kc[e2] = tk;
+            const double tv = kv[e];
+            kv[e] = kv[e2];
+            kv[e2] = tv;
+          }
+        } else {
+          const int32_t ok = __shfl_xor_sync(0xffffffffu, kc[e], j);
+          const double ov = __shfl_xor_sync(0xffffffffu, kv[e], j);
+          const bool take_min = ((lane & j) == 0) == up;
+          if (take_min ? ok < kc[e] : ok > kc[e]) {
+            kc[e] = ok;
+            kv[e] = ov;
+          }
+        }
+      }
+    }
+  }
+}
+
+// Light rows of the shortest tier (under 128 products): one warp per row
+// with an open-addressing table of H column slots in shared memory instead
+// of a sort of every product. The products arrive 32 per round in the
+// reference's visiting order (j ascending, then k); in each round the lanes
+// holding the same column find each other (__match_any_sync) and the lowest
+// of them, the column's owner for the round, adds its own product and then
+// the others' in lane order into the column's slot (the first product of a
+// column is stored, not added). Rounds run in order, so every column's value
+// is the reference's sequential sum bit for bit. The distinct columns (fewer
+// than H / 2) are then sorted by a bitonic network in registers and written
+// in order. About a quarter of the instructions of the staged sort.
+template <bool NUMERIC, int H>
+__global__ void __launch_bounds__(kLightWarps * 32) k_light_hash(PassArgs a) {
+  static_assert(H == 256, "distinct columns < H / 2 = 128: at most four sorted entries per lane");
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t* hk = reinterpret_cast<int32_t*>(smem) + (size_t)warp * H;
+  double* hv = reinterpret_cast<double*>(smem + sizeof(int32_t) * H * kLightWarps) + (size_t)warp * H;
+  const int lo_idx = *a.nheavy, hi_idx = *a.nwork;
+  const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) {
+      idx = claim_or_yield(a.light_counter, a, t0);
+      idx = idx == INT_MAX ? INT_MAX : idx + lo_idx;
+    }
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= hi_idx) break;
+    const int32_t i = a.order[idx];
+    const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
+#pragma unroll
+    for (int t = lane; t < H; t += 32) hk[t] = -1;
+    __syncwarp();
+    int fresh_count = 0;  // columns this lane inserted
+    for (int32_t qb = q0; qb < q1; qb += 32) {
+      Slice sl{0, 0, 0.0};
+      const int32_t q = qb + lane;
+      if (q < q1) {
+        const int32_t j = __ldg(a.Aj + q);
+        sl.s = __ldg(a.Bp + j);
+        sl.len = __ldg(a.Bp + j + 1) - sl.s;
+        if (NUMERIC) sl.a = __ldg(a.Av + q);
+      }
+      warp_expand_rounds(sl, [&](bool valid, int, int32_t p, double av) {
+        const int32_t col = valid ? __ldg(a.Bk + p) : -1;
+        double v = 0.0;
+        if (NUMERIC && valid) v = __dmul_rn(av, __ldg(a.Bv + p));
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        const unsigned peers = __match_any_sync(0xffffffffu, col) & vm;
+        const bool owner = valid && (__ffs(peers) - 1) == lane;
+        int slot = -1;
+        bool fresh = false;
+        if (owner) {  // find the column's slot, or claim an empty one
+          unsigned h = ((unsigned)col * 0x9E3779B1u) >> 24;  // top 8 bits: H = 256 slots
+          // fewer than H / 2 distinct columns, so a free slot is always in
+          // reach; the bound only guards against a row outside the tier
+          for (int probe = 0; probe < H; probe++, h = (h + 1) & (H - 1)) {
+            const int k = hk[h];
+            if (k == col) {
+              slot = (int)h;
+              break;
+            }
+            if (k == -1) {
+              const int old = atomicCAS(&hk[h], -1, col);
+              if (old == -1 || old == col) {
+                fresh = old == -1;
+                slot = (int)h;
+                break;
+              }
+            }
+          }
+          if (slot < 0) atomicExch(a.err, 1);
+          fresh_count += fresh;
+        }
+        if (NUMERIC) {
+          double acc = 0.0;
+          if (slot >= 0) acc = fresh ? v : __dadd_rn(hv[slot], v);
+          unsigned rest = owner ? (peers & (peers - 1u)) : 0u;  // the other holders, lowest lane first
+          const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)__popc(rest));
+          for (int r = 0; r < rounds; r++) {
+            const int src = rest ? __ffs(rest) - 1 : lane;
+            const double x = __shfl_sync(0xffffffffu, v, src);
+            if (rest) {
+              acc = __dadd_rn(acc, x);
+              rest &= rest - 1u;
+            }
+          }
+          if (slot >= 0) hv[slot] = acc;
+        }
+        __syncwarp();  // the next round sees this round's slots
+      });
+    }
+    const int U = __reduce_add_sync(0xffffffffu, (unsigned)fresh_count);  // distinct columns (< H / 2)
+    if (!NUMERIC) {
+      if (lane == 0) a.rowcnt[i] = U;
+      __syncwarp();
+      continue;
+    }
+    // compact the occupied slots in place (chunk c's entries land at
+    // positions below c*32 + 32, all read before any is written), then load
+    // them as entry e of lane l = position e*32 + l, padding INT_MAX
+    int filled = 0;
+#pragma unroll
+    for (int c = 0; c < H / 32; c++) {
+      const int t = c * 32 + lane;
+      const int32_t k = hk[t];
+      const double x = hv[t];
+      const unsigned occ = __ballot_sync(0xffffffffu, k != -1);
+      __syncwarp();
+      if (k != -1) {
+        const int at = filled + __popc(occ & ((1u << lane) - 1u));
+        hk[at] = k;
+        hv[at] = x;
+      }
+      filled += __popc(occ);
+      __syncwarp();
+    }
+    int32_t kc[4];
+    double kv[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int p = e * 32 + lane;
+      kc[e] = p < U ? hk[p] : INT_MAX;
+      kv[e] = p < U ? hv[p] : 0.0;
+    }
+    if (U <= 32)
+      warp_sort_pairs<1>(kc, kv);
+    else if (U <= 64)
+      warp_sort_pairs<2>(kc, kv);
+    else
+      warp_sort_pairs<4>(kc, kv);
+    const int32_t out = a.Cp[i];
+    const int32_t shift = a.col_shift ? a.col_shift[i] : 0;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int p = e * 32 + lane;
+      if (p < U && out + p < a.Cp[i + 1]) {  // never write past the row the symbolic pass sized
+        a.Ck[out + p] = kc[e] - shift;
+        a.Cv[out + p] = kv[e];
+      }
+    }
+    if (lane == 0 && out + U != a.Cp[i + 1]) atomicExch(a.err, 1);
+    __syncwarp();
+  }
+}
+
+constexpr int kLightHashSlots = 256;
+constexpr size_t light_hash_smem() { return (sizeof(int32_t) + sizeof(double)) * kLightHashSlots * kLightWarps; }
+
 constexpr size_t light_smem(bool numeric, int stage) {
   return (numeric ? sizeof(unsigned long long) + sizeof(double) : sizeof(unsigned long long)) * (size_t)stage *
          kLightWarps;
@@ -884,7 +1071,12 @@ int light_cfg(RowKernelCfg* c) {
   int* per = NUMERIC ? c->per_ln : c->per_ls;
   SPWS_TRY((light_cfg_one<NUMERIC, kLightStage[0]>(&per[0])));
   SPWS_TRY((light_cfg_one<NUMERIC, kLightStage[1]>(&per[1])));
-  SPWS_TRY((light_cfg_one<NUMERIC, kLightStage[2]>(&per[2])));
+  const size_t smem = light_hash_smem();
+  SPWS_CUDA(cudaFuncSetAttribute(k_light_hash<NUMERIC, kLightHashSlots>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], k_light_hash<NUMERIC, kLightHashSlots>,
+                                                          kLightWarps * 32, smem));
+  per[2] = std::max(per[2], 1);
   return SPWS_OK;
 }
 
@@ -905,13 +1097,12 @@ int launch_light(const PassArgs& base, const int* tier, int* counters, const Row
     p.yield_ns = yield_ns;
     p.yield_ctas = waves > 1 ? g * (waves - 1) : 0;
     const unsigned grid = (unsigned)(g * waves);
-    const size_t smem = light_smem(NUMERIC, kLightStage[t]);
     if (t == 0)
-      k_light<NUMERIC, kLightStage[0]><<<grid, kLightWarps * 32, smem, s>>>(p);
+      k_light<NUMERIC, kLightStage[0]><<<grid, kLightWarps * 32, light_smem(NUMERIC, kLightStage[0]), s>>>(p);
     else if (t == 1)
-      k_light<NUMERIC, kLightStage[1]><<<grid, kLightWarps * 32, smem, s>>>(p);
+      k_light<NUMERIC, kLightStage[1]><<<grid, kLightWarps * 32, light_smem(NUMERIC, kLightStage[1]), s>>>(p);
     else
-      k_light<NUMERIC, kLightStage[2]><<<grid, kLightWarps * 32, smem, s>>>(p);
+      k_light_hash<NUMERIC, kLightHashSlots><<<grid, kLightWarps * 32, light_hash_smem(), s>>>(p);
   }
   count_launch(kLightTiers);
   SPWS_CUDA(cudaGetLastError());

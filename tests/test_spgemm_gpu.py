@@ -176,3 +176,44 @@ def test_large_output_copied_to_host(spws_lib):
     assert_csr_close(Cd.download(), ref, scale_of(A, A), "download")
     Cd.release()
     d.release()
+
+
+@pytest.mark.parametrize("shape", ["er", "band", "mixed"])
+def test_light_rows_bit_exact(spws_lib, shape):
+    """Rows under 512 products go to the warp-per-row kernels, which sum each
+    column's products in the reference's visiting order (j ascending, then
+    k): the values equal the reference's sequential sums bit for bit (the
+    oracle with a capacity that never flushes), not just within tolerance.
+    'mixed' spreads rows over all three light tiers (<128, 128-255, 256-511
+    products) and includes columns hit by many products of one round."""
+    import sparsews_gb300 as sp
+    if shape == "er":
+        A = gen.er(3000, 6, seed=62)
+    elif shape == "band":
+        A = gen.band(20000, 8, 0.5, seed=63)
+    else:
+        rng = np.random.default_rng(64)
+        n = 4000
+        lens = rng.choice([1, 4, 9, 14, 20, 40, 55], size=n)  # products per row ~ len * 8 (B rows <= 8)
+        rows = np.repeat(np.arange(n), lens)
+        cols = rng.integers(0, 300, size=len(rows))  # few columns: many collisions per round
+        key = np.unique(rows.astype(np.int64) * 300 + cols)
+        r, c = key // 300, key % 300
+        pos = np.zeros(n + 1, np.int64)
+        np.add.at(pos, r + 1, 1)
+        A = (np.cumsum(pos).astype(np.int32), c.astype(np.int32), rng.uniform(-1, 1, len(c)), n, 300)
+        B = gen.er(300, 8, seed=65)
+        B = (B[0], B[1] % 300, B[2], 300, 300)
+        key = np.unique(np.repeat(np.arange(300), np.diff(B[0])).astype(np.int64) * 300 + B[1])
+        r, c = key // 300, key % 300
+        pos = np.zeros(301, np.int64)
+        np.add.at(pos, r + 1, 1)
+        B = (np.cumsum(pos).astype(np.int32), c.astype(np.int32), rng.uniform(-1, 1, len(c)), 300, 300)
+    Bm = A if shape != "mixed" else B
+    prods = np.diff(Bm[0]).astype(np.int64)[A[1]]
+    per_row = np.bincount(np.repeat(np.arange(A[3]), np.diff(A[0])), weights=prods, minlength=A[3])
+    assert per_row.max() < 512  # every row is light
+    got = sp.spgemm(A, Bm)
+    ref = oracle.spgemm("hash", A, Bm, w_cap=1 << 24)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    assert np.array_equal(got[2], ref[2])
