@@ -127,8 +127,8 @@ namespace {
 
 // L lanes per row: 0 <= pos[i] <= pos[i+1] <= nnz, columns in [0, ncols)
 // and strictly increasing within the row. Any violation sets *bad. L follows
-// the average row length (launch_validate_csr): a warp per row for long rows,
-// one thread per row for the one- or two-entry rows of a CSF level.
+// the average row length (launch_validate_csr): one thread per row for the
+// one- or two-entry rows of a CSF level, else a warp per row.
 template <int L>
 __global__ void k_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int32_t* __restrict__ pos,
                                const int32_t* __restrict__ crd, int* __restrict__ bad) {
@@ -152,14 +152,14 @@ __global__ void k_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int3
 
 void launch_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int32_t* pos, const int32_t* crd, int* bad,
                          cudaStream_t s) {
+  // A warp per row unless rows average at most two entries: with fewer lanes,
+  // one long row of a skewed matrix (R-MAT) would hold its lanes for the
+  // whole launch (4 lanes per row measured 7x slower there).
   const int64_t avg = n > 0 ? nnz / n : 0;
-  if (avg <= 2) {
+  if (avg <= 2)
     k_validate_csr<1><<<(unsigned)(((int64_t)n + 255) / 256), 256, 0, s>>>(n, nnz, ncols, pos, crd, bad);
-  } else if (avg <= 24) {
-    k_validate_csr<4><<<(unsigned)(((int64_t)n * 4 + 255) / 256), 256, 0, s>>>(n, nnz, ncols, pos, crd, bad);
-  } else {
+  else
     k_validate_csr<32><<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, s>>>(n, nnz, ncols, pos, crd, bad);
-  }
   count_launch(1);
 }
 
