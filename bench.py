@@ -189,6 +189,44 @@ def run_cpu(A, rows, threads, kind):
     return time.perf_counter() - t0
 
 
+def cpu_instances(insts, threads, target_products, seed=11):
+    """Runs the reference algorithm (oracle port: row-wise hash, the
+    reference's w_cap heuristic) over a random sample of whole instances
+    whose products total ~target, split over `threads` threads. Returns
+    (instances solved, products, seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    kind = "ref" if cpu_kind() == "reference" else "port"
+    rng = np.random.default_rng(seed)
+    sample, total = [], 0
+    for t in rng.permutation(len(insts)):
+        A = insts[t]
+        p = int(np.diff(A[0]).astype(np.int64)[A[1]].sum())
+        sample.append((A, p))
+        total += p
+        if total >= target_products:
+            break
+    sample.sort(key=lambda x: -x[1])
+    parts = [[] for _ in range(threads)]
+    load = [0] * threads
+    for A, p in sample:  # largest first onto the least-loaded thread
+        t = int(np.argmin(load))
+        parts[t].append(A)
+        load[t] += p
+
+    def work(t):
+        for A in parts[t]:
+            oracle.spgemm("hash", A, A, w_cap=oracle.w_cap_default(len(A[1])), kind=kind)
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    t0 = time.perf_counter()
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    return len(sample), total, time.perf_counter() - t0
+
+
 def cpu_kind():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -330,6 +368,9 @@ def bench_spws(args, ws, rank, local, dist):
     ms_sym = sum(s.ms_symbolic for s in stats) / len(stats)
     ms_dev = sum(s.ms_total for s in stats) / len(stats)
     alg_bytes = gustavson_bytes(nA, len(A[1]), products, nA, nnzC)
+    compulsory = 2 * (4 * (nA + 1) + 12 * len(A[1])) + 4 * (nA + 1) + 12 * nnzC  # A, B (= A), C
+    fp64 = C.c_double(0.0)
+    fp64_peak = fp64.value if L.spws_measure_fp64(C.byref(fp64)) == 0 and fp64.value > 0 else None
     peak, peak_src = measured_peaks()
     achieved = alg_bytes / (ms_num * 1e-3) / 1e9
     dev_flops = 2.0 * products / (ms_dev * 1e-3) / 1e9
@@ -393,7 +434,16 @@ def bench_spws(args, ws, rank, local, dist):
         "roofline": {"bound": "hbm", "kernel": "k_numeric", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "traffic": profiled_traffic(args.workload)},
+                     "traffic": profiled_traffic(args.workload),
+                     # the ceiling is max(bytes / BW, flops / FP64 peak); which term binds
+                     "fp64_peak_gflops": fp64_peak,
+                     "ceiling_ms": {"hbm": alg_bytes / (peak * 1e9) * 1e3,
+                                    "fp64": (2.0 * products / (fp64_peak * 1e9) * 1e3) if fp64_peak else None},
+                     "binding": ("hbm" if not fp64_peak or alg_bytes / (peak * 1e9) >= 2.0 * products /
+                                 (fp64_peak * 1e9) else "fp64"),
+                     # A, B and C read or written once each: the floor L2 reuse of B cannot beat
+                     "compulsory_bytes": compulsory,
+                     "compulsory_gbs": compulsory / (ms_dev * 1e-3) / 1e9},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_wall * 1e3, "path": "spws_csr_csr_hash_compute (taco_tensor_t, host arrays)"},
@@ -502,6 +552,13 @@ def bench_batched(args):
                               "taco_abi_solves_per_s": n / seq_abi, "taco_abi_sample": nplain,
                               "speedup_vs_device_entry": seq_dev / wall, "speedup_vs_taco_abi": seq_abi / wall},
             "clocks": clk.summary(), "generation_s": gen_s}
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        k, prods, secs = cpu_instances(insts, threads, args.cpu_batch_products)
+        line["cpu_baseline"] = {"value": k / secs, "unit": "solves/s", "cores": threads, "kind": cpu_kind(),
+                                "sample": f"{k} random instances of the batch ({prods} products) on {threads} "
+                                          f"threads, {secs:.1f} s",
+                                "gflops": 2.0 * prods / secs / 1e9}
     print(json.dumps(line), flush=True)
 
 
@@ -929,7 +986,46 @@ def bench_served(args):
                               "speedup_vs_device_entry": cap / (n / seq_dev),
                               "speedup_vs_taco_abi": cap * abi_mean},
             "clocks": clk.summary(), "generation_s": gen_s}
+    if not args.no_cpu:
+        line["cpu_baseline"] = served_cpu_baseline(small, big, tensors, factor)
     print(json.dumps(line), flush=True)
+
+
+def served_cpu_baseline(small, big, tensors, factor):
+    """The reference algorithm (oracle port of the row-wise hash and TTM
+    hash_il, the reference's capacity heuristics) serving the same mix as
+    N = nproc independent single-threaded workers: single-thread time per
+    request kind is measured on bounded samples (small products: random pool
+    instances of ~2e7 products, scaled to the pool's mean product count;
+    R-MAT: a row sample, scaled by products; TTM: the
+    slices of the 1M-nonzero tensor up to ~40k nonzeros, scaled by nonzeros
+    to the 1M and 5M tensors), and throughput = N / the mix's mean time."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    kind = "ref" if cpu_kind() == "reference" else "port"
+    k, p_small, secs = cpu_instances(small, 1, 20_000_000)
+    p_pool = np.mean([int(np.diff(A[0]).astype(np.int64)[A[1]].sum()) for A in small])
+    t_small = secs / p_small * p_pool
+    rows, prods = cpu_sample_rows(big, 20_000_000)
+    secs = run_cpu(big, rows, 1, kind)
+    p_big = int(np.diff(big[0]).astype(np.int64)[big[1]].sum())
+    t_rmat = secs * p_big / prods
+    (c1, d1), (c5, _) = tensors
+    kk = np.sort(c1[0])[min(len(c1[0]) - 1, 40_000)]  # root slices below kk: ~40k nonzeros
+    keep = c1[0] < kk
+    sub = tuple(x[keep] for x in c1)
+    t0 = time.perf_counter()
+    oracle.ttm("hash", sub, d1, factor, kind=kind)
+    t_sub = time.perf_counter() - t0
+    per_nnz = t_sub / max(int(keep.sum()), 1)
+    t_ttm = 0.5 * per_nnz * (len(c1[3]) + len(c5[3]))
+    mean_t = SERVED_MIX[0] * t_small + SERVED_MIX[1] * t_rmat + SERVED_MIX[2] * t_ttm
+    n = os.cpu_count() or 1
+    return {"value": float(n / mean_t), "unit": "solves/s", "cores": n, "kind": "reference" if kind == "ref" else "port",
+            "sample": f"single-thread s per request: small {t_small:.3f} ({k} instances timed, scaled), "
+                      f"R-MAT {t_rmat:.1f} "
+                      f"({len(rows)}-row sample, {prods} products, scaled), TTM {t_ttm:.2f} ({int(keep.sum())} "
+                      f"nonzeros timed, scaled); {n} independent workers"}
 
 
 def main():
@@ -948,6 +1044,8 @@ def main():
     ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
                     help="products per step of the reference arm (all cores)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-batch-products", type=int, default=300_000_000,
+                    help="batched workload: products in the CPU-baseline sample (all host cores)")
     ap.add_argument("--transpose-cpu-products", type=int, default=30_000_000,
                     help="transpose workload: largest product count timed on the CPU port")
     ap.add_argument("--rank", type=int, default=32, help="mttkrp/ttm workloads: factor rank R")

@@ -192,6 +192,11 @@ unsigned long long spws_launch_count(void);
 /* Overwrite `bytes` of scratch device memory (evicts the L2 between timed runs). */
 int spws_flush_l2(size_t bytes);
 
+/* FP64 FMA throughput of the current device in GFLOP/s (an FMA counts two):
+ * every SM runs eight independent FMA chains per thread for about 10 ms. The
+ * FP64 term of the roofline the benchmarks report. */
+int spws_measure_fp64(double* gflops);
+
 /* Page-lock / unlock a host range so copies to and from it run at DMA speed. */
 int spws_host_pin(void* p, size_t bytes);
 int spws_host_unpin(void* p);

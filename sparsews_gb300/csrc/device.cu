@@ -223,6 +223,61 @@ void spws_free(void* p) { free(p); }
 
 unsigned long long spws_launch_count(void) { return __atomic_load_n(&spws::g_launches, __ATOMIC_RELAXED); }
 
+}  // extern "C"
+
+namespace spws {
+namespace {
+
+// Eight independent FMA chains per thread (x <- x*b + a, |b| slightly above
+// 1, so no chain overflows in `iters` steps); the sum is stored only if it
+// equals an impossible value, which keeps every chain live.
+__global__ void k_fp64_fma(int iters, double* sink) {
+  const double a = 1e-9 * (double)(threadIdx.x + 1), b = 1.0 + 1e-12;
+  double x[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) x[c] = (double)c;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < 8; c++) x[c] = fma(x[c], b, a);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) s += x[c];
+  if (s == -1.0) *sink = s;
+}
+
+}  // namespace
+}  // namespace spws
+
+extern "C" {
+
+int spws_measure_fp64(double* gflops) {
+  if (!gflops) return SPWS_ERR_INVALID;
+  spws::DeviceState* ds = nullptr;
+  SPWS_TRY(spws::device_state(&ds));
+  double* sink = nullptr;
+  SPWS_TRY(spws::dalloc((void**)&sink, sizeof(double), ds->stream));
+  const int threads = 256, blocks = ds->sm_count * 8, iters = 4096;
+  cudaEvent_t e0, e1;
+  SPWS_CUDA(cudaEventCreate(&e0));
+  SPWS_CUDA(cudaEventCreate(&e1));
+  float ms = 0.f;
+  for (int rep = 0; rep < 2; rep++) {  // the first run warms up clocks and caches
+    SPWS_CUDA(cudaEventRecord(e0, ds->stream));
+    spws::k_fp64_fma<<<blocks, threads, 0, ds->stream>>>(iters, sink);
+    spws::count_launch(1);
+    SPWS_CUDA(cudaEventRecord(e1, ds->stream));
+    SPWS_CUDA(cudaEventSynchronize(e1));
+    SPWS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  spws::dfree(sink, ds->stream);
+  const double flops = 2.0 * 8.0 * iters * (double)threads * (double)blocks;
+  *gflops = ms > 0.f ? flops / ((double)ms * 1e-3) / 1e9 : 0.0;
+  return SPWS_OK;
+}
+
 int spws_flush_l2(size_t bytes) {
   spws::DeviceState* ds = nullptr;
   SPWS_TRY(spws::device_state(&ds));
