@@ -214,6 +214,7 @@ __device__ __forceinline__ int claim_or_yield(int* counter, const PassArgs& a, u
 constexpr int kPieceLen = 256;   // B entries per warp work piece of a long slice
 constexpr int kLongMin = 128;    // default: slices this long are cut into pieces; shorter ones are packed
 constexpr int kLongMinMax = 256; // packed stream length < 512 * 256 fits the 17-bit field of fill_batch
+static_assert(kThreads * (kLongMinMax - 1) < (1 << 17), "short slices (< long_min entries) fill at most 17 bits");
 constexpr int kChunkLen = 128;   // packed entries per warp work item (4 rounds of 32 lanes)
 
 // Shared staging of one batch of j's. Every thread t loads one B-row slice
