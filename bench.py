@@ -372,6 +372,10 @@ def bench_spws(args, ws, rank, local, dist):
     fp64 = C.c_double(0.0)
     fp64_peak = fp64.value if L.spws_measure_fp64(C.byref(fp64)) == 0 and fp64.value > 0 else None
     peak, peak_src = measured_peaks()
+    ceilings = {"hbm": alg_bytes / (peak * 1e9) * 1e3}
+    if fp64_peak:
+        ceilings["fp64_fma"] = 2.0 * products / (fp64_peak * 1e9) * 1e3
+        ceilings["fp64_mul_add"] = 4.0 * products / (fp64_peak * 1e9) * 1e3
     achieved = alg_bytes / (ms_num * 1e-3) / 1e9
     dev_flops = 2.0 * products / (ms_dev * 1e-3) / 1e9
 
@@ -435,12 +439,13 @@ def bench_spws(args, ws, rank, local, dist):
                      "frac": achieved / peak, "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "traffic": profiled_traffic(args.workload),
-                     # the ceiling is max(bytes / BW, flops / FP64 peak); which term binds
+                     # the ceiling is max(bytes / BW, flops / FP64 peak); which term binds. The FP64
+                     # peak counts an FMA as two flops; a product summed by an atomic add is a
+                     # multiply and an add, two FP64 instructions, so its floor is twice that.
                      "fp64_peak_gflops": fp64_peak,
-                     "ceiling_ms": {"hbm": alg_bytes / (peak * 1e9) * 1e3,
-                                    "fp64": (2.0 * products / (fp64_peak * 1e9) * 1e3) if fp64_peak else None},
-                     "binding": ("hbm" if not fp64_peak or alg_bytes / (peak * 1e9) >= 2.0 * products /
-                                 (fp64_peak * 1e9) else "fp64"),
+                     "ceiling_ms": ceilings,
+                     "binding": max(ceilings, key=lambda k: ceilings[k] or 0.0),
+                     "frac_of_binding_ceiling": max(v or 0.0 for v in ceilings.values()) / ms_num,
                      # A, B and C read or written once each: the floor L2 reuse of B cannot beat
                      "compulsory_bytes": compulsory,
                      "compulsory_gbs": compulsory / (ms_dev * 1e-3) / 1e9},
