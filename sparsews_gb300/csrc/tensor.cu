@@ -71,16 +71,17 @@ __global__ void k_leaf_fiber(int32_t nf, const int32_t* __restrict__ pos2, int32
   for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) leaf_fib[p] = (int32_t)f;
 }
 
-// Bucket keys: MTTKRP buckets by the leaf coordinate, TTM by (root, leaf).
+// Bucket keys: MTTKRP buckets by the leaf coordinate, TTM by (root, leaf)
+// packed as (root << leaf_bits) | leaf.
 __global__ void k_keys(int64_t nnz, int mode, const int32_t* __restrict__ crd2, const int32_t* __restrict__ leaf_fib,
-                       const int32_t* __restrict__ fib_root, int32_t dim_leaf, unsigned long long* __restrict__ keys,
+                       const int32_t* __restrict__ fib_root, int leaf_bits, unsigned long long* __restrict__ keys,
                        unsigned long long* __restrict__ pay) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nnz) return;
   if (mode == 0)
     keys[p] = (unsigned long long)crd2[p];
   else
-    keys[p] = (unsigned long long)fib_root[leaf_fib[p]] * (unsigned long long)dim_leaf + (unsigned long long)crd2[p];
+    keys[p] = ((unsigned long long)fib_root[leaf_fib[p]] << leaf_bits) | (unsigned long long)crd2[p];
   pay[p] = (unsigned long long)p;
 }
 
@@ -257,7 +258,7 @@ __global__ void k_seg_counts(int64_t nseg, const uint32_t* __restrict__ segmask,
 
 // Warp per segment: write (coordinates, value) for every present column.
 __global__ void k_write(int64_t nseg, int mode, const unsigned long long* __restrict__ skeys,
-                        const long long* __restrict__ starts, int32_t dim_leaf, const double* __restrict__ segval,
+                        const long long* __restrict__ starts, int leaf_bits, const double* __restrict__ segval,
                         const uint32_t* __restrict__ segmask, int32_t R, int32_t mw, const long long* __restrict__ off,
                         int32_t* __restrict__ o0, int32_t* __restrict__ o1, int32_t* __restrict__ o2,
                         double* __restrict__ ov) {
@@ -275,8 +276,8 @@ __global__ void k_write(int64_t nseg, int mode, const unsigned long long* __rest
         o0[p] = (int32_t)key;
         o1[p] = j;
       } else {
-        o0[p] = (int32_t)(key / (unsigned long long)dim_leaf);
-        o1[p] = (int32_t)(key % (unsigned long long)dim_leaf);
+        o0[p] = (int32_t)(key >> leaf_bits);
+        o1[p] = (int32_t)(key & ((1ull << leaf_bits) - 1ull));
         o2[p] = j;
       }
       ov[p] = segval[s * (int64_t)R + j];
@@ -371,17 +372,18 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   SPWS_TRY(alloc(k1, kb, s));
   SPWS_TRY(alloc(p1, kb, s));
   const unsigned gn = (unsigned)((nnz + 255) / 256);
+  // bucket keys: the leaf coordinate (MTTKRP), or (root << leaf_bits) | leaf
+  // (TTM), decoded with a shift and a mask
+  const int leaf_bits = bits_for((unsigned long long)std::max(B.d2, 1));
   if (nnz > 0) {
-    k_keys<<<gn, 256, 0, s>>>(nnz, mode, B.crd2, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), B.d2,
+    k_keys<<<gn, 256, 0, s>>>(nnz, mode, B.crd2, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), leaf_bits,
                               k0.as<unsigned long long>(), p0.as<unsigned long long>());
     count_launch(1);
   }
-  const unsigned long long keyspace =
-      mode == 0 ? (unsigned long long)std::max(B.d2, 1)
-                : (unsigned long long)std::max(B.d0, 1) * (unsigned long long)std::max(B.d2, 1);
+  const int key_bits = mode == 0 ? leaf_bits : bits_for((unsigned long long)std::max(B.d0, 1)) + leaf_bits;
   bool in_tmp = false;
   SPWS_TRY(radix_sort_pairs(k0.as<unsigned long long>(), p0.as<unsigned long long>(), k1.as<unsigned long long>(),
-                            p1.as<unsigned long long>(), nnz, bits_for(keyspace), &in_tmp, s));
+                            p1.as<unsigned long long>(), nnz, key_bits, &in_tmp, s));
   const unsigned long long* sk = in_tmp ? k1.as<unsigned long long>() : k0.as<unsigned long long>();
   const unsigned long long* perm = in_tmp ? p1.as<unsigned long long>() : p0.as<unsigned long long>();
   SPWS_TRY(alloc(r0, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
@@ -480,7 +482,7 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   for (int d = 0; d < ncrd; d++) SPWS_TRY(dalloc((void**)&out->crd[d], sizeof(int32_t) * (size_t)std::max(total, 1LL), s));
   SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max(total, 1LL), s));
   if (nseg > 0) {
-    k_write<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, mode, sk, starts.as<long long>(), B.d2,
+    k_write<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, mode, sk, starts.as<long long>(), leaf_bits,
                                                        segval.as<double>(), segmask.as<uint32_t>(), R, mw,
                                                        segoff.as<long long>(), out->crd[0], out->crd[1],
                                                        mode == 0 ? nullptr : out->crd[2], out->vals);
