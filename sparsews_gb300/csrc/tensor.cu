@@ -72,17 +72,50 @@ __global__ void k_leaf_fiber(int32_t nf, const int32_t* __restrict__ pos2, int32
 }
 
 // Bucket keys: MTTKRP buckets by the leaf coordinate, TTM by (root, leaf)
-// packed as (root << leaf_bits) | leaf.
+// packed as (root << leaf_bits) | leaf. When `packed` is set (the bucket key
+// and the leaf's factor rows each fit 32 bits) the key's upper half carries
+// the factor rows (MTTKRP: root << r1_bits | level-1 coordinate; TTM: the
+// level-1 coordinate) and the payload the value, so the sort itself brings
+// every sorted leaf what it needs and no gather by permutation follows; the
+// sort only ranks the low key_bits bits. Otherwise the payload is the leaf's
+// position, for k_gather.
 __global__ void k_keys(int64_t nnz, int mode, const int32_t* __restrict__ crd2, const int32_t* __restrict__ leaf_fib,
-                       const int32_t* __restrict__ fib_root, int leaf_bits, unsigned long long* __restrict__ keys,
-                       unsigned long long* __restrict__ pay) {
+                       const int32_t* __restrict__ fib_root, int leaf_bits, int packed, int r1_bits,
+                       const int32_t* __restrict__ crd1, const double* __restrict__ vals,
+                       unsigned long long* __restrict__ keys, unsigned long long* __restrict__ pay) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nnz) return;
-  if (mode == 0)
-    keys[p] = (unsigned long long)crd2[p];
-  else
-    keys[p] = ((unsigned long long)fib_root[leaf_fib[p]] << leaf_bits) | (unsigned long long)crd2[p];
-  pay[p] = (unsigned long long)p;
+  const int32_t f = leaf_fib[p];
+  unsigned long long k = mode == 0 ? (unsigned long long)crd2[p]
+                                   : ((unsigned long long)fib_root[f] << leaf_bits) | (unsigned long long)crd2[p];
+  if (packed) {
+    const unsigned long long up = mode == 0
+                                      ? ((unsigned long long)fib_root[f] << r1_bits) | (unsigned long long)crd1[f]
+                                      : (unsigned long long)crd1[f];
+    k |= up << 32;
+    pay[p] = (unsigned long long)__double_as_longlong(vals[p]);
+  } else {
+    pay[p] = (unsigned long long)p;
+  }
+  keys[p] = k;
+}
+
+// Per sorted leaf, from a packed key and its value payload: the factor rows
+// and the value (the packed counterpart of k_gather).
+__global__ void k_unpack(int64_t nnz, int mode, const unsigned long long* __restrict__ skeys,
+                         const unsigned long long* __restrict__ spay, int r1_bits, int32_t* __restrict__ r0,
+                         int32_t* __restrict__ r1, double* __restrict__ b) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nnz) return;
+  const unsigned long long up = skeys[q] >> 32;
+  if (mode == 0) {
+    r0[q] = (int32_t)(up >> r1_bits);
+    r1[q] = (int32_t)(up & ((1ull << r1_bits) - 1ull));
+  } else {
+    r0[q] = (int32_t)up;
+    r1[q] = 0;
+  }
+  b[q] = __longlong_as_double((long long)spay[q]);
 }
 
 // Per sorted leaf: the two factor rows it multiplies and its value.
@@ -105,10 +138,12 @@ __global__ void k_gather(int64_t nnz, int mode, const unsigned long long* __rest
   b[q] = vals[p];
 }
 
-__global__ void k_heads(int64_t n, const unsigned long long* __restrict__ keys, int32_t* __restrict__ head) {
+// Bucket heads; keys compare on their low bucket bits (`mask`).
+__global__ void k_heads(int64_t n, const unsigned long long* __restrict__ keys, unsigned long long mask,
+                        int32_t* __restrict__ head) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  head[p] = (p == 0 || keys[p] != keys[p - 1]) ? 1 : 0;
+  head[p] = (p == 0 || ((keys[p] ^ keys[p - 1]) & mask) != 0) ? 1 : 0;
 }
 
 __global__ void k_starts(int64_t n, const int32_t* __restrict__ head, const long long* __restrict__ hpos,
@@ -258,14 +293,15 @@ __global__ void k_seg_counts(int64_t nseg, const uint32_t* __restrict__ segmask,
 
 // Warp per segment: write (coordinates, value) for every present column.
 __global__ void k_write(int64_t nseg, int mode, const unsigned long long* __restrict__ skeys,
-                        const long long* __restrict__ starts, int leaf_bits, const double* __restrict__ segval,
+                        const long long* __restrict__ starts, int leaf_bits, unsigned long long kmask,
+                        const double* __restrict__ segval,
                         const uint32_t* __restrict__ segmask, int32_t R, int32_t mw, const long long* __restrict__ off,
                         int32_t* __restrict__ o0, int32_t* __restrict__ o1, int32_t* __restrict__ o2,
                         double* __restrict__ ov) {
   const int lane = threadIdx.x & 31;
   const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= nseg) return;
-  const unsigned long long key = skeys[starts[s]];
+  const unsigned long long key = skeys[starts[s]] & kmask;
   long long at = off[s];
   for (int w = 0; w < mw; w++) {
     const uint32_t m = segmask[s * (int64_t)mw + w];
@@ -375,12 +411,17 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   // bucket keys: the leaf coordinate (MTTKRP), or (root << leaf_bits) | leaf
   // (TTM), decoded with a shift and a mask
   const int leaf_bits = bits_for((unsigned long long)std::max(B.d2, 1));
+  const int key_bits = mode == 0 ? leaf_bits : bits_for((unsigned long long)std::max(B.d0, 1)) + leaf_bits;
+  const int r1_bits = bits_for((unsigned long long)std::max(B.d1, 1));
+  const int up_bits = mode == 0 ? bits_for((unsigned long long)std::max(B.d0, 1)) + r1_bits : r1_bits;
+  const bool packed = key_bits <= 32 && up_bits <= 32;
+  const unsigned long long kmask = key_bits >= 64 ? ~0ull : (1ull << key_bits) - 1ull;
   if (nnz > 0) {
     k_keys<<<gn, 256, 0, s>>>(nnz, mode, B.crd2, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), leaf_bits,
-                              k0.as<unsigned long long>(), p0.as<unsigned long long>());
+                              packed ? 1 : 0, r1_bits, B.crd1, B.vals, k0.as<unsigned long long>(),
+                              p0.as<unsigned long long>());
     count_launch(1);
   }
-  const int key_bits = mode == 0 ? leaf_bits : bits_for((unsigned long long)std::max(B.d0, 1)) + leaf_bits;
   bool in_tmp = false;
   SPWS_TRY(radix_sort_pairs(k0.as<unsigned long long>(), p0.as<unsigned long long>(), k1.as<unsigned long long>(),
                             p1.as<unsigned long long>(), nnz, key_bits, &in_tmp, s));
@@ -393,9 +434,12 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   SPWS_TRY(alloc(hpos, sizeof(long long) * (size_t)std::max<int64_t>(nnz, 1), s));
   SPWS_TRY(alloc(starts, sizeof(long long) * ((size_t)nnz + 1), s));
   if (nnz > 0) {
-    k_gather<<<gn, 256, 0, s>>>(nnz, mode, perm, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), B.crd1, B.vals,
-                                r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>());
-    k_heads<<<gn, 256, 0, s>>>(nnz, sk, head.as<int32_t>());
+    if (packed)
+      k_unpack<<<gn, 256, 0, s>>>(nnz, mode, sk, perm, r1_bits, r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>());
+    else
+      k_gather<<<gn, 256, 0, s>>>(nnz, mode, perm, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), B.crd1, B.vals,
+                                  r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>());
+    k_heads<<<gn, 256, 0, s>>>(nnz, sk, kmask, head.as<int32_t>());
     count_launch(2);
   }
   SPWS_TRY(scan_i32_to_i64(head.as<int32_t>(), hpos.as<long long>(), nnz, tot.as<long long>(), s));
@@ -482,7 +526,7 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   for (int d = 0; d < ncrd; d++) SPWS_TRY(dalloc((void**)&out->crd[d], sizeof(int32_t) * (size_t)std::max(total, 1LL), s));
   SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max(total, 1LL), s));
   if (nseg > 0) {
-    k_write<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, mode, sk, starts.as<long long>(), leaf_bits,
+    k_write<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, mode, sk, starts.as<long long>(), leaf_bits, kmask,
                                                        segval.as<double>(), segmask.as<uint32_t>(), R, mw,
                                                        segoff.as<long long>(), out->crd[0], out->crd[1],
                                                        mode == 0 ? nullptr : out->crd[2], out->vals);
