@@ -176,6 +176,46 @@ struct Factor {
   int32_t rows, R, mw;
 };
 
+// Output written straight from the bucket sums (o0 == nullptr: not used).
+// When every factor row the tensor can reach holds all R columns, every
+// bucket has all R outputs, so bucket s's column j is entry s * R + j of the
+// sorted COO and no presence masks, counts, scan or separate write pass are
+// needed. Coordinates come from the bucket's sort key.
+struct DirectOut {
+  int32_t* o0;
+  int32_t* o1;
+  int32_t* o2;
+  double* ov;
+  const unsigned long long* skeys;
+  const long long* starts;
+  unsigned long long kmask;
+  int leaf_bits;
+};
+
+__device__ __forceinline__ void direct_write(const DirectOut& d, int mode, int64_t sg, int32_t R, int j, double v) {
+  const unsigned long long key = d.skeys[d.starts[sg]] & d.kmask;
+  const int64_t p = sg * (int64_t)R + j;
+  if (mode == 0) {
+    d.o0[p] = (int32_t)key;
+    d.o1[p] = j;
+  } else {
+    d.o0[p] = (int32_t)(key >> d.leaf_bits);
+    d.o1[p] = (int32_t)(key & ((1ull << d.leaf_bits) - 1ull));
+    d.o2[p] = j;
+  }
+  d.ov[p] = v;
+}
+
+// *notfull = 1 if some row among the first `rows` lacks one of its R columns.
+__global__ void k_all_present(int32_t rows, int32_t R, int32_t mw, const uint32_t* __restrict__ mask,
+                              int* __restrict__ notfull) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)rows * mw) return;
+  const int w = (int)(t % mw);
+  const uint32_t want = (w < mw - 1 || R % 32 == 0) ? 0xffffffffu : ((1u << (R % 32)) - 1u);
+  if ((mask[t] & want) != want) atomicExch(notfull, 1);
+}
+
 // Warp per piece: left-to-right FP64 sums of the piece's leaves for output
 // columns [j0, j0 + 32 * JPL) (lane handles j0 + lane + 32u, u < JPL). MTTKRP
 // forms (b * C(k,j)) * D(l,j) (hash_free.h:307), TTM forms b * C(i,l)
@@ -188,7 +228,8 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
                          const long long* __restrict__ starts, const int32_t* __restrict__ r0,
                          const int32_t* __restrict__ r1, const double* __restrict__ bv, Factor F0, Factor F1, int32_t R,
                          int32_t j0, int32_t mw, int32_t pw, double* __restrict__ partial,
-                         uint32_t* __restrict__ pmask, double* __restrict__ segval, uint32_t* __restrict__ segmask) {
+                         uint32_t* __restrict__ pmask, double* __restrict__ segval, uint32_t* __restrict__ segmask,
+                         DirectOut direct) {
   const int lane = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= npieces) return;
@@ -246,7 +287,9 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
     const int j = j0 + lane + 32 * u;
     const bool in = j < R;
     const unsigned m = __ballot_sync(0xffffffffu, in && ((started >> u) & 1u));  // all lanes, one call site
-    if (single) {
+    if (single && direct.o0) {
+      if (in) direct_write(direct, MODE, sg, R, j, acc[u]);
+    } else if (single) {
       if (in) segval[sg * (int64_t)R + j] = acc[u];
       if (lane == 0 && (j0 / 32 + u) < mw) segmask[sg * (int64_t)mw + j0 / 32 + u] = m;
     } else {
@@ -259,9 +302,10 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
 // Warp per segment: add the pieces' partials in piece order into the
 // segment's running values for this column tile (first present value
 // assigns, later ones add), and accumulate the presence mask.
-__global__ void k_combine(int64_t nseg, const long long* __restrict__ poff, const double* __restrict__ partial,
-                          const uint32_t* __restrict__ pmask, int32_t R, int32_t j0, int32_t mw, int32_t pw,
-                          double* __restrict__ segval, uint32_t* __restrict__ segmask) {
+__global__ void k_combine(int64_t nseg, int mode, const long long* __restrict__ poff,
+                          const double* __restrict__ partial, const uint32_t* __restrict__ pmask, int32_t R, int32_t j0,
+                          int32_t mw, int32_t pw, double* __restrict__ segval, uint32_t* __restrict__ segmask,
+                          DirectOut direct) {
   const int lane = threadIdx.x & 31;
   const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (s >= nseg || poff[s + 1] - poff[s] == 1) return;  // one piece: k_pieces wrote it
@@ -276,6 +320,10 @@ __global__ void k_combine(int64_t nseg, const long long* __restrict__ poff, cons
         v = have ? __dadd_rn(v, x) : x;
         have = true;
       }
+    }
+    if (direct.o0) {
+      if (j < R && u < pw) direct_write(direct, mode, s, R, j, v);
+      continue;
     }
     if (j < R) segval[s * (int64_t)R + j] = v;
     const unsigned m = __ballot_sync(0xffffffffu, have && j < R);
@@ -390,7 +438,7 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   for (auto& c : out->crd) c = nullptr;
   out->vals = nullptr;
   DevArr fib_root, leaf_fib, k0, p0, k1, p1, r0, r1, bv, head, hpos, starts, pc, poff, pseg, pstart, partial, pmask,
-      segval, segmask, segcnt, segoff, tot;
+      segval, segmask, segcnt, segoff, tot, notfull;
   SPWS_TRY(alloc(fib_root, sizeof(int32_t) * (size_t)B.nf, s));
   SPWS_TRY(alloc(leaf_fib, sizeof(int32_t) * (size_t)nnz, s));
   SPWS_TRY(alloc(tot, sizeof(long long), s));
@@ -447,10 +495,31 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
     k_starts<<<gn, 256, 0, s>>>(nnz, head.as<int32_t>(), hpos.as<long long>(), starts.as<long long>());
     count_launch(1);
   }
+  // Do the factors hold every column of every row the tensor can reach?
+  // (MTTKRP: C over the roots, D over the level-1 coordinates; TTM: C over
+  // the level-1 coordinates.) Then every bucket has all R outputs.
+  SPWS_TRY(alloc(notfull, sizeof(int), s));
+  SPWS_CUDA(cudaMemsetAsync(notfull.p, 0, sizeof(int), s));
+  const int32_t need0 = mode == 0 ? B.d0 : B.d1;
+  bool reach = R > 0 && F0.rows >= need0 && (mode != 0 || F1->rows >= B.d1);
+  if (reach) {
+    auto check = [&](const FactorDense& F) {
+      const int64_t words = (int64_t)F.rows * F.mw;
+      if (words > 0) {
+        k_all_present<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(F.rows, R, F.mw, F.mask, notfull.as<int>());
+        count_launch(1);
+      }
+    };
+    check(F0);
+    if (mode == 0) check(*F1);
+  }
   long long nseg = 0;
+  int hnotfull = 1;
   Readback rb(s);
   SPWS_TRY(rb.get(&nseg, tot.p, sizeof(long long)));
+  SPWS_TRY(rb.get(&hnotfull, notfull.p, sizeof(int)));
   SPWS_TRY(rb.wait());
+  const bool direct_out = reach && hnotfull == 0 && (long long)nseg * R <= INT32_MAX;
   SPWS_TRY(store_i64(starts.as<long long>() + nseg, nnz, s));
 
   SPWS_TRY(alloc(pc, sizeof(int32_t) * (size_t)std::max<long long>(nseg, 1), s));
@@ -476,8 +545,20 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   const int32_t pw = std::min(kTileR / 32, mw);
   SPWS_TRY(alloc(partial, sizeof(double) * (size_t)std::max<long long>(npieces, 1) * 32 * pw, s));
   SPWS_TRY(alloc(pmask, sizeof(uint32_t) * (size_t)std::max<long long>(npieces, 1) * pw, s));
-  SPWS_TRY(alloc(segval, sizeof(double) * (size_t)std::max<long long>(nseg, 1) * std::max(R, 1), s));
-  SPWS_TRY(alloc(segmask, sizeof(uint32_t) * (size_t)std::max<long long>(nseg, 1) * mw, s));
+  DirectOut direct{};
+  const int ncrd = mode == 0 ? 2 : 3;
+  if (direct_out) {  // every bucket has all R outputs: the COO is nseg * R entries, written by the sum kernels
+    const long long total = (long long)nseg * R;
+    out->n = total;
+    for (int d = 0; d < ncrd; d++)
+      SPWS_TRY(dalloc((void**)&out->crd[d], sizeof(int32_t) * (size_t)std::max(total, 1LL), s));
+    SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max(total, 1LL), s));
+    direct = DirectOut{out->crd[0], out->crd[1], mode == 0 ? nullptr : out->crd[2], out->vals, sk,
+                       starts.as<long long>(), kmask, leaf_bits};
+  } else {
+    SPWS_TRY(alloc(segval, sizeof(double) * (size_t)std::max<long long>(nseg, 1) * std::max(R, 1), s));
+    SPWS_TRY(alloc(segmask, sizeof(uint32_t) * (size_t)std::max<long long>(nseg, 1) * mw, s));
+  }
   Factor f0{F0.dense, F0.mask, F0.rows, F0.R, F0.mw};
   Factor f1 = F1 ? Factor{F1->dense, F1->mask, F1->rows, F1->R, F1->mw} : f0;
   for (int32_t j0 = 0; j0 < R; j0 += kTileR) {
@@ -488,7 +569,7 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
         kernel<<<gp, 256, 0, s>>>(npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
                                   r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw, pw,
                                   partial.as<double>(), pmask.as<uint32_t>(), segval.as<double>(),
-                                  segmask.as<uint32_t>());
+                                  segmask.as<uint32_t>(), direct);
       };
       if (mode == 0) {
         if (jpl <= 1) launch(k_pieces<0, 1>);
@@ -501,11 +582,16 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
         else if (jpl == 4) launch(k_pieces<1, 4>);
         else launch(k_pieces<1, 8>);
       }
-      k_combine<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, poff.as<long long>(), partial.as<double>(),
+      k_combine<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, mode, poff.as<long long>(), partial.as<double>(),
                                                            pmask.as<uint32_t>(), R, j0, mw, pw, segval.as<double>(),
-                                                           segmask.as<uint32_t>());
+                                                           segmask.as<uint32_t>(), direct);
       count_launch(2);
     }
+  }
+  if (direct_out) {
+    SPWS_CUDA(cudaGetLastError());
+    SPWS_CUDA(cudaStreamSynchronize(s));
+    return SPWS_OK;
   }
   SPWS_TRY(alloc(segcnt, sizeof(int32_t) * (size_t)std::max<long long>(nseg, 1), s));
   SPWS_TRY(alloc(segoff, sizeof(long long) * (size_t)std::max<long long>(nseg, 1), s));
@@ -522,7 +608,6 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
     return SPWS_ERR_CAPACITY;
   }
   out->n = total;
-  const int ncrd = mode == 0 ? 2 : 3;
   for (int d = 0; d < ncrd; d++) SPWS_TRY(dalloc((void**)&out->crd[d], sizeof(int32_t) * (size_t)std::max(total, 1LL), s));
   SPWS_TRY(dalloc((void**)&out->vals, sizeof(double) * (size_t)std::max(total, 1LL), s));
   if (nseg > 0) {
