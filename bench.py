@@ -803,6 +803,15 @@ def bench_tensor(args):
         alg = 12 * nnz + 8 * (nslices + nfibers + 2) + 8 * R * d2 + 20 * n_out
     bw, peak_src = measured_peaks()
     achieved = alg / (ms_dev * 1e-3) / 1e9
+    # FP64 term: the bucket sums are (b*C)*D + acc (MTTKRP) and b*C + acc (TTM) per
+    # leaf and column, kept as separate multiplies and adds for the reference's
+    # rounding: 3 or 2 FP64 instructions, against the FMA peak's two flops each
+    fp64 = C.c_double(0.0)
+    fp64_peak = fp64.value if L.spws_measure_fp64(C.byref(fp64)) == 0 and fp64.value > 0 else None
+    ops = (3.0 if args.workload == "mttkrp" else 2.0) * R * nnz
+    ceilings = {"hbm": alg / (bw * 1e9) * 1e3}
+    if fp64_peak:
+        ceilings["fp64_instructions"] = ops / (fp64_peak / 2.0 * 1e9) * 1e3
     line = {"metric": f"{args.workload}_gflops", "value": flops / wall / 1e9, "unit": "GFLOP/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zipf tensor)",
@@ -813,7 +822,10 @@ def bench_tensor(args):
             "roofline": {"bound": "hbm", "kernel": "tensor_bucket (whole call: sort, bucket sums, output)",
                          "achieved": achieved, "peak": bw, "unit": "GB/s",
                          "frac": achieved / bw, "peak_source": peak_src,
-                         "algorithmic_bytes_per_launch": alg, "traffic": None},
+                         "algorithmic_bytes_per_launch": alg, "traffic": None,
+                         "fp64_peak_gflops": fp64_peak, "ceiling_ms": ceilings,
+                         "binding": max(ceilings, key=lambda k: ceilings[k]),
+                         "frac_of_binding_ceiling": max(ceilings.values()) / ms_dev},
             "gpu_launches": launches, "clocks": clk.summary(), "generation_s": gen_s}
     print(json.dumps(line), flush=True)
 
