@@ -217,3 +217,42 @@ def test_light_rows_bit_exact(spws_lib, shape):
     ref = oracle.spgemm("hash", A, Bm, w_cap=1 << 24)
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
     assert np.array_equal(got[2], ref[2])
+
+
+def test_light_tier_boundaries_and_single_column(spws_lib):
+    """Rows whose product counts sit on the light tiers' edges (127/128,
+    255/256, 511/512 products: the hash kernel, the two staged-sort tiers and
+    the CTA kernels), empty rows between them, and rows whose every product
+    lands on one column (a whole round of 32 lanes holding the same column):
+    structure and values bit-exact with the reference's sequential sums."""
+    import sparsews_gb300 as sp
+    rng = np.random.default_rng(66)
+    m = 2048
+    # B: row j has exactly one entry at column 7 for j < 600, else 8 random columns
+    brows, bcols = [], []
+    for j in range(m):
+        cs = [7] if j < 600 else sorted(rng.choice(m, 8, replace=False))
+        brows += [j] * len(cs)
+        bcols += list(cs)
+    bpos = np.zeros(m + 1, np.int64)
+    np.add.at(bpos, np.array(brows) + 1, 1)
+    B = (np.cumsum(bpos).astype(np.int32), np.array(bcols, np.int32), rng.uniform(-1, 1, len(bcols)), m, m)
+    rows = []
+    for P in (127, 128, 255, 256, 511, 512, 0, 1, 31, 32, 33):  # products per row via 8-entry B rows
+        k = P // 8
+        rows.append(sorted(rng.choice(np.arange(600, m), k, replace=False)) if k else [])
+    for k in (1, 32, 100, 127, 128, 255, 256, 300, 511, 512):  # one-column rows: k products on column 7
+        rows.append(sorted(rng.choice(600, k, replace=False)))
+    apos = np.zeros(len(rows) + 1, np.int64)
+    apos[1:] = np.cumsum([len(r) for r in rows])
+    acol = np.array([c for r in rows for c in r], np.int32)
+    A = (apos.astype(np.int32), acol, rng.uniform(-1, 1, len(acol)), len(rows), m)
+    got = sp.spgemm(A, B)
+    ref = oracle.spgemm("hash", A, B, w_cap=1 << 24)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    # rows under 512 products are light (bit-exact); heavier ones sum with atomics
+    prods = np.array([8 * len(r) if (len(r) == 0 or r[0] >= 600) else len(r) for r in rows])
+    for i in np.nonzero(prods < 512)[0]:
+        s, e = got[0][i], got[0][i + 1]
+        assert np.array_equal(got[2][s:e], ref[2][s:e]), f"row {i} ({prods[i]} products)"
+    assert_csr_close(got, ref, scale_of(A, B), "tier edges")
