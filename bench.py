@@ -461,19 +461,9 @@ def bench_spws(args, ws, rank, local, dist):
 
 # ------------------------------------------------------------------ batched form
 def batch_workload(count, seed=42):
-    """The batched config: n_i log-uniform in [256, 65536], Poisson(8)
-    distinct columns per row; even instances uniform, odd ones R-MAT
-    (a, b, c = .57, .19, .19). Seeded per instance."""
+    """The batched config (sparsews_gb300.gen.batch_instances)."""
     from sparsews_gb300 import gen
-    rng = np.random.default_rng(seed)
-    ns = np.exp(rng.uniform(np.log(256), np.log(65536), count)).astype(np.int64)
-    out = []
-    for t, n in enumerate(ns):
-        if t % 2 == 0:
-            out.append(gen.poisson_rows(int(n), 8.0, seed=seed * 100003 + t))
-        else:
-            out.append(gen.rmat_n(int(n), 8.0, seed=seed * 100003 + t))
-    return out
+    return gen.batch_instances(count, seed)
 
 
 def bench_batched(args):

@@ -172,3 +172,18 @@ def csr_transpose(pos, crd, vals, nrow, ncol):
     tpos = np.zeros(ncol + 1, np.int64)
     np.add.at(tpos, cols + 1, 1)
     return np.cumsum(tpos).astype(np.int32), rows[order].astype(np.int32), np.asarray(vals)[order]
+
+
+def batch_instances(count, seed=42):
+    """The batched config: n_i log-uniform in [256, 65536], Poisson(8)
+    distinct columns per row; even instances uniform, odd ones R-MAT
+    (a, b, c = .57, .19, .19). Seeded per instance."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(256), np.log(65536), count)).astype(np.int64)
+    out = []
+    for t, n in enumerate(ns):
+        if t % 2 == 0:
+            out.append(poisson_rows(int(n), 8.0, seed=seed * 100003 + t))
+        else:
+            out.append(rmat_n(int(n), 8.0, seed=seed * 100003 + t))
+    return out

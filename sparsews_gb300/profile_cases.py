@@ -6,6 +6,7 @@ not exercise, for profiling one kernel family at a time under ncu:
     python -m sparsews_gb300.profile_cases ttm       # tensor bucket kernel, mode 1
     python -m sparsews_gb300.profile_cases outer     # DCSC x DCSR conversion + row-wise pipeline
     python -m sparsews_gb300.profile_cases transpose # (A*A)^T fused and non-fused (device transposes)
+    python -m sparsews_gb300.profile_cases batched   # the batched form on the 1024-instance workload
 
 Each case runs its call `--repeat` times (default 2: one warm-up, one to
 capture) on inputs larger than the L2 cache and prints one line of sizes.
@@ -18,7 +19,7 @@ import numpy as np
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["coord", "mttkrp", "ttm", "outer", "transpose"])
+    ap.add_argument("case", choices=["coord", "mttkrp", "ttm", "outer", "transpose", "batched"])
     ap.add_argument("--scale", type=int, default=15, help="transpose case: R-MAT scale")
     ap.add_argument("--repeat", type=int, default=2)
     args = ap.parse_args()
@@ -32,6 +33,14 @@ def main():
         for _ in range(args.repeat):
             C = sp.spgemm(A, A, "coord") if args.case == "coord" else sp.spgemm_outer(A, A, "hash")
         print(f"{args.case}: band 2^20, nnz(A) {len(A[1])}, nnz(C) {len(C[1])}, {time.perf_counter() - t0:.1f} s")
+        return
+    if args.case == "batched":
+        dev = [sp.DeviceCsr.upload(*A) for A in gen.batch_instances(1024)]
+        for _ in range(args.repeat):
+            b = sp.spgemm_batched(dev, dev)
+            print(f"batched: {b.stats.instances} instances, {b.stats.groups} groups, {b.stats.products} products, "
+                  f"kernels {b.stats.ms_kernels:.2f} ms, total {b.stats.ms_total:.2f} ms")
+            b.release()
         return
     if args.case == "transpose":
         A = gen.rmat(args.scale, 8, seed=42)
