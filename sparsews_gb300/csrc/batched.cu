@@ -105,20 +105,35 @@ __global__ void k_row_shift(int count, const Inst* __restrict__ ib, const long l
 
 // Products of each A row, summed per instance (an upper bound of the
 // instance's output nonzeros, used to cut the batch into int32-sized groups).
+// Thread per row; a warp's rows are consecutive, so each instance they touch
+// is a contiguous run of lanes: a segmented reduction within the warp leaves
+// the run's total on its first lane, and one atomic per run per warp goes to
+// the instance's counter (one atomic per row serialised on the few counters
+// of large instances: 6 ms for the 1024-instance batch).
 __global__ void k_inst_products(int count, const long long* __restrict__ row_offs, int32_t total_rows,
                                 const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
                                 const int32_t* __restrict__ Bp, unsigned long long* __restrict__ prods) {
   const int lane = threadIdx.x & 31;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= total_rows) return;
-  long long p = 0;
-  for (int32_t q = Ap[r] + lane; q < Ap[r + 1]; q += 32) {
-    const int32_t j = Aj[q];
-    p += Bp[j + 1] - Bp[j];
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = r < total_rows;
+  unsigned long long p = 0;
+  int inst = -1;
+  if (valid) {
+    for (int32_t q = Ap[r]; q < Ap[r + 1]; q++) {
+      const int32_t j = Aj[q];
+      p += (unsigned long long)(Bp[j + 1] - Bp[j]);
+    }
+    inst = find_inst(row_offs, count, r);
   }
+  // lane l ends with the sum over lanes [l, 32) of its own run
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-  if (lane == 0 && p) atomicAdd(&prods[find_inst(row_offs, count, r)], (unsigned long long)p);
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long op = __shfl_down_sync(0xffffffffu, p, o);
+    const int oi = __shfl_down_sync(0xffffffffu, inst, o);
+    if (lane + o < 32 && oi == inst) p += op;
+  }
+  const int prev = __shfl_up_sync(0xffffffffu, inst, 1);
+  if (valid && p && (lane == 0 || prev != inst)) atomicAdd(&prods[inst], p);
 }
 
 __global__ void k_zero_rows(int count, const Inst* __restrict__ ia, int first, int last,
@@ -272,7 +287,8 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
     SPWS_TRY(dalloc((void**)&dprod, sizeof(unsigned long long) * count, s));
     SPWS_CUDA(cudaMemsetAsync(dprod, 0, sizeof(unsigned long long) * count, s));
     if (ar > 0) {
-      k_inst_products<<<(unsigned)((ar + 7) / 8), 256, 0, s>>>(count, darow, (int32_t)ar, Ab.pos, Ab.crd, Bb.pos, dprod);
+      k_inst_products<<<(unsigned)((ar + 255) / 256), 256, 0, s>>>(count, darow, (int32_t)ar, Ab.pos, Ab.crd, Bb.pos,
+                                                                 dprod);
       count_launch(1);
     }
     SPWS_CUDA(cudaMemcpyAsync(iprod.data(), dprod, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, s));
