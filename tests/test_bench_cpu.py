@@ -1,0 +1,52 @@
+"""CPU tests of bench.py's host-side pieces: the CPU-baseline samplers (they
+run the oracle, the reference algorithm's restatement, on bounded samples)
+and the seeded workload generators the benchmarks and profiling cases share."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def test_cpu_instances_covers_target_and_balances_threads():
+    import bench
+    from sparsews_gb300 import gen
+    insts = [gen.poisson_rows(300 + 50 * t, 4.0, seed=t) for t in range(12)]
+    prods = [int(np.diff(A[0]).astype(np.int64)[A[1]].sum()) for A in insts]
+    k, p, secs = bench.cpu_instances(insts, 3, target_products=sum(prods) // 2)
+    assert 1 <= k <= len(insts) and secs > 0
+    assert p >= sum(prods) // 2 or k == len(insts)  # stops once the target is reached
+    k, p, _ = bench.cpu_instances(insts, 2, target_products=10 ** 12)
+    assert k == len(insts) and p == sum(prods)
+
+
+def test_cpu_sample_rows_reaches_target():
+    import bench
+    from sparsews_gb300 import gen
+    A = gen.rmat(9, 6, seed=3)
+    rows, prods = bench.cpu_sample_rows(A, 20000)
+    assert np.all(np.diff(rows) > 0)
+    assert prods >= 20000
+    sub = bench.sub_rows(A, rows)
+    assert sub[3] == len(rows) and sub[0][-1] == len(sub[1])
+
+
+def test_batch_generator_is_seeded_and_shaped():
+    from sparsews_gb300 import gen
+    a = gen.batch_instances(6, seed=5)
+    b = gen.batch_instances(6, seed=5)
+    assert len(a) == 6
+    for x, y in zip(a, b):
+        assert x[3] == y[3] and np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1])
+        assert 256 <= x[3] <= 65536 and x[3] == x[4]
+
+
+def test_transpose_suite_spans_output_sizes():
+    import bench
+    kinds = {k for k, _, _ in bench.TRANSPOSE_SUITE}
+    assert kinds == {"er", "rmat", "band"}
+    A, desc = bench.transpose_suite_matrix("er", 600, 3)
+    assert A[3] == 600 and desc["kind"] == "er"
+    assert bench.gstats([1.0, 4.0])["gmean"] == 2.0
