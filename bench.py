@@ -911,7 +911,8 @@ def bench_served(args):
     dfac = served.DeviceFactor(factor)
     pools = (len(dsmall), 1, len(dtens))
 
-    srv = served.Server(workers=args.served_workers, memory_budget=int(args.served_budget_gb * (1 << 30)))
+    srv = served.Server(workers=args.served_workers, memory_budget=int(args.served_budget_gb * (1 << 30)),
+                        slice_us=args.served_slice_us)
 
     def submit(r):
         k, i = r
@@ -982,6 +983,7 @@ def bench_served(args):
                        "mix": {"small_batched_size": SERVED_MIX[0], "rmat_2^18_deg16": SERVED_MIX[1],
                                "ttm_1M_5M_nnz_R32": SERVED_MIX[2]},
                        "small_pool": len(small), "workers": args.served_workers,
+                       "slice_us": args.served_slice_us or 500,
                        "memory_budget_gb": st.budget / (1 << 30), "arrivals": "Poisson at swept rates",
                        "l2": "inputs resident; R-MAT operands and outputs far larger than L2"},
             "p50_ms": runs[-1]["p50_ms"], "p99_ms": runs[-1]["p99_ms"], "runs": runs,
@@ -1059,6 +1061,8 @@ def main():
     ap.add_argument("--served-requests", type=int, default=400, help="served workload: requests per run")
     ap.add_argument("--served-pool", type=int, default=512, help="served workload: distinct small products")
     ap.add_argument("--served-workers", type=int, default=8)
+    ap.add_argument("--served-slice-us", type=int, default=0,
+                    help="served workload: time slice of large requests' row kernels (0: the server's 500 us)")
     ap.add_argument("--served-budget-gb", type=float, default=120.0)
     ap.add_argument("--served-rates", type=float, nargs="*", default=[0.5, 0.8],
                     help="Poisson arrival rates as fractions of the saturating throughput")
