@@ -537,8 +537,12 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
   for (int q = threadIdx.x; q < ACC; q += kThreads) acc[q] = 0.0;
   const int nwork = *a.nheavy;
   const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
+  // Rows are claimed one ahead: while row i is being summed, the stored
+  // bitmap of the row claimed next is prefetched into L2, so its load at the
+  // start of that row does not wait on DRAM.
+  int next = claim(a.counter, &s_idx, a, t0);
   for (;;) {
-    const int idx = claim(a.counter, &s_idx, a, t0);
+    const int idx = next;
     if (idx >= nwork) break;
     const int32_t i = a.order[idx];
     const RowInfo ri = a.info[i];
@@ -547,6 +551,7 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
     const int32_t row_end = a.Cp[i + 1];
     const int32_t shift = a.col_shift ? a.col_shift[i] : 0;
     int32_t out = a.Cp[i];
+    next = claim(a.counter, &s_idx, a, t0);
     for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
       const int32_t wlo = (int32_t)wl;
       const int nw = words_in(wl, ri.hi);
@@ -557,6 +562,16 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
 #pragma unroll 4
         for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = src[w];
         __syncthreads();
+        if (next < nwork) {  // one 128-byte line per thread and step
+          const int32_t ni = a.order[next];
+          const RowInfo nr = a.info[ni];
+          if ((long long)nr.hi - nr.lo + 1 <= kSpanBits) {
+            const uint32_t* nsrc = a.bmstore + a.bmoff[ni];
+            const int nwn = words_in(nr.lo, nr.hi);
+            for (int w = threadIdx.x * 32; w < nwn; w += kThreads * 32)
+              asm volatile("prefetch.global.L2 [%0];" ::"l"(nsrc + w));
+          }
+        }
       } else {
         for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = make_uint4(0u, 0u, 0u, 0u);
         __syncthreads();
