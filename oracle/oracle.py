@@ -21,6 +21,7 @@ from sparsews_gb300 import taco
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libspws_oracle.so")
+PORT_O0_SO = os.path.join(HERE, "libspws_oracle_O0.so")
 REF_SO = os.path.join(HERE, "_ref", "libspws_ref.so")
 REF_ROOT_DEFAULT = "/root/reference"
 
@@ -34,6 +35,17 @@ def build_port(force=False):
         subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-std=gnu11", "-fPIC", "-shared",
                                "-o", PORT_SO, src])
     return PORT_SO
+
+
+def build_port_o0(force=False):
+    """The same restatement compiled without optimisation (-O0 -g), the way
+    the reference's own Makefile builds its drivers: a labelled, secondary
+    CPU baseline."""
+    src = os.path.join(HERE, "spws_oracle.c")
+    if force or not os.path.exists(PORT_O0_SO) or os.path.getmtime(PORT_O0_SO) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-O0", "-g", "-ffp-contract=off", "-std=gnu11", "-fPIC", "-shared",
+                               "-o", PORT_O0_SO, src])
+    return PORT_O0_SO
 
 
 def build_ref(ref_root=None, force=False):
@@ -51,6 +63,9 @@ def _load(kind):
     if kind == "port":
         lib = C.CDLL(build_port())
         prefix = "ora_"
+    elif kind == "port_O0":
+        lib = C.CDLL(build_port_o0())
+        prefix = "ora_"
     elif kind == "ref":
         if not os.path.exists(REF_SO):
             raise FileNotFoundError("reference oracle not built (needs the reference checkout)")
@@ -61,7 +76,7 @@ def _load(kind):
     P = C.POINTER(taco.TacoTensor)
     names = [("csr_csr_hash", 3), ("dcsc_dcsr_hash", 3), ("dcsc_dcsr_coord", 3), ("dcsc_dcsr_bucket", 3),
              ("dcsc_dcsr_t_hash", 3), ("ttm_hash", 3), ("ttm_bucket", 3)]
-    if kind == "port":
+    if prefix == "ora_":
         names.append(("dcsc_dcsr_coord_faithful", 3))
     for name, nt in names:
         f = getattr(lib, prefix + name)
