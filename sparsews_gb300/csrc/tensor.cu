@@ -233,8 +233,10 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   const int lane = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= npieces) return;
+  const int64_t sg = pseg[w];
+  const long long s_beg = starts[sg], s_end = starts[sg + 1];
   const long long q0 = pstart[w];
-  const long long q1 = min(q0 + (long long)kPiece, starts[pseg[w] + 1]);
+  const long long q1 = min(q0 + (long long)kPiece, s_end);
   double acc[JPL];
   unsigned started = 0;
 #pragma unroll
@@ -280,15 +282,30 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   // A segment that is this one piece is final here: write its values and
   // presence straight into the segment arrays (what k_combine would copy);
   // k_combine handles only segments of several pieces.
-  const int64_t sg = pseg[w];
-  const bool single = q0 == starts[sg] && starts[sg + 1] - q0 <= (long long)kPiece;
+  const bool single = q0 == s_beg && s_end - q0 <= (long long)kPiece;
+  int32_t c0 = 0, c1 = 0;  // the bucket's output coordinates, decoded once from its sort key
+  if (single && direct.o0) {
+    const unsigned long long key = direct.skeys[s_beg] & direct.kmask;
+    c0 = MODE == 0 ? (int32_t)key : (int32_t)(key >> direct.leaf_bits);
+    c1 = MODE == 0 ? 0 : (int32_t)(key & ((1ull << direct.leaf_bits) - 1ull));
+  }
 #pragma unroll
   for (int u = 0; u < JPL; u++) {
     const int j = j0 + lane + 32 * u;
     const bool in = j < R;
     const unsigned m = __ballot_sync(0xffffffffu, in && ((started >> u) & 1u));  // all lanes, one call site
     if (single && direct.o0) {
-      if (in) direct_write(direct, MODE, sg, R, j, acc[u]);
+      if (in) {
+        const int64_t p = sg * (int64_t)R + j;
+        direct.o0[p] = c0;
+        if (MODE == 0) {
+          direct.o1[p] = j;
+        } else {
+          direct.o1[p] = c1;
+          direct.o2[p] = j;
+        }
+        direct.ov[p] = acc[u];
+      }
     } else if (single) {
       if (in) segval[sg * (int64_t)R + j] = acc[u];
       if (lane == 0 && (j0 / 32 + u) < mw) segmask[sg * (int64_t)mw + j0 / 32 + u] = m;
