@@ -316,6 +316,113 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   }
 }
 
+// The piece kernel for buckets of a few leaves (TTM: about two), rank at most
+// 32 (one column per lane), direct output only (single-piece buckets go
+// straight to the COO, split ones to the partial sums for k_combine): a warp
+// takes G consecutive pieces, whose leaves
+// are consecutive in the sorted order, loads their bounds and bucket data in
+// one go (lane k holds piece k's), streams the leaves 32 at a time and
+// writes a piece out when its last leaf is summed. Same sums in the same
+// order as k_pieces; the bucket set-up that dominated a two-leaf piece is
+// paid once per G pieces.
+template <int MODE>
+__global__ void k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const int32_t* __restrict__ pseg,
+                                 const long long* __restrict__ pstart, const long long* __restrict__ starts,
+                                 const int32_t* __restrict__ r0, const int32_t* __restrict__ r1,
+                                 const double* __restrict__ bv, Factor F0, Factor F1, int32_t R, int32_t mw,
+                                 int32_t pw, double* __restrict__ partial, uint32_t* __restrict__ pmask,
+                                 DirectOut direct) {
+  const int lane = threadIdx.x & 31;
+  const int64_t p0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * G;
+  if (p0 >= npieces) return;
+  const int np = (int)min((int64_t)G, npieces - p0);
+  // lane k (k <= np): piece p0+k's first leaf (k = np: the group's end), its
+  // bucket, the bucket's bounds, and the bucket's output coordinates
+  long long my_start = nleaves, my_sbeg = 0, my_send = 0;
+  int64_t my_sg = 0;
+  int32_t my_c0 = 0, my_c1 = 0;
+  if (lane <= np) my_start = p0 + lane < npieces ? pstart[p0 + lane] : nleaves;
+  if (lane < np) {
+    my_sg = pseg[p0 + lane];
+    my_sbeg = starts[my_sg];
+    my_send = starts[my_sg + 1];
+    if (direct.o0) {
+      const unsigned long long key = direct.skeys[my_sbeg] & direct.kmask;
+      my_c0 = MODE == 0 ? (int32_t)key : (int32_t)(key >> direct.leaf_bits);
+      my_c1 = MODE == 0 ? 0 : (int32_t)(key & ((1ull << direct.leaf_bits) - 1ull));
+    }
+  }
+  const long long L0 = __shfl_sync(0xffffffffu, my_start, 0), L1 = __shfl_sync(0xffffffffu, my_start, np);
+  const int j = lane;
+  const bool in = j < R;
+  int cp = 0;                                                 // current piece (0 .. np-1)
+  long long ce = __shfl_sync(0xffffffffu, my_start, 1);       // its end
+  double acc = 0.0;
+  bool started = false;
+  auto flush = [&]() {
+    const long long ps = __shfl_sync(0xffffffffu, my_start, cp);
+    const long long sb = __shfl_sync(0xffffffffu, my_sbeg, cp), se = __shfl_sync(0xffffffffu, my_send, cp);
+    const int64_t sg = __shfl_sync(0xffffffffu, my_sg, cp);
+    const int32_t c0 = __shfl_sync(0xffffffffu, my_c0, cp), c1 = __shfl_sync(0xffffffffu, my_c1, cp);
+    const unsigned m = __ballot_sync(0xffffffffu, in && started);
+    const bool single = ps == sb && se - ps <= (long long)kPiece;
+    if (single && direct.o0) {
+      if (in) {
+        const int64_t p = sg * (int64_t)R + j;
+        direct.o0[p] = c0;
+        if (MODE == 0) {
+          direct.o1[p] = j;
+        } else {
+          direct.o1[p] = c1;
+          direct.o2[p] = j;
+        }
+        direct.ov[p] = acc;
+      }
+    } else {
+      const int64_t w = p0 + cp;
+      if (in) partial[w * (int64_t)(32 * pw) + j] = acc;
+      if (lane == 0 && pw > 0) pmask[w * (int64_t)pw] = m;
+    }
+    acc = 0.0;
+    started = false;
+    cp++;
+    ce = __shfl_sync(0xffffffffu, my_start, min(cp + 1, np));
+  };
+  for (long long qb = L0; qb < L1; qb += 32) {
+    const long long q = qb + lane;
+    int32_t a0 = -1, a1 = -1;
+    double b = 0.0;
+    if (q < L1) {
+      a0 = r0[q];
+      a1 = r1[q];
+      b = bv[q];
+    }
+    const int nb = (int)min(32LL, L1 - qb);
+    for (int t = 0; t < nb; t++) {
+      while (qb + t >= ce) flush();  // the leaf starts the next piece
+      const int32_t x0 = __shfl_sync(0xffffffffu, a0, t);
+      const int32_t x1 = __shfl_sync(0xffffffffu, a1, t);
+      const double bb = __shfl_sync(0xffffffffu, b, t);
+      if (!in || x0 >= F0.rows || (MODE == 0 && x1 >= F1.rows)) continue;  // factor row absent
+      const uint32_t m0 = F0.mask[(int64_t)x0 * F0.mw + (j >> 5)];
+      const double d0 = F0.dense[(int64_t)x0 * F0.R + j];
+      uint32_t m1 = 0xffffffffu;
+      double d1 = 0.0;
+      if (MODE == 0) {
+        m1 = F1.mask[(int64_t)x1 * F1.mw + (j >> 5)];
+        d1 = F1.dense[(int64_t)x1 * F1.R + j];
+      }
+      if (!(((m0 & m1) >> (j & 31)) & 1u)) continue;
+      double t0 = __dmul_rn(bb, d0);
+      if (MODE == 0) t0 = __dmul_rn(t0, d1);
+      acc = started ? __dadd_rn(acc, t0) : t0;
+      started = true;
+    }
+  }
+  while (cp < np) flush();
+  (void)mw;
+}
+
 // Warp per segment: add the pieces' partials in piece order into the
 // segment's running values for this column tile (first present value
 // assigns, later ones add), and accumulate the presence mask.
@@ -588,7 +695,22 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
                                   partial.as<double>(), pmask.as<uint32_t>(), segval.as<double>(),
                                   segmask.as<uint32_t>(), direct);
       };
-      if (mode == 0) {
+      const bool grouped = direct_out && jpl <= 1 && npieces > 0 && nnz <= 8 * npieces;
+      if (grouped) {  // tiny buckets: G pieces per warp
+        constexpr int G = 8;
+        const int64_t warps = (npieces + G - 1) / G;
+        const unsigned gg = (unsigned)((warps + 7) / 8);
+        if (mode == 0)
+          k_pieces_grouped<0><<<gg, 256, 0, s>>>(npieces, G, nnz, pseg.as<int32_t>(), pstart.as<long long>(),
+                                                 starts.as<long long>(), r0.as<int32_t>(), r1.as<int32_t>(),
+                                                 bv.as<double>(), f0, f1, R, mw, pw, partial.as<double>(),
+                                                 pmask.as<uint32_t>(), direct);
+        else
+          k_pieces_grouped<1><<<gg, 256, 0, s>>>(npieces, G, nnz, pseg.as<int32_t>(), pstart.as<long long>(),
+                                                 starts.as<long long>(), r0.as<int32_t>(), r1.as<int32_t>(),
+                                                 bv.as<double>(), f0, f1, R, mw, pw, partial.as<double>(),
+                                                 pmask.as<uint32_t>(), direct);
+      } else if (mode == 0) {
         if (jpl <= 1) launch(k_pieces<0, 1>);
         else if (jpl == 2) launch(k_pieces<0, 2>);
         else if (jpl == 4) launch(k_pieces<0, 4>);
