@@ -430,28 +430,37 @@ __global__ void k_combine(int64_t nseg, int mode, const long long* __restrict__ 
                           const double* __restrict__ partial, const uint32_t* __restrict__ pmask, int32_t R, int32_t j0,
                           int32_t mw, int32_t pw, double* __restrict__ segval, uint32_t* __restrict__ segmask,
                           DirectOut direct) {
+  // A warp looks at 32 segments at once and works through the split ones
+  // among them (one piece: k_pieces wrote it), so a batch of millions of
+  // one-piece buckets costs one check per lane, not a warp each.
   const int lane = threadIdx.x & 31;
-  const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (s >= nseg || poff[s + 1] - poff[s] == 1) return;  // one piece: k_pieces wrote it
-  for (int u = 0; u < kJpl; u++) {
-    const int j = j0 + lane + 32 * u;
-    double v = 0.0;
-    bool have = false;
-    for (long long pc = poff[s]; u < pw && pc < poff[s + 1]; pc++) {
-      const uint32_t m = pmask[pc * pw + u];
-      if ((m >> lane) & 1u) {
-        const double x = partial[pc * (int64_t)(32 * pw) + (j - j0)];
-        v = have ? __dadd_rn(v, x) : x;
-        have = true;
+  const int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+  const int64_t mine = base + lane;
+  const bool split = mine < nseg && poff[mine + 1] - poff[mine] > 1;
+  unsigned todo = __ballot_sync(0xffffffffu, split);
+  while (todo) {
+    const int64_t s = base + (__ffs(todo) - 1);
+    todo &= todo - 1u;
+    for (int u = 0; u < kJpl; u++) {
+      const int j = j0 + lane + 32 * u;
+      double v = 0.0;
+      bool have = false;
+      for (long long pc = poff[s]; u < pw && pc < poff[s + 1]; pc++) {
+        const uint32_t m = pmask[pc * pw + u];
+        if ((m >> lane) & 1u) {
+          const double x = partial[pc * (int64_t)(32 * pw) + (j - j0)];
+          v = have ? __dadd_rn(v, x) : x;
+          have = true;
+        }
       }
+      if (direct.o0) {
+        if (j < R && u < pw) direct_write(direct, mode, s, R, j, v);
+        continue;
+      }
+      if (j < R) segval[s * (int64_t)R + j] = v;
+      const unsigned m = __ballot_sync(0xffffffffu, have && j < R);
+      if (lane == 0 && (j0 / 32 + u) < mw) segmask[s * (int64_t)mw + j0 / 32 + u] = m;
     }
-    if (direct.o0) {
-      if (j < R && u < pw) direct_write(direct, mode, s, R, j, v);
-      continue;
-    }
-    if (j < R) segval[s * (int64_t)R + j] = v;
-    const unsigned m = __ballot_sync(0xffffffffu, have && j < R);
-    if (lane == 0 && (j0 / 32 + u) < mw) segmask[s * (int64_t)mw + j0 / 32 + u] = m;
   }
 }
 
@@ -721,7 +730,7 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
         else if (jpl == 4) launch(k_pieces<1, 4>);
         else launch(k_pieces<1, 8>);
       }
-      k_combine<<<(unsigned)((nseg + 7) / 8), 256, 0, s>>>(nseg, mode, poff.as<long long>(), partial.as<double>(),
+      k_combine<<<(unsigned)((nseg + 255) / 256), 256, 0, s>>>(nseg, mode, poff.as<long long>(), partial.as<double>(),
                                                            pmask.as<uint32_t>(), R, j0, mw, pw, segval.as<double>(),
                                                            segmask.as<uint32_t>(), direct);
       count_launch(2);
