@@ -800,6 +800,49 @@ def bench_tensor(args):
         alg = 12 * nnz + 8 * (nslices + nfibers + 2) + 8 * R * d2 + 20 * n_out
     bw, peak_src = measured_peaks()
     achieved = alg / (ms_dev * 1e-3) / 1e9
+
+    # ---- e2e through the TACO C entry point (COO_CSF_DCSR[_DCSR]_bucket), host arrays ----
+    for f in F:
+        f.release()
+    B.release()
+    Bh = taco.csf3_from_coo(*coo, dims)
+    Fh = [taco.dcsr(*f) for f in facs]
+    pinned = []
+    for h in [Bh] + Fh:
+        for arr in h.keep:
+            if isinstance(arr, np.ndarray) and arr.nbytes >= (1 << 20) and \
+                    L.spws_host_pin(arr.ctypes.data, arr.nbytes) == 0:
+                pinned.append(arr)
+    # CSF: roots, pos1, crd1, pos2, crd2, vals; DCSR factor: row ids, pos, crd, vals
+    h2d = 4 * (2 * nslices + 1) + 4 * (2 * nfibers + 1) + 12 * nnz + \
+        sum(4 * (2 * f[3] + 1) + 12 * len(f[1]) for f in facs)
+    order_out = 2 if args.workload == "mttkrp" else 3
+    out_dims = (dims[2], R) if args.workload == "mttkrp" else (dims[0], dims[2], R)
+    e2e_walls, d2h = [], 0
+    for it in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+        A = taco.init_coo(out_dims)
+        t0 = time.perf_counter()
+        if args.workload == "mttkrp":
+            sp.check(L.spws_coo_csf_dcsr_dcsr_bucket_compute(A.ptr(), Bh.ptr(), Fh[0].ptr(), Fh[1].ptr(), 0))
+        else:
+            sp.check(L.spws_coo_csf_dcsr_bucket_compute(A.ptr(), Bh.ptr(), Fh[0].ptr(), 0))
+        t1 = time.perf_counter()
+        d2h = int(A.t.vals_size) * (4 * order_out + 8)
+        for m in range(1, order_out + 1):
+            L.spws_free(C.cast(A.t.indices[m][0], C.c_void_p))
+        L.spws_free(C.cast(A.t.vals, C.c_void_p))
+        if it > 0:  # first call is a warm-up (host allocator, page faults)
+            e2e_walls.append(t1 - t0)
+    for arr in pinned:
+        L.spws_host_unpin(arr.ctypes.data)
+    e2e_wall = sum(e2e_walls) / len(e2e_walls) if e2e_walls else float("nan")
+    flops_e2e = 2.0 * R * nnz + (R * nfibers if args.workload == "mttkrp" else 0.0)
+    e2e = {"value": flops_e2e / e2e_wall / 1e9 if e2e_walls else None, "unit": "GFLOP/s",
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_wall * 1e3,
+           "path": ("spws_coo_csf_dcsr_dcsr_bucket_compute" if args.workload == "mttkrp"
+                    else "spws_coo_csf_dcsr_bucket_compute") + " (taco_tensor_t, host arrays)"}
+    cpu = None if args.no_cpu else tensor_cpu_baseline(args.workload, coo, dims, facs, args.cpu_tensor_nnz)
+
     # FP64 term: the bucket sums are (b*C)*D + acc (MTTKRP) and b*C + acc (TTM) per
     # leaf and column, kept as separate multiplies and adds for the reference's
     # rounding: 3 or 2 FP64 instructions, against the FMA peak's two flops each
@@ -823,8 +866,53 @@ def bench_tensor(args):
                          "fp64_peak_gflops": fp64_peak, "ceiling_ms": ceilings,
                          "binding": max(ceilings, key=lambda k: ceilings[k]),
                          "frac_of_binding_ceiling": max(ceilings.values()) / ms_dev},
-            "gpu_launches": launches, "clocks": clk.summary(), "generation_s": gen_s}
+            "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e, "generation_s": gen_s}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+
+
+def tensor_sample(coo, target_nnz, seed=7):
+    """Whole level-0 slices of a COO tensor (CSF level order), drawn at random
+    until they hold about target_nnz nonzeros. Returns (sub-COO, slices, nnz)."""
+    c0 = np.asarray(coo[0])
+    roots, counts = np.unique(c0, return_counts=True)
+    order = np.random.default_rng(seed).permutation(len(roots))
+    k = min(len(roots), int(np.searchsorted(np.cumsum(counts[order]), target_nnz)) + 1)
+    keep = np.isin(c0, roots[np.sort(order[:k])])
+    return tuple(np.asarray(a)[keep] for a in coo), k, int(keep.sum())
+
+
+def tensor_cpu_baseline(workload, coo, dims, facs, target_nnz):
+    """The reference's bucket kernel for the tensor workload (oracle/_ref when
+    it was built, else the oracle port), one core, on randomly drawn whole
+    slices of the same tensor with the full factors; only the kernel call is
+    timed (the CSF and factors are built before it)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    kind = cpu_kind()
+    if target_nnz is None:
+        target_nnz = 4_000_000 if workload == "mttkrp" else 200_000
+    sub, nslices, nnz = tensor_sample(coo, target_nnz)
+    R = facs[0][4]
+    okind = "ref" if kind == "reference" else "port"
+    secs = []
+    if workload == "mttkrp":
+        w_cap = oracle.w_cap_default(int(dims[2] * R * 0.2))  # bench_bucket_mttkrp.cpp:35
+        oracle.mttkrp("bucket", sub, dims, facs[0], facs[1], w_cap=w_cap, kind=okind, timing=secs)
+        nfib = len(np.unique(sub[0].astype(np.int64) * dims[1] + sub[1]))
+        flops = 2.0 * R * nnz + R * nfib
+        note = ""
+    else:
+        w_cap = oracle.w_cap_default(int(dims[1] * R * 0.05))  # bench_bucket_ttm.cpp:41
+        oracle.ttm("bucket", sub, dims, facs[0], w_cap=w_cap, kind=okind, timing=secs)
+        flops = 2.0 * R * nnz
+        # COO_CSF_DCSR_bucket_il.h:200-290: each full workspace is merged into the whole output so far
+        note = "; the reference merges every workspace flush into the whole output so far, so its rate " \
+               "falls as the output grows and the full tensor runs slower than this sample"
+    return {"value": flops / secs[0] / 1e9, "unit": "GFLOP/s", "cores": 1, "kind": kind,
+            "sample": f"{nslices} random whole slices (seed 7), {nnz} nonzeros, full factors, w_cap {w_cap}: "
+                      f"{secs[0]:.2f} s{note}"}
 
 
 SERVED_MIX = (0.90, 0.09, 0.01)  # small products, R-MAT 2^18 products, TTM requests
@@ -1065,6 +1153,8 @@ def main():
     ap.add_argument("--transpose-cpu-products", type=int, default=30_000_000,
                     help="transpose workload: largest product count timed on the CPU port")
     ap.add_argument("--rank", type=int, default=32, help="mttkrp/ttm workloads: factor rank R")
+    ap.add_argument("--cpu-tensor-nnz", type=int, default=None,
+                    help="mttkrp/ttm workloads: nonzeros in the CPU-baseline sample (4M / 200k)")
     ap.add_argument("--served-requests", type=int, default=400, help="served workload: requests per run")
     ap.add_argument("--served-pool", type=int, default=512, help="served workload: distinct small products")
     ap.add_argument("--served-workers", type=int, default=8)

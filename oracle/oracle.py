@@ -14,6 +14,7 @@ outputs: CSR results as (pos, crd, vals), COO results as ([crd per mode], vals).
 import ctypes as C
 import os
 import subprocess
+import time
 
 import numpy as np
 
@@ -211,10 +212,11 @@ def spgemm_t_nofuse(A, B, w_cap=None, kind="port"):
     return taco.take_csr(CnoT, an, fr), taco.take_csr(Cout, bm, fr), int(coll.value)
 
 
-def mttkrp(method, Bcsf, dims, Cf, Df, w_cap=None, kind="port"):
+def mttkrp(method, Bcsf, dims, Cf, Df, w_cap=None, kind="port", timing=None):
     """A(i,j) = sum B(k,l,i) C(k,j) D(l,j). Bcsf: (c0,c1,c2,vals) COO in CSF
     level order (k,l,i) with dims; Cf, Df: CSR triples of the factors.
-    Returns ([i, j], vals)."""
+    Returns ([i, j], vals). A list given as `timing` gets the seconds of the
+    kernel call alone (operands already built, output not yet copied out)."""
     lib, pre, fr = _load(kind)
     B = taco.csf3_from_coo(*Bcsf, dims)
     Ct = taco.dcsr(*Cf)
@@ -223,16 +225,19 @@ def mttkrp(method, Bcsf, dims, Cf, Df, w_cap=None, kind="port"):
     A = taco.init_coo((dims[2], R))
     if w_cap is None:
         w_cap = w_cap_default(int(dims[2] * R * 0.1))
+    t0 = time.perf_counter()
     rc = getattr(lib, pre + ("mttkrp_hash" if method == "hash" else "mttkrp_bucket"))(
         A.ptr(), B.ptr(), Ct.ptr(), Dt.ptr(), w_cap)
+    if timing is not None:
+        timing.append(time.perf_counter() - t0)
     if rc != 0:
         raise RuntimeError(f"oracle mttkrp failed rc={rc}")
     return taco.take_coo(A, 2, fr)
 
 
-def ttm(method, Bcsf, dims, Cf, w_cap=None, kind="port"):
+def ttm(method, Bcsf, dims, Cf, w_cap=None, kind="port", timing=None):
     """A(k,j,l) = sum_i B(k,i,j) C(i,l). Bcsf in CSF level order (k,i,j).
-    Returns ([k, j, l], vals)."""
+    Returns ([k, j, l], vals); `timing` as in mttkrp."""
     lib, pre, fr = _load(kind)
     B = taco.csf3_from_coo(*Bcsf, dims)
     Ct = taco.dcsr(*Cf)
@@ -240,7 +245,10 @@ def ttm(method, Bcsf, dims, Cf, w_cap=None, kind="port"):
     A = taco.init_coo((dims[0], dims[2], R))
     if w_cap is None:
         w_cap = w_cap_default(int(dims[1] * R * 0.05))
+    t0 = time.perf_counter()
     rc = getattr(lib, pre + ("ttm_hash" if method == "hash" else "ttm_bucket"))(A.ptr(), B.ptr(), Ct.ptr(), w_cap)
+    if timing is not None:
+        timing.append(time.perf_counter() - t0)
     if rc != 0:
         raise RuntimeError(f"oracle ttm failed rc={rc}")
     return taco.take_coo(A, 3, fr)

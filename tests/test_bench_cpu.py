@@ -50,3 +50,26 @@ def test_transpose_suite_spans_output_sizes():
     A, desc = bench.transpose_suite_matrix("er", 600, 3)
     assert A[3] == 600 and desc["kind"] == "er"
     assert bench.gstats([1.0, 4.0])["gmean"] == 2.0
+
+
+def test_tensor_sample_takes_whole_slices():
+    import bench
+    from sparsews_gb300 import gen
+    c0, c1, c2, v = gen.tensor3((300, 200, 100), 20000, zipf_s=1.1, seed=3)
+    sub, k, nnz = bench.tensor_sample((c0, c1, c2, v), 5000)
+    assert nnz == len(sub[0]) and nnz >= 5000 and k == len(np.unique(sub[0]))
+    for r in np.unique(sub[0]):  # every drawn slice keeps all of its nonzeros
+        assert np.count_nonzero(sub[0] == r) == np.count_nonzero(c0 == r)
+
+
+def test_tensor_cpu_baseline_reports_rate():
+    import bench
+    from sparsews_gb300 import gen
+    dims = (300, 200, 100)
+    c0, c1, c2, v = gen.tensor3(dims, 20000, zipf_s=1.1, seed=3)
+    f = gen.dense_factor(dims[2], 8, seed=4)
+    out = bench.tensor_cpu_baseline("ttm", (c0, c2, c1, v), (dims[0], dims[2], dims[1]), [f], 3000)
+    assert out["value"] > 0 and out["cores"] == 1 and out["kind"] in ("reference", "port")
+    g = [gen.dense_factor(dims[1], 8, seed=5), gen.dense_factor(dims[2], 8, seed=6)]
+    out = bench.tensor_cpu_baseline("mttkrp", (c1, c2, c0, v), (dims[1], dims[2], dims[0]), g, 3000)
+    assert out["value"] > 0 and "slices" in out["sample"]
