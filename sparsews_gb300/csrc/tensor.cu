@@ -222,16 +222,22 @@ __global__ void k_all_present(int32_t rows, int32_t R, int32_t mw, const uint32_
 // (hash_il.h:317). JPL is the smallest power of two covering the rank (at
 // most kJpl): a rank-32 factor needs one accumulator per lane, and the
 // registers the other seven would hold are what limits how many warps (each
-// waiting on its factor-row loads) an SM keeps in flight.
-template <int MODE, int JPL>
+// waiting on its factor-row loads) an SM keeps in flight. LW = 16 gives each
+// half-warp its own piece, for ranks of at most 16 (one column per lane),
+// which would otherwise leave half of every warp idle; the sums and their
+// order are the same.
+template <int MODE, int JPL, int LW = 32>
 __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, const long long* __restrict__ pstart,
                          const long long* __restrict__ starts, const int32_t* __restrict__ r0,
                          const int32_t* __restrict__ r1, const double* __restrict__ bv, Factor F0, Factor F1, int32_t R,
                          int32_t j0, int32_t mw, int32_t pw, double* __restrict__ partial,
                          uint32_t* __restrict__ pmask, double* __restrict__ segval, uint32_t* __restrict__ segmask,
                          DirectOut direct) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  static_assert(LW == 32 || (LW == 16 && JPL == 1), "a half-warp piece holds one column per lane");
+  const int lane = threadIdx.x & (LW - 1);  // lane within the piece's lanes
+  const int hshift = LW == 32 ? 0 : (int)(threadIdx.x & 16);
+  const unsigned gm = LW == 32 ? 0xffffffffu : (0xffffu << hshift);  // this piece's lanes
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LW;
   if (w >= npieces) return;
   const int64_t sg = pseg[w];
   const long long s_beg = starts[sg], s_end = starts[sg + 1];
@@ -241,7 +247,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   unsigned started = 0;
 #pragma unroll
   for (int u = 0; u < JPL; u++) acc[u] = 0.0;
-  for (long long qb = q0; qb < q1; qb += 32) {
+  for (long long qb = q0; qb < q1; qb += LW) {
     const long long q = qb + lane;
     int32_t a0 = -1, a1 = -1;
     double b = 0.0;
@@ -250,11 +256,11 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
       a1 = r1[q];
       b = bv[q];
     }
-    const int nb = (int)min(32LL, q1 - qb);
+    const int nb = (int)min((long long)LW, q1 - qb);
     for (int t = 0; t < nb; t++) {
-      const int32_t x0 = __shfl_sync(0xffffffffu, a0, t);
-      const int32_t x1 = __shfl_sync(0xffffffffu, a1, t);
-      const double bb = __shfl_sync(0xffffffffu, b, t);
+      const int32_t x0 = __shfl_sync(gm, a0, t, LW);
+      const int32_t x1 = __shfl_sync(gm, a1, t, LW);
+      const double bb = __shfl_sync(gm, b, t, LW);
       if (x0 >= F0.rows || (MODE == 0 && x1 >= F1.rows)) continue;  // factor row absent
 #pragma unroll
       for (int u = 0; u < JPL; u++) {
@@ -293,7 +299,9 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   for (int u = 0; u < JPL; u++) {
     const int j = j0 + lane + 32 * u;
     const bool in = j < R;
-    const unsigned m = __ballot_sync(0xffffffffu, in && ((started >> u) & 1u));  // all lanes, one call site
+    // all of the piece's lanes, one call site; bit k = the piece's lane k (the
+    // other half-warp's bits, if it votes in the same step, are masked off)
+    const unsigned m = (__ballot_sync(gm, in && ((started >> u) & 1u)) & gm) >> hshift;
     if (single && direct.o0) {
       if (in) {
         const int64_t p = sg * (int64_t)R + j;
@@ -704,6 +712,12 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
                                   partial.as<double>(), pmask.as<uint32_t>(), segval.as<double>(),
                                   segmask.as<uint32_t>(), direct);
       };
+      auto launch_half = [&](auto kernel) {  // 16 pieces per 256-thread block
+        kernel<<<(unsigned)((npieces + 15) / 16), 256, 0, s>>>(
+            npieces, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(), r0.as<int32_t>(),
+            r1.as<int32_t>(), bv.as<double>(), f0, f1, R, j0, mw, pw, partial.as<double>(), pmask.as<uint32_t>(),
+            segval.as<double>(), segmask.as<uint32_t>(), direct);
+      };
       const bool grouped = direct_out && jpl <= 1 && npieces > 0 && nnz <= 8 * npieces;
       if (grouped) {  // tiny buckets: G pieces per warp
         constexpr int G = 8;
@@ -720,12 +734,14 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
                                                  bv.as<double>(), f0, f1, R, mw, pw, partial.as<double>(),
                                                  pmask.as<uint32_t>(), direct);
       } else if (mode == 0) {
-        if (jpl <= 1) launch(k_pieces<0, 1>);
+        if (R <= 16) launch_half(k_pieces<0, 1, 16>);
+        else if (jpl <= 1) launch(k_pieces<0, 1>);
         else if (jpl == 2) launch(k_pieces<0, 2>);
         else if (jpl == 4) launch(k_pieces<0, 4>);
         else launch(k_pieces<0, 8>);
       } else {
-        if (jpl <= 1) launch(k_pieces<1, 1>);
+        if (R <= 16) launch_half(k_pieces<1, 1, 16>);
+        else if (jpl <= 1) launch(k_pieces<1, 1>);
         else if (jpl == 2) launch(k_pieces<1, 2>);
         else if (jpl == 4) launch(k_pieces<1, 4>);
         else launch(k_pieces<1, 8>);
