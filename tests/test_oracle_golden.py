@@ -178,3 +178,29 @@ def test_port_matches_live_reference_transposed(wcap):
     assert g[2] == r[2]
     for x, y in ((g[0], r[0]), (g[1], r[1])):
         assert all(np.array_equal(a, b) for a, b in zip(x, y))
+
+
+def _sparse_factor(rows, rank, density, seed):
+    """A CSR factor with about density * rows * rank entries (rows may be empty)."""
+    rng = np.random.default_rng(seed)
+    r, c = np.nonzero(rng.random((rows, rank)) < density)
+    pos = np.zeros(rows + 1, np.int64)
+    np.add.at(pos, r + 1, 1)
+    return np.cumsum(pos).astype(np.int32), c.astype(np.int32), rng.uniform(-1, 1, len(r)), rows, rank
+
+
+@needs_ref
+@pytest.mark.parametrize("density", [0.05, 0.4])
+def test_port_matches_live_reference_tensors_sparse_factors(density):
+    """The co-iteration over factor rows with missing entries (and missing
+    rows) matches the reference, for both workspaces."""
+    i0, i1, i2, tv = gen.tensor3((60, 40, 30), 1500, seed=44)
+    Cf, Df = _sparse_factor(40, 12, density, 45), _sparse_factor(30, 12, density, 46)
+    Ct = _sparse_factor(30, 9, density, 47)
+    for m in ("hash", "bucket"):
+        g = oracle.mttkrp(m, (i1, i2, i0, tv), (40, 30, 60), Cf, Df, w_cap=32, kind="port")
+        r = oracle.mttkrp(m, (i1, i2, i0, tv), (40, 30, 60), Cf, Df, w_cap=32, kind="ref")
+        assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
+        g = oracle.ttm(m, (i0, i2, i1, tv), (60, 30, 40), Ct, w_cap=32, kind="port")
+        r = oracle.ttm(m, (i0, i2, i1, tv), (60, 30, 40), Ct, w_cap=32, kind="ref")
+        assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
