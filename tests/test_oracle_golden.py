@@ -204,3 +204,32 @@ def test_port_matches_live_reference_tensors_sparse_factors(density):
         g = oracle.ttm(m, (i0, i2, i1, tv), (60, 30, 40), Ct, w_cap=32, kind="port")
         r = oracle.ttm(m, (i0, i2, i1, tv), (60, 30, 40), Ct, w_cap=32, kind="ref")
         assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
+
+
+@needs_ref
+def test_port_matches_live_reference_tensor_edges():
+    """Empty and one-nonzero tensors, and every CSF level order of one tensor."""
+    z = np.zeros(0, np.int64)
+    Cf, Df, Ct = gen.dense_factor(40, 4, seed=1), gen.dense_factor(30, 4, seed=2), gen.dense_factor(30, 4, seed=3)
+    one = (np.array([5]), np.array([7]), np.array([3]), np.array([0.5]))
+    for m in ("hash", "bucket"):
+        for B in ((z, z, z, np.zeros(0)), one):
+            g = oracle.mttkrp(m, B, (40, 30, 60), Cf, Df, w_cap=32, kind="port")
+            r = oracle.mttkrp(m, B, (40, 30, 60), Cf, Df, w_cap=32, kind="ref")
+            assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
+            g = oracle.ttm(m, B, (60, 30, 40), Ct, w_cap=32, kind="port")
+            r = oracle.ttm(m, B, (60, 30, 40), Ct, w_cap=32, kind="ref")
+            assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
+    dims = (24, 20, 16)
+    c = gen.tensor3(dims, 900, seed=48)
+    for perm in ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)):
+        B = tuple(c[p] for p in perm) + (c[3],)
+        d = tuple(dims[p] for p in perm)
+        F0, F1 = _sparse_factor(d[0], 6, 0.5, 49), _sparse_factor(d[1], 6, 0.5, 50)
+        g = oracle.mttkrp("bucket", B, d, F0, F1, w_cap=16, kind="port")
+        r = oracle.mttkrp("bucket", B, d, F0, F1, w_cap=16, kind="ref")
+        assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
+        Fi = _sparse_factor(d[1], 5, 0.5, 51)
+        g = oracle.ttm("bucket", B, d, Fi, w_cap=16, kind="port")
+        r = oracle.ttm("bucket", B, d, Fi, w_cap=16, kind="ref")
+        assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
