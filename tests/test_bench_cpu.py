@@ -73,3 +73,42 @@ def test_tensor_cpu_baseline_reports_rate():
     g = [gen.dense_factor(dims[1], 8, seed=5), gen.dense_factor(dims[2], 8, seed=6)]
     out = bench.tensor_cpu_baseline("mttkrp", (c1, c2, c0, v), (dims[1], dims[2], dims[0]), g, 3000)
     assert out["value"] > 0 and "slices" in out["sample"]
+
+
+def _json_lines(out):
+    import json
+    return [json.loads(l) for l in out.splitlines() if l.startswith("{")]
+
+
+def test_reference_arm_prints_contract_line():
+    """bench.py --impl reference runs the reference algorithm on host cores and
+    prints one line with the arm's keys (small R-MAT, bounded sample)."""
+    import subprocess
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--scale", "9", "--steps", "1",
+                        "--warmup", "3", "--cpu-step-products", "100000"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _json_lines(r.stdout)
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference" and d["metric"] == "spgemm_gflops" and d["value"] > 0
+    assert d["warmup"] == 3 and d["n_gpus"] == 1 and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_two_ranks_prints_once():
+    """Under torchrun with two (gloo, CPU) ranks, rank 0 alone prints the line."""
+    import socket
+    import subprocess
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl",
+                        "reference", "--gpus", "2", "--scale", "9", "--steps", "1", "--warmup", "3",
+                        "--cpu-step-products", "100000"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _json_lines(r.stdout)
+    assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["n_gpus"] == 2
