@@ -59,3 +59,33 @@ def test_package_fails_loudly_without_library(tmp_path, monkeypatch):
     monkeypatch.setattr(pkg, "_lib", None)
     with pytest.raises(ImportError):
         pkg.lib()
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_c_and_cpp_callers_compile_link_and_run(built, tmp_path, lang):
+    """A caller in C11 or C++17 includes every public header under -Wall
+    -Wextra -Werror, takes the address of every declared entry point (so the
+    link resolves each one against libspws.so), and runs a non-compute call."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("needs gcc/g++")
+    names = declared_functions()
+    heads = [f for f in sorted(os.listdir(INC)) if f.endswith(".h")]
+    src = [f'#include "spws/{h}"' for h in heads] + ["#include <stdio.h>", "typedef void (*fp)(void);",
+                                                     "static fp table[] = {"]
+    src += [f"  (fp){n}," for n in names] + ["};", "int main(void) {",
+                                            '  printf("%s %d\\n", spws_version(), (int)(sizeof table / sizeof *table));',
+                                            "  return 0;", "}"]
+    ext = "c" if lang == "c" else "cpp"
+    (tmp_path / f"caller.{ext}").write_text("\n".join(src) + "\n")
+    libdir = os.path.dirname(built)
+    std = "-std=c11" if lang == "c" else "-std=c++17"
+    r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(tmp_path / f"caller.{ext}"), "-o", str(tmp_path / "caller"), f"-L{libdir}", "-lspws",
+                        f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run([str(tmp_path / "caller")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "sm_103a" in r.stdout and r.stdout.split()[-1] == str(len(names))
