@@ -458,7 +458,7 @@ def bench_spws(args, ws, rank, local, dist):
                      "compulsory_gbs": compulsory / (ms_dev * 1e-3) / 1e9},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_wall * 1e3, "path": "spws_csr_csr_hash_compute (taco_tensor_t, host arrays)"},
+                "ms_per_step": e2e_wall * 1e3 if e2e_walls else None, "path": "spws_csr_csr_hash_compute (taco_tensor_t, host arrays)"},
         "gpu_launches": int(launches * args.steps),
     }
     if cpu is not None:
@@ -838,7 +838,7 @@ def bench_tensor(args):
     e2e_wall = sum(e2e_walls) / len(e2e_walls) if e2e_walls else float("nan")
     flops_e2e = 2.0 * R * nnz + (R * nfibers if args.workload == "mttkrp" else 0.0)
     e2e = {"value": flops_e2e / e2e_wall / 1e9 if e2e_walls else None, "unit": "GFLOP/s",
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_wall * 1e3,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_wall * 1e3 if e2e_walls else None,
            "path": ("spws_coo_csf_dcsr_dcsr_bucket_compute" if args.workload == "mttkrp"
                     else "spws_coo_csf_dcsr_bucket_compute") + " (taco_tensor_t, host arrays)"}
     cpu = None if args.no_cpu else tensor_cpu_baseline(args.workload, coo, dims, facs, args.cpu_tensor_nnz)
