@@ -233,3 +233,55 @@ def test_port_matches_live_reference_tensor_edges():
         g = oracle.ttm("bucket", B, d, Fi, w_cap=16, kind="port")
         r = oracle.ttm("bucket", B, d, Fi, w_cap=16, kind="ref")
         assert all(np.array_equal(a, b) for a, b in zip(g[0] + [g[1]], r[0] + [r[1]]))
+
+
+def _rect(n, m, deg, seed):
+    """n x m CSR with 0..deg distinct sorted columns per row (some rows empty)."""
+    rng = np.random.default_rng(seed)
+    pos, crd = [0], []
+    for _ in range(n):
+        k = int(rng.integers(0, deg + 1))
+        crd.extend(np.sort(rng.choice(m, size=min(k, m), replace=False)))
+        pos.append(len(crd))
+    return np.array(pos, np.int32), np.array(crd, np.int32), rng.uniform(-1, 1, len(crd)), n, m
+
+
+def _empty(n, m):
+    return np.zeros(n + 1, np.int32), np.zeros(0, np.int32), np.zeros(0), n, m
+
+
+EDGE_PAIRS = {"rect": (_rect(70, 50, 6, 1), _rect(50, 90, 5, 2)),
+              "empty_A": (_empty(30, 20), _rect(20, 25, 4, 3)),
+              "empty_B": (_rect(30, 20, 4, 4), _empty(20, 25))}
+
+
+@needs_ref
+@pytest.mark.parametrize("case", sorted(EDGE_PAIRS))
+@pytest.mark.parametrize("method,wcap", [("hash", 16), ("hash", None), ("taco", None), ("outer_hash", 16),
+                                         ("outer_coord", 16), ("outer_bucket", 16)])
+def test_port_matches_live_reference_rectangular_and_empty(case, method, wcap):
+    """A*B with A and B of different shapes, rows without entries, and an
+    empty operand, for every workspace (small capacities force flushes)."""
+    A, B = EDGE_PAIRS[case]
+    m = "outer_coord_faithful" if method == "outer_coord" else method
+    got = oracle.spgemm(m, A, B, w_cap=wcap, kind="port")
+    ref = oracle.spgemm(method, A, B, w_cap=wcap, kind="ref")
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+
+
+@needs_ref
+@pytest.mark.parametrize("case", sorted(EDGE_PAIRS))
+def test_port_matches_live_reference_transposed_rectangular_and_empty(case):
+    A, B = EDGE_PAIRS[case]
+    (g, gc) = oracle.spgemm_t(A, B, w_cap=16, kind="port")
+    (r, rc) = oracle.spgemm_t(A, B, w_cap=16, kind="ref")
+    assert gc == rc and all(np.array_equal(a, b) for a, b in zip(g, r))
+    g = oracle.spgemm_outer_t(A, B, w_cap=16, kind="port")
+    r = oracle.spgemm_outer_t(A, B, w_cap=16, kind="ref")
+    assert all(np.array_equal(a, b) for a, b in zip(g, r))
+    g = oracle.spgemm_t_nofuse(A, B, w_cap=16, kind="port")
+    r = oracle.spgemm_t_nofuse(A, B, w_cap=16, kind="ref")
+    assert g[2] == r[2]
+    for x, y in ((g[0], r[0]), (g[1], r[1])):
+        assert all(np.array_equal(a, b) for a, b in zip(x, y))
