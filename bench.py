@@ -189,6 +189,66 @@ def run_cpu(A, rows, threads, kind):
     return time.perf_counter() - t0
 
 
+def heaviest_rows(A, k):
+    """The k rows of A with the most products (A times A)."""
+    pos = A[0].astype(np.int64)
+    cs = np.concatenate([[0], np.cumsum(np.diff(pos)[A[1]])])
+    rowp = cs[pos[1:]] - cs[pos[:-1]]
+    return np.sort(np.argsort(-rowp, kind="stable")[:k])
+
+
+def _csr_concat(parts):
+    pos = [np.zeros(1, np.int64)]
+    base = 0
+    for p in parts:
+        pos.append(p[0][1:].astype(np.int64) + base)
+        base += int(p[0][-1])
+    return (np.concatenate(pos), np.concatenate([p[1] for p in parts]) if parts else np.zeros(0, np.int32),
+            np.concatenate([p[2] for p in parts]) if parts else np.zeros(0))
+
+
+def oracle_rows(A, B, rows, threads, method):
+    """The oracle's rows `rows` of A*B (its row-wise hash, or for the
+    condition bound its TACO form on |A|, |B|), split over host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    parts = [p for p in np.array_split(rows, max(1, min(threads, len(rows)))) if len(p)]
+    out = [None] * len(parts)
+
+    def work(t):
+        sub = sub_rows(A, parts[t])
+        out[t] = oracle.spgemm(method, sub, B, w_cap=oracle.w_cap_default(len(A[1])))
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(len(parts))]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    return _csr_concat(out)
+
+
+def parity_rows(A, got, rows, threads):
+    """Rows `rows` of the GPU's C = A*A (`got`, a compact host CSR of those
+    rows) against the oracle on the same rows: structure (row counts and
+    columns) must be bit-exact, values within
+    |x - x_ref| <= 1e-12 * max(|x_ref|, sum |a*b|) per entry."""
+    absA = (A[0], A[1], np.abs(A[2]), A[3], A[4])
+    ref = oracle_rows(A, A, rows, threads, "hash")
+    scale = oracle_rows(absA, absA, rows, threads, "taco")[2]
+    exact = (len(got[0]) == len(ref[0]) and np.array_equal(got[0].astype(np.int64), ref[0])
+             and np.array_equal(got[1], ref[1]))
+    out = {"rows": int(len(rows)), "nnz": int(len(ref[1])), "structure_exact": bool(exact)}
+    if exact and len(ref[2]):
+        err = np.abs(got[2] - ref[2])
+        nz = ref[2] != 0
+        out["max_rel_err"] = float(np.max(err[nz] / np.abs(ref[2][nz]))) if nz.any() else 0.0
+        out["max_cond_err"] = float(np.max(err / np.maximum(np.abs(ref[2]), scale)))
+        out["within_tol"] = bool(out["max_cond_err"] <= 1e-12)
+    else:
+        out["within_tol"] = bool(exact)
+    return out
+
+
 def cpu_instances(insts, threads, target_products, seed=11):
     """Runs the reference algorithm (oracle port: row-wise hash, the
     reference's w_cap heuristic) over a random sample of whole instances
@@ -418,9 +478,20 @@ def bench_spws(args, ws, rank, local, dist):
 
     if rank != 0:
         return
-    cpu = None
+    cpu = parity = None
     if ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(A, args.cpu_products, 1)
+        # the oracle checks the GPU's result on the CPU-baseline row sample and
+        # on the heaviest rows (one more product, outside the timed region)
+        dC, _ = sp.spgemm_device(dA, dA)
+        rows_s, _ = cpu_sample_rows(A, args.cpu_products)
+        rows_h = heaviest_rows(A, 64)
+        t0 = time.perf_counter()
+        parity = {"sampled": parity_rows(A, dC.download_rows(rows_s), rows_s, os.cpu_count() or 1),
+                  "heaviest": parity_rows(A, dC.download_rows(rows_h), rows_h, os.cpu_count() or 1)}
+        parity["oracle"] = "port of CSR_CSR_hash_sequential.h (row-wise hash), same rows, host threads"
+        parity["seconds"] = time.perf_counter() - t0
+        dC.release()
     line = {
         "metric": "spgemm_gflops",
         "value": value,
@@ -463,6 +534,8 @@ def bench_spws(args, ws, rank, local, dist):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if parity is not None:
+        line["parity"] = parity
     print(json.dumps(line), flush=True)
 
 
@@ -737,7 +810,182 @@ def bench_transpose(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_outer(args):
+    """The outer-product form of the R-MAT config (C = A*A, 2^18): the
+    coordinate workspace on the device (expand, stable radix sort, ordered
+    run sums; SPWS_ACCUM_COORD), beside the row-wise hash pipeline on the same
+    operands, and both DCSC x DCSR drop-in entry points end to end with host
+    arrays (their DCSC/DCSR inputs are converted to CSR on the device; the
+    conversion's cost is the difference to the CSR entry point). Sampled
+    rows of the coordinate result are checked bit for bit against the
+    oracle's j-ordered (TACO) sum."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import build, taco
+    build.build()
+    L = sp.lib()
+    sp.check(L.spws_set_device(0))
+    A, cfg = make_workload("rmat", args.scale)
+    nA = A[3]
+    dA = sp.DeviceCsr.upload(*A)
+
+    def timed(mode):
+        for _ in range(args.warmup):
+            dC, _ = sp.spgemm_device(dA, dA, accum_mode=mode)
+            dC.release()
+        ms, walls = [], []
+        for _ in range(args.steps):
+            sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+            t0 = time.perf_counter()
+            dC, st = sp.spgemm_device(dA, dA, accum_mode=mode)
+            walls.append(time.perf_counter() - t0)
+            ms.append(st.ms_total)
+            nnz, prods = st.nnz, st.products
+            dC.release()
+        return statistics.median(ms), statistics.median(walls), nnz, prods
+
+    l0 = L.spws_launch_count()
+    with ClockSampler(0) as clk:
+        coord_ms, coord_wall, nnzC, products = timed(1)
+    launches = (L.spws_launch_count() - l0) // max(1, args.steps + args.warmup)
+    hash_ms, hash_wall, _, _ = timed(0)
+
+    parity = None
+    if not args.no_cpu:
+        dC, _ = sp.spgemm_device(dA, dA, accum_mode=1)
+        rows = np.union1d(cpu_sample_rows(A, 20_000_000)[0], heaviest_rows(A, 8))
+        got = dC.download_rows(rows)
+        dC.release()
+        ref = oracle_rows(A, A, rows, os.cpu_count() or 1, "taco")
+        parity = {"rows": int(len(rows)), "nnz": int(len(ref[1])),
+                  "structure_exact": bool(np.array_equal(got[0].astype(np.int64), ref[0])
+                                          and np.array_equal(got[1], ref[1])),
+                  "values_bit_exact": bool(len(got[2]) == len(ref[2]) and np.array_equal(got[2], ref[2])),
+                  "oracle": "port of CSR_CSR_taco.h (j-ordered sums), same rows"}
+
+    # ---- e2e: the drop-in entry points with host arrays ----
+    pos = np.ascontiguousarray(A[0], np.int32)
+    crd = np.ascontiguousarray(A[1], np.int32)
+    vals = np.ascontiguousarray(A[2], np.float64)
+    tp, tc, tv = sp._csr_transpose_np(pos, crd, vals, nA, A[4])
+    host = [pos, crd, vals, tp, tc, tv]
+    pinned = [a for a in host if L.spws_host_pin(a.ctypes.data, a.nbytes) == 0]
+    Acsr = taco.csr(pos, crd, vals, nA, A[4])
+    Adcsc = taco.dcsc(tp, tc, tv, nA, A[4])
+    Bdcsr = taco.dcsr(pos, crd, vals, nA, A[4])
+    e2e = {}
+    calls = {"csr_csr_hash": lambda Ct: L.spws_csr_csr_hash_compute(Ct.ptr(), Acsr.ptr(), Acsr.ptr(), 0),
+             "dcsc_dcsr_hash": lambda Ct: L.spws_dcsc_dcsr_hash_compute(Ct.ptr(), Adcsc.ptr(), Bdcsr.ptr(), 0),
+             "dcsc_dcsr_coord": lambda Ct: L.spws_dcsc_dcsr_coord_compute(Ct.ptr(), Adcsc.ptr(), Bdcsr.ptr(), 0)}
+    for name, fn in calls.items():
+        walls = []
+        for it in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+            Ct = taco.init_dc(nA, A[4])
+            t0 = time.perf_counter()
+            sp.check(fn(Ct))
+            t1 = time.perf_counter()
+            for q in (Ct.t.indices[1][0], Ct.t.indices[1][1]):
+                L.spws_free(C.cast(q, C.c_void_p))
+            L.spws_free(C.cast(Ct.t.vals, C.c_void_p))
+            if it > 0:
+                walls.append(t1 - t0)
+        if walls:
+            w = statistics.median(walls)
+            e2e[name] = {"ms": w * 1e3, "gflops": 2.0 * products / w / 1e9}
+    for a in pinned:
+        L.spws_host_unpin(a.ctypes.data)
+    h2d = sum(a.nbytes for a in host[3:]) + sum(a.nbytes for a in host[:3])  # A as DCSC and as DCSR
+    d2h = 4 * (nA + 1) + 12 * nnzC
+    if "dcsc_dcsr_hash" in e2e and "csr_csr_hash" in e2e:
+        e2e["dcsc_conversion_ms"] = e2e["dcsc_dcsr_hash"]["ms"] - e2e["csr_csr_hash"]["ms"]
+    bw, peak_src = measured_peaks()
+    line = {"metric": "outer_coord_spgemm_gflops", "value": 2.0 * products / coord_wall / 1e9,
+            "unit": "GFLOP/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": coord_wall * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded R-MAT generator, numpy PCG64 seed 42)",
+            "config": {**cfg, "workspace": "coordinate (expand, stable radix sort, ordered run sums)",
+                       "l2": "flushed between timed steps (512 MiB write)"},
+            "device": {"coord_ms": coord_ms, "coord_gflops": 2.0 * products / (coord_ms * 1e-3) / 1e9,
+                       "hash_ms": hash_ms, "hash_gflops": 2.0 * products / (hash_ms * 1e-3) / 1e9,
+                       "coord_bytes_per_product_at_peak": coord_ms * 1e-3 * bw * 1e9 / products,
+                       "hbm_peak_gbs": bw, "hbm_peak_source": peak_src},
+            "nnz_C": nnzC, "products": products, "gpu_launches": int(launches * args.steps),
+            "e2e": {"value": e2e.get("dcsc_dcsr_coord", {}).get("gflops"), "unit": "GFLOP/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "calls": e2e,
+                    "path": "spws_dcsc_dcsr_coord_compute (taco_tensor_t DCSC x DCSR, host arrays)"},
+            "clocks": clk.summary()}
+    if parity is not None:
+        line["parity"] = parity
+    print(json.dumps(line), flush=True)
+
+
 TENSOR = dict(dims=(50000, 40000, 20000), nnz=20_000_000, zipf_s=1.1, seed=42)
+
+
+def bench_profile_case(args):
+    """Small, seeded runs of kernel families the headline workload does not
+    exercise, sized for an ncu capture (inputs larger than L2, a few GB on
+    the device at most). Each case runs its call --steps times and prints
+    one JSON line of sizes and times:
+      coord      coordinate workspace (expand, radix sort, run sums), banded 2^20
+      outer      DCSC x DCSR conversion + row-wise pipeline, banded 2^20
+      mttkrp     tensor bucket kernel, mode 0 (2M-nonzero Zipf tensor, rank --rank)
+      ttm        tensor bucket kernel, mode 1 (same tensor)
+      transpose  (A*A)^T fused and non-fused, R-MAT 2^--scale (default 15)
+      batched    the batched form on the 1024-instance workload"""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import build, gen, served
+    build.build()
+    sp.check(sp.lib().spws_set_device(0))
+    t0 = time.perf_counter()
+    out = {"workload": "profile", "case": args.case, "steps": args.steps}
+    if args.case in ("coord", "outer"):
+        A = gen.band(1 << 20, 8, 0.5, seed=42)  # the banded companion of the R-MAT config
+        for _ in range(args.steps):
+            Cm = sp.spgemm(A, A, "coord") if args.case == "coord" else sp.spgemm_outer(A, A, "hash")
+        out.update(matrix="band 2^20", nnz_A=int(len(A[1])), nnz_C=int(len(Cm[1])))
+    elif args.case == "batched":
+        dev = [sp.DeviceCsr.upload(*A) for A in gen.batch_instances(1024)]
+        for _ in range(args.steps):
+            b = sp.spgemm_batched(dev, dev)
+            out.update(instances=b.stats.instances, groups=b.stats.groups, products=b.stats.products,
+                       ms_kernels=b.stats.ms_kernels, ms_total=b.stats.ms_total)
+            b.release()
+    elif args.case == "transpose":
+        sc = args.scale or 15
+        A = gen.rmat(sc, 8, seed=42)
+        tp, tc, tv = sp._csr_transpose_np(*A)
+        At = sp.DeviceCsr.upload(tp, tc, tv, A[4], A[3])
+        Bd = sp.DeviceCsr.upload(*A)
+        for _ in range(args.steps):
+            for fuse in (True, False):
+                Cd, _, st = sp.spgemm_t_device(At, Bd, fuse=fuse)
+                Cd.release()
+                out["fused" if fuse else "nofuse"] = {
+                    "ms_input_transpose": st.ms_input_transpose, "ms_spgemm": st.ms_spgemm,
+                    "ms_output_transpose": st.ms_output_transpose, "ms_total": st.ms_total, "nnz": st.nnz}
+        out["matrix"] = f"rmat 2^{sc} degree 8"
+    else:
+        i0, i1, i2, tv = gen.tensor3((50000, 40000, 20000), 2_000_000, zipf_s=1.1, seed=42)
+        R = args.rank
+        if args.case == "mttkrp":
+            B = served.DeviceCsf3((i1, i2, i0, tv), (40000, 20000, 50000))
+            Cf, Df = served.DeviceFactor(gen.dense_factor(40000, R, seed=43)), served.DeviceFactor(
+                gen.dense_factor(20000, R, seed=44))
+            for _ in range(args.steps):
+                res, ms = served.mttkrp_device(B, Cf, Df, keep=True)
+                n = int(res.nnz)
+                served.coo_release(res)
+        else:
+            B = served.DeviceCsf3((i0, i2, i1, tv), (50000, 20000, 40000))
+            F = served.DeviceFactor(gen.dense_factor(20000, R, seed=45))
+            for _ in range(args.steps):
+                res, ms = served.ttm_device(B, F, keep=True)
+                n = int(res.nnz)
+                served.coo_release(res)
+        out.update(tensor="50000x40000x20000", nnz=len(tv), rank=R, output_nnz=n, last_call_ms=ms)
+    out["seconds"] = time.perf_counter() - t0
+    print(json.dumps(out), flush=True)
 
 
 def bench_tensor(args):
@@ -1138,7 +1386,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spws", choices=["spws", "reference"])
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "er", "band", "batched", "served", "mttkrp", "ttm", "transpose"])
+    ap.add_argument("--workload", default="rmat",
+                    choices=["rmat", "er", "band", "batched", "served", "mttkrp", "ttm", "transpose", "outer",
+                             "profile"])
+    ap.add_argument("--case", default="coord", choices=["coord", "outer", "mttkrp", "ttm", "transpose", "batched"],
+                    help="profile workload: the kernel family to run (small case for ncu)")
     ap.add_argument("--instances", type=int, default=1024,
                     help="batched workload: number of products (4096 holds ~220 GB of output at once)")
     ap.add_argument("--plain-sample", type=int, default=512, help="batched workload: one-at-a-time ABI sample")
@@ -1177,6 +1429,12 @@ def main():
     elif args.workload == "transpose":
         if rank == 0 and args.impl != "reference":
             bench_transpose(args)
+    elif args.workload == "outer":
+        if rank == 0 and args.impl != "reference":
+            bench_outer(args)
+    elif args.workload == "profile":
+        if rank == 0 and args.impl != "reference":
+            bench_profile_case(args)
     elif args.impl == "reference":
         bench_reference(args, ws, rank, dist)
     else:

@@ -30,8 +30,12 @@ typedef struct spws_csr_dev {
 /* How products are summed into an output entry.
  *  SPWS_ACCUM_ATOMIC: products are added with FP64 atomics in the order the
  *    GPU issues them (fastest path; order not fixed).
+ *  SPWS_ACCUM_COORD: the coordinate workspace (the reference's
+ *    DCSC_DCSR_coord_index_chase_flex.h): products are expanded as
+ *    (row, column) keys, stably radix-sorted and each run summed left to
+ *    right, i.e. in ascending j, bit for bit the reference's sequential sum.
  */
-enum { SPWS_ACCUM_ATOMIC = 0 };
+enum { SPWS_ACCUM_ATOMIC = 0, SPWS_ACCUM_COORD = 1 };
 
 typedef struct spws_spgemm_stats {
   int64_t products;      /* scalar products a_ij * b_jk (flops = 2 * products) */
@@ -63,6 +67,13 @@ int spws_csr_upload(const int32_t* pos, const int32_t* crd, const double* vals, 
                     spws_csr_dev* out);
 /* Copy a device CSR back into caller-provided host arrays (sizes from `m`). */
 int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double* vals);
+/* Copy the rows rows[0..nsel) of a device CSR into a compact host CSR: pos
+ * (nsel + 1 ints) is always filled; crd and vals receive the rows' entries in
+ * the order given, and need room for `cap` entries (SPWS_ERR_CAPACITY, with
+ * pos filled in, when they are more). For checking samples of a result too
+ * large to bring back whole. */
+int spws_csr_download_rows(const spws_csr_dev* m, const int32_t* rows, int32_t nsel, int32_t* pos, int32_t* crd,
+                           double* vals, int64_t cap);
 /* Overwrite the values of a device CSR with `m->nnz` host values (structure
  * unchanged), e.g. before re-solving a batch plan. */
 int spws_csr_set_values(const spws_csr_dev* m, const double* vals);
@@ -188,6 +199,16 @@ int spws_device_sync(void);
 
 /* Number of kernels this library has launched so far in this process. */
 unsigned long long spws_launch_count(void);
+
+/* Number of device allocations (stream-ordered pool blocks, server pools) and
+ * page-locked host buffers this library has made so far in this process. */
+unsigned long long spws_alloc_count(void);
+
+/* Failure injection on the host, for testing callers' error paths: the
+ * countdown-th device allocation from now on fails as if the device were out
+ * of memory (the entry point returns SPWS_ERR_NOMEM and frees what it had
+ * allocated); then injection disarms. 0 disarms it at once. */
+void spws_inject_alloc_failure(long long countdown);
 
 /* Overwrite `bytes` of scratch device memory (evicts the L2 between timed runs). */
 int spws_flush_l2(size_t bytes);

@@ -270,5 +270,90 @@ void COO_CSF_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, in
 
 #ifdef __cplusplus
 }
+
+/* ---- C++ callers: the reference's call forms, unedited -------------------
+ * The reference declares its wrappers with C++ default arguments and takes
+ * the collision count by reference; these redeclarations and overloads let
+ * its drivers compile against this header with only the include swapped. */
+
+/* bench = false, print = false: CSR_CSR_hash_sequential.h:355,
+ * CSR_CSR_taco.h:108, DCSC_DCSR_hash.h:361, DCSC_DCSR_taco.h:136,
+ * DCSC_DCSR_coord_index_chase_flex.h:381, COO_CSF_DCSR_DCSR_hash_free.h:369,
+ * COO_CSF_DCSR_DCSR_coord_bucket.h:408, _coord_index_chase_flex.h:382,
+ * COO_CSF_DCSR_hash_il.h:379, COO_CSF_DCSR_bucket_il.h:411,
+ * COO_CSF_DCSR_coord_il.h:395. */
+double CSR_CSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                    int32_t repeat, bool bench = false, bool print = false);
+double CSR_CSR_taco(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t warmup, int32_t repeat,
+                    bool bench = false, bool print = false);
+double DCSC_DCSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                      int32_t repeat, bool bench = false, bool print = false);
+double DCSC_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                        int32_t repeat, bool bench = false, bool print = false);
+void DCSC_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print = false);
+double DCSC_DCSR_taco(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t warmup, int32_t repeat,
+                      bool bench = false, bool print = false);
+double DCSC_DCSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                        int32_t repeat, bool bench = false, bool print = false);
+double DCSC_DCSR_T_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                          int32_t repeat, bool bench = false, bool print = false);
+void DCSC_DCSR_T_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print = false);
+double COO_CSF_DCSR_DCSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D, int32_t w_cap,
+                              int32_t warmup, int32_t repeat, bool bench = false, bool print = false);
+double COO_CSF_DCSR_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D,
+                                int32_t w_cap, int32_t warmup, int32_t repeat, bool bench = false,
+                                bool print = false);
+void COO_CSF_DCSR_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D, int32_t w_cap,
+                             bool print = false);
+double COO_CSF_DCSR_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                         int32_t repeat, bool bench = false, bool print = false);
+double COO_CSF_DCSR_bucket(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                           int32_t repeat, bool bench = false, bool print = false);
+void COO_CSF_DCSR_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print = false);
+
+/* `double CSC_CSR_T_hash(A, B, C, int w_cap, int& collisions)` of
+ * evaluate/CSC_CSR_T_hash_record.h:354 and `CSC_CSR_T_hash_nonfuse(A, B,
+ * C_noT, C, int w_cap, int& collisions)` of _nofuse.h:405: the count by
+ * reference, forwarded to the pointer forms above. */
+inline double CSC_CSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int w_cap, int& collisions) {
+  int32_t c = 0;
+  const double t = CSC_CSR_T_hash(A, B, C, (int32_t)w_cap, &c);
+  collisions = (int)c;
+  return t;
+}
+inline double CSC_CSR_T_hash_nonfuse(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C_noT, taco_tensor_t* C,
+                                     int w_cap, int& collisions) {
+  int32_t c = 0;
+  const double t = CSC_CSR_T_hash_nonfuse(A, B, C_noT, C, (int32_t)w_cap, &c);
+  collisions = (int)c;
+  return t;
+}
+
+/* The DCSC x DCSR transposed-output files (benchmark/DCSC_DCSR_T/) name their
+ * wrappers CSC_CSR_T_hash (DCSC_DCSR_T_hash.h:361, and the bucket file
+ * DCSC_DCSR_T_coord_bucket.h:404) and CSC_CSR_T_coord
+ * (DCSC_DCSR_T_coord_index_chase_flex.h:381); C++ tells them from the
+ * collision-counting form by their arguments. */
+inline double CSC_CSR_T_hash(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, int32_t warmup,
+                             int32_t repeat, bool bench = false, bool print = false) {
+#if defined(SPWSBUCKET)
+  return DCSC_DCSR_T_bucket(A, B, C, w_cap, warmup, repeat, bench, print);
+#else
+  return DCSC_DCSR_T_hash(A, B, C, w_cap, warmup, repeat, bench, print);
 #endif
+}
+inline void CSC_CSR_T_coord(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, int32_t w_cap, bool print = false) {
+  DCSC_DCSR_T_coord(A, B, C, w_cap, print);
+}
+
+/* The reference's bucket files reuse the hash wrappers' names
+ * (DCSC_DCSR_coord_bucket.h:404 and COO_CSF_DCSR_DCSR_coord_bucket.h:408 both
+ * define ..._hash). A driver compiled with -DSPWSBUCKET, the reference's own
+ * selector for the bucket workspace (bench_hash_outer_cc_noT.cpp:5), gets the
+ * bucket workspaces under those names. */
+#if defined(SPWSBUCKET)
+#define DCSC_DCSR_hash DCSC_DCSR_bucket
+#define COO_CSF_DCSR_DCSR_hash COO_CSF_DCSR_DCSR_bucket
+#endif
+#endif /* __cplusplus */
 #endif

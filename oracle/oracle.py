@@ -24,7 +24,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "libspws_oracle.so")
 PORT_O0_SO = os.path.join(HERE, "libspws_oracle_O0.so")
 REF_SO = os.path.join(HERE, "_ref", "libspws_ref.so")
-REF_ROOT_DEFAULT = "/root/reference"
 
 _libs = {}
 
@@ -50,11 +49,18 @@ def build_port_o0(force=False):
 
 
 def build_ref(ref_root=None, force=False):
-    """Compile the reference headers (needs the reference checkout)."""
-    ref_root = ref_root or os.environ.get("SPWS_REFERENCE_ROOT", REF_ROOT_DEFAULT)
-    if not os.path.isdir(ref_root):
+    """Compile the reference headers (needs the reference checkout). The
+    checkout is ref_root, else $SPWS_REFERENCE_ROOT, else the recipe's own
+    default (oracle/Makefile, REF); returns None where it is absent."""
+    ref_root = ref_root or os.environ.get("SPWS_REFERENCE_ROOT")
+    args = ["make", "-s", "-C", HERE, "ref"] + (["REF=" + ref_root] if ref_root else []) + (["-B"] if force else [])
+    if ref_root and not os.path.isdir(ref_root):
         return None
-    subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF=" + ref_root] + (["-B"] if force else []))
+    r = subprocess.run(args, capture_output=True, text=True)
+    if r.returncode != 0:
+        if "reference checkout not found" in r.stdout + r.stderr:
+            return None
+        raise RuntimeError(r.stdout + r.stderr)
     return REF_SO if os.path.exists(REF_SO) else None
 
 

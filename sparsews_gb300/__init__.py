@@ -106,6 +106,8 @@ def lib():
         "COO_CSF_DCSR_hash": ([P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_bool, C.c_bool], C.c_double),
         "spws_set_device": ([C.c_int], C.c_int),
         "spws_launch_count": ([], C.c_ulonglong),
+        "spws_alloc_count": ([], C.c_ulonglong),
+        "spws_inject_alloc_failure": ([C.c_longlong], None),
         "spws_flush_l2": ([C.c_size_t], C.c_int),
         "spws_measure_fp64": ([C.POINTER(C.c_double)], C.c_int),
         "spws_host_pin": ([C.c_void_p, C.c_size_t], C.c_int),
@@ -296,6 +298,23 @@ class DeviceCsr:
         vals = np.empty(max(self.m.nnz, 1), np.float64)
         check(L.spws_csr_download(C.byref(self.m), pos.ctypes.data, crd.ctypes.data, vals.ctypes.data))
         return pos, crd[: self.m.nnz], vals[: self.m.nnz]
+
+    def download_rows(self, rows):
+        """Rows `rows` of the matrix as a compact host CSR (pos, crd, vals)."""
+        L = lib()
+        rows = np.ascontiguousarray(rows, np.int32)
+        f = L.spws_csr_download_rows
+        f.argtypes = [C.POINTER(CsrDev), C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        f.restype = C.c_int
+        pos = np.empty(len(rows) + 1, np.int32)
+        st = f(C.byref(self.m), rows.ctypes.data, len(rows), pos.ctypes.data, None, None, 0)
+        if st not in (0, 4):
+            check(st)
+        n = int(pos[-1])
+        crd = np.empty(max(n, 1), np.int32)
+        vals = np.empty(max(n, 1), np.float64)
+        check(f(C.byref(self.m), rows.ctypes.data, len(rows), pos.ctypes.data, crd.ctypes.data, vals.ctypes.data, n))
+        return pos, crd[:n], vals[:n]
 
     def release(self):
         if self.owns and self.m.pos:

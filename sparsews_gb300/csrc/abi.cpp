@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "abi_util.h"
 #include "spws_internal.h"
@@ -237,6 +238,47 @@ int spws_csr_download(const spws_csr_dev* m, int32_t* pos, int32_t* crd, double*
   return SPWS_OK;
 }
 
+int spws_csr_download_rows(const spws_csr_dev* m, const int32_t* rows, int32_t nsel, int32_t* pos, int32_t* crd,
+                           double* vals, int64_t cap) {
+  clear_error();
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  if (!m || !pos || nsel < 0 || (nsel > 0 && !rows) || cap < 0 || (cap > 0 && (!crd || !vals)) || m->nrows < 0 ||
+      !m->pos) {
+    set_error("spws_csr_download_rows: bad arguments");
+    return SPWS_ERR_INVALID;
+  }
+  for (int32_t t = 0; t < nsel; t++)
+    if (rows[t] < 0 || rows[t] >= m->nrows) {
+      set_error("spws_csr_download_rows: row index out of range");
+      return SPWS_ERR_INVALID;
+    }
+  cudaStream_t s = ds->stream;
+  std::vector<int32_t> mpos((size_t)m->nrows + 1);
+  SPWS_TRY(copy_to_host(mpos.data(), m->pos, sizeof(int32_t) * mpos.size(), s));
+  pos[0] = 0;
+  for (int32_t t = 0; t < nsel; t++) {
+    const int32_t b = mpos[rows[t]], e = mpos[(size_t)rows[t] + 1];
+    if (b < 0 || e < b || (int64_t)e > m->nnz) {
+      set_error("spws_csr_download_rows: positions of the matrix are inconsistent");
+      return SPWS_ERR_INVALID;
+    }
+    pos[t + 1] = pos[t] + (e - b);
+  }
+  if ((int64_t)pos[nsel] > cap) {
+    set_error("spws_csr_download_rows: output capacity is smaller than the rows' entries (pos is filled in)");
+    return SPWS_ERR_CAPACITY;
+  }
+  for (int32_t t = 0; t < nsel; t++) {
+    const int32_t b = mpos[rows[t]], n = pos[t + 1] - pos[t];
+    if (n == 0) continue;
+    SPWS_CUDA(cudaMemcpyAsync(crd + pos[t], m->crd + b, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaMemcpyAsync(vals + pos[t], m->vals + b, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, s));
+  }
+  SPWS_CUDA(cudaStreamSynchronize(s));
+  return SPWS_OK;
+}
+
 
 int spws_spgemm_batched(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
                         spws_batch** batch, spws_batch_stats* stats) {
@@ -298,6 +340,11 @@ int spws_spgemm_csr_device(const spws_csr_dev* A, const spws_csr_dev* B, spws_cs
   // operands may have been filled by the caller: check them before any kernel indexes them
   SPWS_TRY(validate_csr_device(A->pos, A->crd, A->nrows, A->ncols, A->nnz, "A", ds->stream));
   if (B != A) SPWS_TRY(validate_csr_device(B->pos, B->crd, B->nrows, B->ncols, B->nnz, "B", ds->stream));
+  if (accum_mode == SPWS_ACCUM_COORD) return spgemm_coord(view(*A), view(*B), C, stats, ds->stream);
+  if (accum_mode != SPWS_ACCUM_ATOMIC) {
+    set_error("spws_spgemm_csr_device: unknown accumulation mode");
+    return SPWS_ERR_INVALID;
+  }
   SpgemmOpts opt;
   opt.accum_mode = accum_mode;
   return spgemm_rowwise(view(*A), view(*B), C, opt, stats, ds->stream);

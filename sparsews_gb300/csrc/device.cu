@@ -16,6 +16,11 @@ namespace spws {
 static thread_local std::string g_err;
 static unsigned long long g_launches = 0;  // kernels this library has launched (all threads)
 void count_launch(int n) { __atomic_fetch_add(&g_launches, (unsigned long long)n, __ATOMIC_RELAXED); }
+static unsigned long long g_allocs = 0;  // device and page-locked host allocations by this library
+void count_alloc() { __atomic_fetch_add(&g_allocs, 1ull, __ATOMIC_RELAXED); }
+// Host-side failure injection: when positive, the countdown-th next device
+// allocation fails as if the device were out of memory (then it disarms).
+static long long g_fail_alloc_in = 0;
 void set_error(const std::string& msg) { g_err = msg; }
 void clear_error() { g_err.clear(); }
 
@@ -61,6 +66,12 @@ void set_thread_pool(cudaMemPool_t pool) { t_pool = pool; }
 int dalloc(void** p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
   if (bytes == 0) bytes = 16;
+  if (__atomic_load_n(&g_fail_alloc_in, __ATOMIC_RELAXED) > 0 &&
+      __atomic_sub_fetch(&g_fail_alloc_in, 1, __ATOMIC_RELAXED) == 0) {
+    set_error("device allocation of " + std::to_string(bytes) + " bytes failed: injected failure");
+    return SPWS_ERR_NOMEM;
+  }
+  count_alloc();
   cudaError_t e = t_pool ? cudaMallocFromPoolAsync(p, bytes, t_pool, s) : cudaMallocAsync(p, bytes, s);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
@@ -94,6 +105,7 @@ __global__ void k_store_i64(long long* dst, long long v) { *dst = v; }
 int Readback::get(void* host, const void* dev, size_t bytes) {
   if (!t_staging.p) {
     void* p = nullptr;
+    count_alloc();
     SPWS_CUDA(cudaHostAlloc(&p, kStagingBytes, cudaHostAllocDefault));
     t_staging.p = static_cast<unsigned char*>(p);
   }
@@ -222,6 +234,10 @@ const char* spws_version(void) { return "spws-gb300 0.1 (sm_103a)"; }
 void spws_free(void* p) { free(p); }
 
 unsigned long long spws_launch_count(void) { return __atomic_load_n(&spws::g_launches, __ATOMIC_RELAXED); }
+unsigned long long spws_alloc_count(void) { return __atomic_load_n(&spws::g_allocs, __ATOMIC_RELAXED); }
+void spws_inject_alloc_failure(long long countdown) {
+  __atomic_store_n(&spws::g_fail_alloc_in, countdown > 0 ? countdown : 0, __ATOMIC_RELAXED);
+}
 
 }  // extern "C"
 
@@ -320,23 +336,38 @@ namespace spws {
 // validate_csr_device with the violation flag at a caller-provided device
 // address `bad` (one int) instead of a pool allocation. Synchronises `s`.
 int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
-                             const char* what, int* bad, cudaStream_t s) {
+                             const char* what, int* bad, cudaStream_t s, bool staged) {
   if (nrows < 0 || ncols < 0 || nnz < 0 || nnz > INT32_MAX) {
     set_error(std::string(what) + ": negative or oversized dimensions");
     return SPWS_ERR_INVALID;
   }
   int32_t ends[2] = {0, 0};
-  Readback rb(s);
-  SPWS_TRY(rb.get(&ends[0], pos, sizeof(int32_t)));
-  SPWS_TRY(rb.get(&ends[1], pos + nrows, sizeof(int32_t)));
-  SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
-  if (nrows > 0) {
-    launch_validate_csr(nrows, nnz, ncols, pos, crd, bad, s);
-    SPWS_CUDA(cudaGetLastError());
-  }
   int hbad = 0;
-  SPWS_TRY(rb.get(&hbad, bad, sizeof(int)));
-  SPWS_TRY(rb.wait());
+  if (staged) {
+    Readback rb(s);
+    SPWS_TRY(rb.get(&ends[0], pos, sizeof(int32_t)));
+    SPWS_TRY(rb.get(&ends[1], pos + nrows, sizeof(int32_t)));
+    SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+    if (nrows > 0) {
+      launch_validate_csr(nrows, nnz, ncols, pos, crd, bad, s);
+      SPWS_CUDA(cudaGetLastError());
+    }
+    SPWS_TRY(rb.get(&hbad, bad, sizeof(int)));
+    SPWS_TRY(rb.wait());
+  } else {
+    // Straight into the caller's stack: no page-locked staging buffer is
+    // allocated (the copies into pageable memory complete before the
+    // synchronisation below returns).
+    SPWS_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+    if (nrows > 0) {
+      launch_validate_csr(nrows, nnz, ncols, pos, crd, bad, s);
+      SPWS_CUDA(cudaGetLastError());
+    }
+    SPWS_CUDA(cudaMemcpyAsync(&ends[0], pos, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaMemcpyAsync(&ends[1], pos + nrows, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaStreamSynchronize(s));
+  }
   if (ends[0] != 0 || (int64_t)ends[1] != nnz) {
     set_error(std::string(what) + ": pos[0] must be 0 and pos[nrows] must equal nnz");
     return SPWS_ERR_INVALID;

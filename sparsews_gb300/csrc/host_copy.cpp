@@ -149,6 +149,7 @@ int copy_to_host(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   if (!r->init) {
     for (int b = 0; b < kRing; b++) {
       void* p = nullptr;
+      count_alloc();
       SPWS_CUDA(cudaHostAlloc(&p, kChunk, cudaHostAllocPortable));
       r->buf[b] = static_cast<char*>(p);
       SPWS_CUDA(cudaEventCreateWithFlags(&r->ev[b], cudaEventDisableTiming));

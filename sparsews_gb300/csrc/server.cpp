@@ -337,6 +337,7 @@ int spws_server_create(const spws_server_config* cfg, spws_server** out) {
   props.allocType = cudaMemAllocationTypePinned;
   props.location.type = cudaMemLocationTypeDevice;
   props.location.id = S->device;
+  spws::count_alloc();
   SPWS_CUDA(cudaMemPoolCreate(&S->pool, &props));
   uint64_t keep = UINT64_MAX;
   SPWS_CUDA(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep));

@@ -1485,6 +1485,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[64] = {};
 
+// The output count the int32 positions of C can address.
+inline bool noalloc_nnz_too_large(long long nnz) { return nnz > (long long)INT32_MAX; }
+
 // Device address of g_noalloc_scratch on the current device, looked up once
 // per device (the caller's first call on a device does this).
 int noalloc_scratch(unsigned char** out) {
@@ -1539,8 +1542,9 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
 
   const cudaStream_t s = cudaStreamPerThread;
   const int32_t nA = A->nrows;
-  SPWS_TRY(validate_csr_device_flag(A->pos, A->crd, A->nrows, A->ncols, A->nnz, "A", &hd->bad, s));
-  if (B != A) SPWS_TRY(validate_csr_device_flag(B->pos, B->crd, B->nrows, B->ncols, B->nnz, "B", &hd->bad, s));
+  SPWS_TRY(validate_csr_device_flag(A->pos, A->crd, A->nrows, A->ncols, A->nnz, "A", &hd->bad, s, false));
+  if (B != A)
+    SPWS_TRY(validate_csr_device_flag(B->pos, B->crd, B->nrows, B->ncols, B->nnz, "B", &hd->bad, s, false));
   if (nA == 0) {
     SPWS_CUDA(cudaMemsetAsync(C_pos, 0, sizeof(int32_t), s));
     SPWS_CUDA(cudaStreamSynchronize(s));
@@ -1593,6 +1597,10 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   *c_nnz = nnz;
   if (err == 2) {
     set_error("a row of A has 2^31 or more products");
+    return SPWS_ERR_CAPACITY;
+  }
+  if (noalloc_nnz_too_large(nnz)) {  // C_pos is int32: the numeric pass would index past C's arrays
+    set_error("output has more than INT32_MAX nonzeros; taco_tensor_t positions are int32");
     return SPWS_ERR_CAPACITY;
   }
   if (nnz > c_cap) {

@@ -19,6 +19,9 @@ void set_error(const std::string& msg);
 void clear_error();
 // Adds n to the count of kernels launched by this library (spws_launch_count).
 void count_launch(int n);
+// Adds one to the count of device and page-locked host allocations made by
+// this library (spws_alloc_count).
+void count_alloc();
 
 // Wraps a CUDA call: on failure records the message and returns SPWS_ERR_CUDA
 // (or SPWS_ERR_NOMEM for allocation failures) from the enclosing function.

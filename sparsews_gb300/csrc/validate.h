@@ -9,6 +9,8 @@ namespace spws {
 int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
                         const char* what, cudaStream_t s);
 // Same checks with the violation flag at a caller-provided device int.
+// staged = false reads the results back into stack variables instead of the
+// calling thread's page-locked staging buffer, so that nothing is allocated.
 int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
-                             const char* what, int* bad, cudaStream_t s);
+                             const char* what, int* bad, cudaStream_t s, bool staged = true);
 }  // namespace spws

@@ -112,3 +112,27 @@ def test_reference_arm_two_ranks_prints_once():
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
     assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["n_gpus"] == 2
+
+
+def test_parity_rows_accepts_the_oracle_and_flags_planted_mistakes():
+    """bench.py's parity leg: rows computed by the oracle itself pass; a
+    value pushed past the tolerance, or a column moved, is reported (the
+    mistakes are planted in a copy of the oracle's output, on the CPU)."""
+    import bench
+    from sparsews_gb300 import gen
+    A = gen.rmat(10, 8, seed=21)
+    rows = np.union1d(bench.cpu_sample_rows(A, 30000)[0], bench.heaviest_rows(A, 5))
+    assert len(bench.heaviest_rows(A, 5)) == 5
+    ref = bench.oracle_rows(A, A, rows, 3, "hash")
+    got = (ref[0].astype(np.int32), ref[1].copy(), ref[2].copy())
+    ok = bench.parity_rows(A, got, rows, 2)
+    assert ok["structure_exact"] and ok["within_tol"] and ok["max_cond_err"] <= 1e-12
+    assert ok["rows"] == len(rows) and ok["nnz"] == len(ref[1])
+    bad = (got[0], got[1], got[2].copy())
+    k = int(np.argmax(np.abs(bad[2])))
+    bad[2][k] *= 1 + 1e-9
+    r = bench.parity_rows(A, bad, rows, 2)
+    assert r["structure_exact"] and not r["within_tol"] and r["max_rel_err"] > 1e-10
+    moved = (got[0], got[1].copy(), got[2])
+    moved[1][0] += 1
+    assert not bench.parity_rows(A, moved, rows, 2)["structure_exact"]
