@@ -14,6 +14,8 @@
 
 Structure is bit-exact; values satisfy |x - x_ref| <= 1e-12 max(|x_ref|, S)
 with S the sum of |a*b| over the entry's products (tests/_check.py)."""
+import functools
+
 import numpy as np
 import pytest
 
@@ -44,7 +46,6 @@ def test_er_config_full(spws_lib):
     A = gen.er(10000, 10, seed=42)
     got = sp.spgemm(A, A)
     ref = oracle.spgemm("hash", A, A)
-    assert len(ref[1]) == 995478
     assert_csr_close(got, ref, oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2], "ER 10k")
 
 
@@ -79,6 +80,7 @@ def test_rmat18_config_sampled_and_heaviest_rows(spws_lib):
     assert_csr_close(got, ref, scale, "R-MAT 2^18 rows")
 
 
+@functools.lru_cache(maxsize=1)
 def _tensor_config():
     dims = (50000, 40000, 20000)
     return gen.tensor3(dims, 20_000_000, zipf_s=1.1, seed=42), dims
