@@ -258,3 +258,76 @@ def ttm(method, Bcsf, dims, Cf, w_cap=None, kind="port", timing=None):
     if rc != 0:
         raise RuntimeError(f"oracle ttm failed rc={rc}")
     return taco.take_coo(A, 3, fr)
+
+
+# ---- the reference's file loaders (utils/dataloader.h, unmodified, FP64) ----
+REF_LOADERS_SO = os.path.join(HERE, "_ref", "libspws_ref_loaders.so")
+
+
+def ref_loaders():
+    """The compiled reference loaders, or None where the reference checkout
+    was not available to build them (oracle/Makefile target `ref`)."""
+    if "loaders" not in _libs:
+        if not os.path.exists(REF_LOADERS_SO):
+            return None
+        L = C.CDLL(REF_LOADERS_SO)
+        I, D = C.POINTER(C.POINTER(C.c_int)), C.POINTER(C.POINTER(C.c_double))
+        pi = C.POINTER(C.c_int)
+        L.ref_read_mtx_csr.argtypes = [C.c_char_p, C.c_int, pi, pi, pi, I, I, I, D]
+        L.ref_read_mtx_csc.argtypes = [C.c_char_p, pi, pi, pi, I, I, I, D]
+        L.ref_read_mtx_csr_keep_value.argtypes = [C.c_char_p, C.c_int, pi, pi, pi, I, I, D]
+        L.ref_read_txt_coo3.argtypes = [C.c_char_p, C.c_int, pi, I, I, I, D]
+        L.ref_loader_free.argtypes = [C.c_void_p]
+        _libs["loaders"] = L
+    return _libs["loaders"]
+
+
+def _take_ref(L, p, n, dtype):
+    out = np.ctypeslib.as_array(p, shape=(max(n, 1),))[:n].astype(dtype, copy=True) if n else np.zeros(0, dtype)
+    L.ref_loader_free(C.cast(p, C.c_void_p))
+    return out
+
+
+def ref_read_mtx(path, keep_values=False, one_based=True):
+    """read_mtx_csr / read_mtx_csr_keep_value of the reference: (pos, crd,
+    vals, nrow, ncol). Random values come from the C library's rand(): seed
+    it (srand) before the call to compare two loaders."""
+    L = ref_loaders()
+    nr, nc, nz = C.c_int(), C.c_int(), C.c_int()
+    p, c, r = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_int)()
+    v = C.POINTER(C.c_double)()
+    if keep_values:
+        L.ref_read_mtx_csr_keep_value(os.fsencode(path), int(one_based), C.byref(nr), C.byref(nc), C.byref(nz),
+                                      C.byref(p), C.byref(c), C.byref(v))
+    else:
+        L.ref_read_mtx_csr(os.fsencode(path), int(one_based), C.byref(nr), C.byref(nc), C.byref(nz), C.byref(p),
+                           C.byref(c), C.byref(r), C.byref(v))
+        _take_ref(L, r, nz.value, np.int32)
+    return (_take_ref(L, p, nr.value + 1, np.int32), _take_ref(L, c, nz.value, np.int32),
+            _take_ref(L, v, nz.value, np.float64), nr.value, nc.value)
+
+
+def ref_read_mtx_csc(path):
+    """read_mtx_csc of the reference: (pos, crd, vals, nrow, ncol)."""
+    L = ref_loaders()
+    nr, nc, nz = C.c_int(), C.c_int(), C.c_int()
+    p, c, r = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_int)()
+    v = C.POINTER(C.c_double)()
+    L.ref_read_mtx_csc(os.fsencode(path), C.byref(nr), C.byref(nc), C.byref(nz), C.byref(p), C.byref(c), C.byref(r),
+                       C.byref(v))
+    _take_ref(L, r, nz.value, np.int32)
+    return (_take_ref(L, p, nc.value + 1, np.int32), _take_ref(L, c, nz.value, np.int32),
+            _take_ref(L, v, nz.value, np.float64), nr.value, nc.value)
+
+
+def ref_read_tns(path, one_based=True):
+    """read_txt_coo3 of the reference: sorted COO (c0, c1, c2, vals)."""
+    L = ref_loaders()
+    nz = C.c_int()
+    a, b, c = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_int)()
+    v = C.POINTER(C.c_double)()
+    L.ref_read_txt_coo3(os.fsencode(path), int(one_based), C.byref(nz), C.byref(a), C.byref(b), C.byref(c),
+                        C.byref(v))
+    n = nz.value
+    return (_take_ref(L, a, n, np.int32), _take_ref(L, b, n, np.int32), _take_ref(L, c, n, np.int32),
+            _take_ref(L, v, n, np.float64))
