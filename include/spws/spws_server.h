@@ -144,6 +144,7 @@ typedef struct spws_server_stats {
   uint64_t reserved;     /* bytes reserved now (running workspaces + unreleased results) */
   uint64_t peak_reserved;
   int64_t admit_waits;   /* reservations that had to wait for memory */
+  int64_t cancelled;     /* requests that finished with SPWS_ERR_CANCELLED */
 } spws_server_stats;
 
 /* Start a server on the current device. `cfg` may be NULL (all defaults). */
@@ -171,6 +172,15 @@ int spws_server_result_coo(spws_server* s, int64_t ticket, spws_coo_dev* A);
  * the caller queued on its own streams that reads the result must be complete. */
 int spws_server_release(spws_server* s, int64_t ticket);
 int spws_server_get_stats(spws_server* s, spws_server_stats* st);
+/* Cancel a request that has not finished. A queued request is withdrawn at
+ * once; a running one stops at its next phase boundary (a SpGEMM between its
+ * symbolic pass and its numeric pass, before its output is admitted; kernels
+ * already launched finish first) or, past that point, completes normally.
+ * Either way the caller still waits for the ticket (status
+ * SPWS_ERR_CANCELLED when it was stopped) and releases it. SPWS_ERR_INVALID
+ * for an unknown ticket or one that has already finished. The reference has
+ * no counterpart: it runs one product per call with no queue. */
+int spws_server_cancel(spws_server* s, int64_t ticket);
 
 #ifdef __cplusplus
 }

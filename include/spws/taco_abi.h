@@ -68,9 +68,10 @@ typedef enum spws_status {
   SPWS_ERR_NOMEM = 2,     /* host or device allocation failed */
   SPWS_ERR_CUDA = 3,      /* a CUDA call failed (message has the detail) */
   SPWS_ERR_CAPACITY = 4,  /* a result exceeds an int32 index or a fixed bound */
-  SPWS_ERR_TIMEOUT = 5,   /* a bounded device wait gave up */
+  SPWS_ERR_TIMEOUT = 5,   /* a bounded wait gave up (spws_server_wait / spws_server_wait_any) */
   SPWS_ERR_NO_DEVICE = 6, /* no CUDA device visible */
-  SPWS_ERR_BUSY = 7       /* admission refused (served form) */
+  SPWS_ERR_BUSY = 7,      /* admission refused (served form) */
+  SPWS_ERR_CANCELLED = 8  /* the request was cancelled (served form, spws_server_cancel) */
 } spws_status;
 
 const char* spws_status_string(int status);

@@ -220,9 +220,10 @@ const char* spws_status_string(int status) {
     case SPWS_ERR_NOMEM: return "out of memory";
     case SPWS_ERR_CUDA: return "CUDA error";
     case SPWS_ERR_CAPACITY: return "capacity exceeded";
-    case SPWS_ERR_TIMEOUT: return "device wait timed out";
+    case SPWS_ERR_TIMEOUT: return "wait timed out";
     case SPWS_ERR_NO_DEVICE: return "no CUDA device";
     case SPWS_ERR_BUSY: return "admission refused";
+    case SPWS_ERR_CANCELLED: return "cancelled";
     default: return "unknown status";
   }
 }

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -64,6 +65,7 @@ struct Request {
   bool large = false;     // lane: large requests run time-sliced on low-priority streams
   bool done = false;
   bool reported = false;  // returned by spws_server_wait / wait_any
+  std::atomic<bool> cancel{false};  // spws_server_cancel on a running request: stop at the next phase boundary
   size_t held = 0;        // bytes the result holds in the budget
 };
 
@@ -99,7 +101,7 @@ struct spws_server {
   std::mutex validate_mu;
   int64_t next_ticket = 1;
   size_t reserved = 0, peak = 0;
-  int64_t submitted = 0, completed = 0, failed = 0, running = 0, admit_waits = 0;
+  int64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, running = 0, admit_waits = 0;
   bool stopping = false;
   std::vector<std::thread> threads;
 
@@ -166,8 +168,15 @@ struct spws_server {
     return SPWS_OK;
   }
 
+  static int stop_if_cancelled(const spws::Request* r) {
+    if (!r->cancel.load()) return SPWS_OK;
+    spws::set_error("request " + std::to_string(r->ticket) + " was cancelled");
+    return SPWS_ERR_CANCELLED;
+  }
+
   int run_spgemm(spws::Request* r, cudaStream_t st) {
     const double deadline = r->info.t_start + admit_timeout_ms * 1e-3;
+    SPWS_TRY(stop_if_cancelled(r));
     SPWS_TRY(validate_once(r->A, "A", st));
     SPWS_TRY(validate_once(r->B, "B", st));
     const int32_t n = r->A.nrows;
@@ -183,6 +192,7 @@ struct spws_server {
     const size_t plan_bytes = rc == SPWS_OK ? plan.scratch_bytes : 0;
     unreserve_locked(ws - std::min(ws, plan_bytes + pos_bytes));
     size_t out_bytes = 0;
+    if (rc == SPWS_OK) rc = stop_if_cancelled(r);  // between the passes: before the output is admitted
     if (rc == SPWS_OK) {
       out_bytes = 12 * (size_t)plan.nnz;
       rc = reserve(out_bytes, deadline);
@@ -214,6 +224,7 @@ struct spws_server {
 
   int run_ttm(spws::Request* r, cudaStream_t st) {
     const double deadline = r->info.t_start + admit_timeout_ms * 1e-3;
+    SPWS_TRY(stop_if_cancelled(r));
     SPWS_TRY(spws::check_csf3(&r->T));
     SPWS_TRY(spws::check_factor(&r->F));
     size_t out_bound = 0;
@@ -276,6 +287,8 @@ struct spws_server {
       running--;
       if (rc == SPWS_OK)
         completed++;
+      else if (rc == SPWS_ERR_CANCELLED)
+        cancelled++;
       else
         failed++;
       if (stopping) free_result(r);  // nobody will read it
@@ -539,6 +552,33 @@ int spws_server_release(spws_server* S, int64_t ticket) {
   return SPWS_OK;
 }
 
+int spws_server_cancel(spws_server* S, int64_t ticket) {
+  spws::clear_error();
+  if (!S) return SPWS_ERR_INVALID;
+  std::lock_guard<std::mutex> g(S->mu);
+  Request* r = S->find(ticket);
+  if (!r) return SPWS_ERR_INVALID;
+  if (r->done) {
+    spws::set_error("request " + std::to_string(ticket) + " has already finished");
+    return SPWS_ERR_INVALID;
+  }
+  for (auto* q : {&S->queue, &S->queue_large}) {
+    auto it = std::find(q->begin(), q->end(), r);
+    if (it == q->end()) continue;
+    q->erase(it);  // not started: it finishes now, having held nothing
+    r->info.status = SPWS_ERR_CANCELLED;
+    r->info.t_start = r->info.t_done = spws::now_s();
+    r->error = "request " + std::to_string(ticket) + " was cancelled before it started";
+    r->done = true;
+    S->cancelled++;
+    S->finished.push_back(ticket);
+    S->cv_done.notify_all();
+    return SPWS_OK;
+  }
+  r->cancel.store(true);  // running: its worker stops it at the next phase boundary
+  return SPWS_OK;
+}
+
 int spws_server_get_stats(spws_server* S, spws_server_stats* st) {
   spws::clear_error();
   if (!S || !st) return SPWS_ERR_INVALID;
@@ -546,6 +586,7 @@ int spws_server_get_stats(spws_server* S, spws_server_stats* st) {
   st->submitted = S->submitted;
   st->completed = S->completed;
   st->failed = S->failed;
+  st->cancelled = S->cancelled;
   st->queued = (int64_t)(S->queue.size() + S->queue_large.size());
   st->running = S->running;
   st->budget = S->budget;

@@ -51,7 +51,7 @@ class RequestInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
                 ("running", C.c_int64), ("budget", C.c_uint64), ("reserved", C.c_uint64),
-                ("peak_reserved", C.c_uint64), ("admit_waits", C.c_int64)]
+                ("peak_reserved", C.c_uint64), ("admit_waits", C.c_int64), ("cancelled", C.c_int64)]
 
 
 _bound = False
@@ -85,6 +85,7 @@ def _lib():
         "spws_server_result_csr": ([C.c_void_p, C.c_int64, C.POINTER(CsrDev)], C.c_int),
         "spws_server_result_coo": ([C.c_void_p, C.c_int64, C.POINTER(CooDev)], C.c_int),
         "spws_server_release": ([C.c_void_p, C.c_int64], C.c_int),
+        "spws_server_cancel": ([C.c_void_p, C.c_int64], C.c_int),
         "spws_server_get_stats": ([C.c_void_p, C.POINTER(ServerStats)], C.c_int),
     }
     for name, (argt, rest) in sig.items():
@@ -230,6 +231,11 @@ class Server:
 
     def release(self, ticket):
         check(_lib().spws_server_release(self.h, ticket))
+
+    def cancel(self, ticket):
+        """Withdraw a queued request or stop a running one at its next phase
+        boundary; wait for and release the ticket as usual."""
+        check(_lib().spws_server_cancel(self.h, ticket))
 
     def stats(self):
         st = ServerStats()

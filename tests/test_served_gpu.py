@@ -178,3 +178,49 @@ def test_served_time_sliced_kernels_match(spws_lib):
             assert_csr_close(got, alone[i], scale, f"sliced {i}")
         srv.release(t)
     srv.close()
+
+
+def test_cancel_queued_and_running_requests(spws_lib):
+    """One worker: a large product runs while small ones queue behind it.
+    Cancelling queued requests withdraws them (SPWS_ERR_CANCELLED, nothing
+    held); cancelling the running one stops it between its passes or lets it
+    complete; every other result is unaffected and the budget returns to
+    zero once all tickets are released."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import served
+    CANCELLED = 8
+    big = gen.rmat(17, 16, seed=95)  # long enough that the small requests are still queued
+    small = [gen.poisson_rows(800 + 50 * t, 6.0, seed=96 + t) for t in range(8)]
+    dbig = sp.DeviceCsr.upload(*big)
+    dsmall = [sp.DeviceCsr.upload(*A) for A in small]
+    srv = served.Server(workers=1, large_workers=1)
+    t_big = srv.submit_spgemm(dbig, dbig)
+    t_small = [srv.submit_spgemm(d, d) for d in dsmall]
+    for t in t_small[::2]:  # queued behind the large product
+        srv.cancel(t)
+    srv.cancel(t_big)
+    info = srv.wait(t_big, raise_on_error=False)
+    assert info.status in (0, CANCELLED)
+    for k, t in enumerate(t_small):
+        info = srv.wait(t, raise_on_error=False)
+        if k % 2 == 0:
+            assert info.status == CANCELLED and info.reserved == 0
+            with pytest.raises(sp.SpwsError):  # no result to read
+                srv.result_csr(t)
+        else:
+            assert info.status == 0
+            got = srv.result_csr(t).download()
+            A = small[k]
+            assert_csr_close(got, oracle.spgemm("hash", A, A), oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2],
+                             f"small {k}")
+    with pytest.raises(sp.SpwsError):  # a finished request cannot be cancelled
+        srv.cancel(t_small[1])
+    st = srv.stats()
+    assert st.cancelled >= len(t_small[::2]) and st.completed + st.cancelled + st.failed == 1 + len(t_small)
+    for t in [t_big] + t_small:
+        srv.release(t)
+    assert srv.stats().reserved == 0
+    srv.close()
+    dbig.release()
+    for d in dsmall:
+        d.release()
