@@ -41,33 +41,70 @@ __global__ void k_row_products(int32_t nA, const int32_t* __restrict__ Ap, const
   if (lane == 0) prods[w] = p;
 }
 
-// Warp per row of the chunk: writes the row's products in (j, k) order at
-// its offset in the chunk buffer.
-__global__ void k_expand(int32_t r0, int32_t r1, const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
-                         const double* __restrict__ Av, const int32_t* __restrict__ Bp,
-                         const int32_t* __restrict__ Bk, const double* __restrict__ Bv, int32_t ncols,
-                         const long long* __restrict__ poff, unsigned long long* __restrict__ keys,
-                         unsigned long long* __restrict__ vals) {
+// B-row length of every A entry (the entry's product count).
+__global__ void k_entry_products(int64_t nnzA, const int32_t* __restrict__ Aj, const int32_t* __restrict__ Bp,
+                                 int32_t* __restrict__ len) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nnzA) len[q] = Bp[Aj[q] + 1] - Bp[Aj[q]];
+}
+
+// Warp per 32 consecutive A entries of the chunk (entries [q0, q1), rows
+// [r0, r1)), whatever rows they belong to, so a heavy row is spread over many
+// warps: lane l takes entry q0 + 32w + l, finds its row, and the warp writes
+// the entries' products as one flat stream at the group's offset (eoff: each
+// entry's product offset over the whole matrix, base: the chunk's). The
+// stream is in (row, j, k) order, as the reference's loop visits it.
+__global__ void k_expand(int32_t r0, int32_t r1, int64_t q0, int64_t q1, const int32_t* __restrict__ Ap,
+                         const int32_t* __restrict__ Aj, const double* __restrict__ Av,
+                         const int32_t* __restrict__ Bp, const int32_t* __restrict__ Bk,
+                         const double* __restrict__ Bv, int32_t ncols, const long long* __restrict__ eoff,
+                         long long base, unsigned long long* __restrict__ keys, unsigned long long* __restrict__ vals) {
   const int lane = threadIdx.x & 31;
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t i = r0 + w;
-  if (i >= r1) return;
-  long long out = poff[i] - poff[r0];
-  const unsigned long long rowkey = (unsigned long long)(i - r0) * (unsigned long long)ncols;
-  for (int32_t qb = Ap[i]; qb < Ap[i + 1]; qb += 32) {
-    Slice sl{0, 0, 0.0};
-    const int32_t q = qb + lane;
-    if (q < Ap[i + 1]) {
-      const int32_t j = Aj[q];
-      sl.s = Bp[j];
-      sl.len = Bp[j + 1] - sl.s;
-      sl.a = Av[q];
+  const int64_t qg = q0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+  if (qg >= q1) return;
+  const int64_t q = qg + lane;
+  int32_t s = 0, len = 0;
+  double a = 0.0;
+  unsigned long long rowkey = 0;
+  if (q < q1) {
+    int32_t lo = r0, hi = r1 - 1;  // the row holding entry q: largest i with Ap[i] <= q
+    while (lo < hi) {
+      const int32_t m = (lo + hi + 1) >> 1;
+      if ((int64_t)Ap[m] <= q) lo = m; else hi = m - 1;
     }
-    const int total = warp_expand_indexed(sl, [&](int f, int32_t p, double a) {
-      keys[out + f] = rowkey + (unsigned long long)Bk[p];
-      vals[out + f] = __double_as_longlong(__dmul_rn(a, Bv[p]));
-    });
-    out += total;
+    const int32_t j = Aj[q];
+    s = Bp[j];
+    len = Bp[j + 1] - s;
+    a = Av[q];
+    rowkey = (unsigned long long)(lo - r0) * (unsigned long long)ncols;
+  }
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int excl = incl - len;
+  const long long out = eoff[qg] - base;
+  for (int b = 0; b < total; b += 32) {
+    const int f = b + lane;
+    int owner = 0;  // largest lane whose products start at or before f
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int cand = owner + step;
+      const int ex = __shfl_sync(0xffffffffu, excl, cand & 31);
+      if (cand < 32 && ex <= f) owner = cand;
+    }
+    const int o_excl = __shfl_sync(0xffffffffu, excl, owner);
+    const int o_s = __shfl_sync(0xffffffffu, s, owner);
+    const double o_a = __shfl_sync(0xffffffffu, a, owner);
+    const unsigned long long o_key = __shfl_sync(0xffffffffu, rowkey, owner);
+    if (f < total) {
+      const int32_t p = o_s + (f - o_excl);
+      keys[out + f] = o_key + (unsigned long long)Bk[p];
+      vals[out + f] = __double_as_longlong(__dmul_rn(o_a, Bv[p]));
+    }
   }
 }
 
@@ -127,19 +164,31 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
   long long* poff = nullptr;
   int32_t* rowcnt = nullptr;
   long long* tot = nullptr;
+  int32_t* elen = nullptr;
+  long long* eoff = nullptr;
+  const int64_t nnzA = A.nnz;
   SPWS_TRY(dalloc((void**)&prods, sizeof(long long) * (size_t)std::max(nA, 1), s));
   SPWS_TRY(dalloc((void**)&poff, sizeof(long long) * ((size_t)nA + 1), s));
   SPWS_TRY(dalloc((void**)&rowcnt, sizeof(int32_t) * (size_t)std::max(nA, 1), s));
   SPWS_TRY(dalloc((void**)&tot, sizeof(long long), s));
+  SPWS_TRY(dalloc((void**)&elen, sizeof(int32_t) * (size_t)std::max<int64_t>(nnzA, 1), s));
+  SPWS_TRY(dalloc((void**)&eoff, sizeof(long long) * ((size_t)nnzA + 1), s));
   SPWS_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int32_t) * (size_t)std::max(nA, 1), s));
   if (nA > 0) {
     k_row_products<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A.pos, A.crd, B.pos, prods);
     count_launch(1);
   }
+  if (nnzA > 0) {
+    k_entry_products<<<(unsigned)((nnzA + 255) / 256), 256, 0, s>>>(nnzA, A.crd, B.pos, elen);
+    count_launch(1);
+  }
+  SPWS_TRY(scan_i32_to_i64(elen, eoff, nnzA, tot, s));
   SPWS_TRY(scan_i64(prods, poff, nA, tot, s));
   SPWS_CUDA(cudaMemcpyAsync(poff + nA, tot, sizeof(long long), cudaMemcpyDeviceToDevice, s));
   std::vector<long long> hoff((size_t)nA + 1);
+  std::vector<int32_t> hApos((size_t)nA + 1);
   SPWS_CUDA(cudaMemcpyAsync(hoff.data(), poff, sizeof(long long) * ((size_t)nA + 1), cudaMemcpyDeviceToHost, s));
+  SPWS_CUDA(cudaMemcpyAsync(hApos.data(), A.pos, sizeof(int32_t) * ((size_t)nA + 1), cudaMemcpyDeviceToHost, s));
   SPWS_CUDA(cudaStreamSynchronize(s));
   const long long total_products = hoff[nA];
 
@@ -180,8 +229,10 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
     const int32_t r0 = cuts[c], r1 = cuts[c + 1];
     const long long n = hoff[r1] - hoff[r0];
     if (n == 0) continue;
-    k_expand<<<(unsigned)((r1 - r0 + 7) / 8), 256, 0, s>>>(r0, r1, A.pos, A.crd, A.vals, B.pos, B.crd, B.vals, ncols,
-                                                            poff, k0, v0);
+    const int64_t q0 = hApos[r0], q1 = hApos[r1];  // the chunk's A entries
+    const int64_t groups = (q1 - q0 + 31) / 32;
+    k_expand<<<(unsigned)((groups + 7) / 8), 256, 0, s>>>(r0, r1, q0, q1, A.pos, A.crd, A.vals, B.pos, B.crd, B.vals,
+                                                         ncols, eoff, hoff[r0], k0, v0);
     count_launch(1);
     bool in_tmp = false;
     const int bits = bits_for((unsigned long long)(r1 - r0) * (unsigned long long)std::max(ncols, 1));
@@ -242,7 +293,7 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  dfree(prods, s); dfree(poff, s); dfree(rowcnt, s); dfree(tot, s);
+  dfree(prods, s); dfree(poff, s); dfree(rowcnt, s); dfree(tot, s); dfree(elen, s); dfree(eoff, s);
   return rc;
 }
 
