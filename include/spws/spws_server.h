@@ -97,6 +97,21 @@ int spws_ttm_device(const spws_csf3_dev* B, const spws_factor_dev* F, spws_coo_d
  * order-2 COO allocated by the library (release with spws_coo_release). */
 int spws_mttkrp_device(const spws_csf3_dev* B, const spws_factor_dev* C, const spws_factor_dev* D, spws_coo_dev* A,
                        float* ms);
+/* Arithmetic of the MTTKRP / TTM bucket sums, for every tensor entry point
+ * of this library (the TACO ones, the device ones and the served form):
+ *  SPWS_TENSOR_SUM_FAST (default): each leaf's term is accumulated with a
+ *    fused multiply-add, b*C(k,j) times D(l,j) plus the running sum for
+ *    MTTKRP, b times C(i,l) plus the running sum for TTM: one FP64
+ *    instruction fewer per leaf and column; values within 1e-12 relative of
+ *    the reference (the tolerance of the parity tests).
+ *  SPWS_TENSOR_SUM_EXACT: the reference's arithmetic
+ *    (COO_CSF_DCSR_DCSR_hash_free.h:307, COO_CSF_DCSR_hash_il.h:317): each
+ *    term rounded, then added in visiting order; bit-exact with the
+ *    reference's sequential sums wherever it did not flush its workspace.
+ * Process-wide; returns SPWS_ERR_INVALID for any other value. */
+enum { SPWS_TENSOR_SUM_FAST = 0, SPWS_TENSOR_SUM_EXACT = 1 };
+int spws_set_tensor_summation(int32_t mode);
+
 /* Copy a device COO into caller host arrays (crd[d] for d < order, vals). */
 int spws_coo_download(const spws_coo_dev* A, int32_t* crd0, int32_t* crd1, int32_t* crd2, double* vals);
 /* Release a COO allocated by spws_ttm_device / spws_mttkrp_device (not a

@@ -20,9 +20,11 @@
 #include <algorithm>
 #include <climits>
 #include <string>
+#include <type_traits>
 
 #include "convert.h"
 #include "sort.h"
+#include "spws/spws_server.h"
 #include "spws_internal.h"
 #include "tensor.h"
 
@@ -226,7 +228,26 @@ __global__ void k_all_present(int32_t rows, int32_t R, int32_t mw, const uint32_
 // half-warp its own piece, for ranks of at most 16 (one column per lane),
 // which would otherwise leave half of every warp idle; the sums and their
 // order are the same.
-template <int MODE, int JPL, int LW = 32>
+// One leaf's term added into a column's running sum. FMA = false keeps the
+// reference's arithmetic: (b * C(k,j)) * D(l,j) for MTTKRP
+// (COO_CSF_DCSR_DCSR_hash_free.h:307), b * C(i,l) for TTM
+// (COO_CSF_DCSR_hash_il.h:317), each rounded, then added (the first term is
+// stored, not added): bit for bit the reference's sum in visiting order.
+// FMA = true fuses the last multiply with the add (one FP64 instruction
+// fewer per leaf and column, the terms rounded once instead of twice); the
+// result stays within the 1e-12 relative bound of the parity tests.
+template <int MODE, bool FMA>
+__device__ __forceinline__ double leaf_update(double acc, bool started, double bb, double d0, double d1) {
+  if (FMA) {
+    const double base = started ? acc : 0.0;
+    return MODE == 0 ? __fma_rn(__dmul_rn(bb, d0), d1, base) : __fma_rn(bb, d0, base);
+  }
+  double t0 = __dmul_rn(bb, d0);
+  if (MODE == 0) t0 = __dmul_rn(t0, d1);
+  return started ? __dadd_rn(acc, t0) : t0;
+}
+
+template <int MODE, int JPL, int LW = 32, bool FMA = false>
 __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, const long long* __restrict__ pstart,
                          const long long* __restrict__ starts, const int32_t* __restrict__ r0,
                          const int32_t* __restrict__ r1, const double* __restrict__ bv, Factor F0, Factor F1, int32_t R,
@@ -278,9 +299,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
           d1 = F1.dense[(int64_t)x1 * F1.R + j];
         }
         if (!(((m0 & m1) >> (j & 31)) & 1u)) continue;
-        double t0 = __dmul_rn(bb, d0);
-        if (MODE == 0) t0 = __dmul_rn(t0, d1);
-        acc[u] = ((started >> u) & 1u) ? __dadd_rn(acc[u], t0) : t0;
+        acc[u] = leaf_update<MODE, FMA>(acc[u], (started >> u) & 1u, bb, d0, d1);
         started |= 1u << u;
       }
     }
@@ -333,7 +352,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
 // writes a piece out when its last leaf is summed. Same sums in the same
 // order as k_pieces; the bucket set-up that dominated a two-leaf piece is
 // paid once per G pieces.
-template <int MODE>
+template <int MODE, bool FMA = false>
 __global__ void k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const int32_t* __restrict__ pseg,
                                  const long long* __restrict__ pstart, const long long* __restrict__ starts,
                                  const int32_t* __restrict__ r0, const int32_t* __restrict__ r1,
@@ -421,9 +440,7 @@ __global__ void k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const 
         d1 = F1.dense[(int64_t)x1 * F1.R + j];
       }
       if (!(((m0 & m1) >> (j & 31)) & 1u)) continue;
-      double t0 = __dmul_rn(bb, d0);
-      if (MODE == 0) t0 = __dmul_rn(t0, d1);
-      acc = started ? __dadd_rn(acc, t0) : t0;
+      acc = leaf_update<MODE, FMA>(acc, started, bb, d0, d1);
       started = true;
     }
   }
@@ -568,6 +585,19 @@ size_t tensor_bucket_bound(int mode, const Csf3Dev& B, int32_t R, size_t* out_by
   const size_t outn = std::min(nseg * (size_t)std::max(R, 0), (size_t)INT32_MAX);
   if (out_bytes) *out_bytes = outn * (mode == 0 ? 16 : 20);
   return ws;
+}
+
+static int g_tensor_sum = SPWS_TENSOR_SUM_FAST;
+
+bool tensor_sum_exact() { return __atomic_load_n(&g_tensor_sum, __ATOMIC_RELAXED) == SPWS_TENSOR_SUM_EXACT; }
+
+int set_tensor_sum(int mode) {
+  if (mode != SPWS_TENSOR_SUM_FAST && mode != SPWS_TENSOR_SUM_EXACT) {
+    set_error("spws_set_tensor_summation: unknown mode");
+    return SPWS_ERR_INVALID;
+  }
+  __atomic_store_n(&g_tensor_sum, mode, __ATOMIC_RELAXED);
+  return SPWS_OK;
 }
 
 int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const FactorDense* F1, CooOut* out,
@@ -719,33 +749,35 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
             segval.as<double>(), segmask.as<uint32_t>(), direct);
       };
       const bool grouped = direct_out && jpl <= 1 && npieces > 0 && nnz <= 8 * npieces;
-      if (grouped) {  // tiny buckets: G pieces per warp
+      auto launch_grouped = [&](auto kernel) {  // tiny buckets: G pieces per warp
         constexpr int G = 8;
         const int64_t warps = (npieces + G - 1) / G;
         const unsigned gg = (unsigned)((warps + 7) / 8);
-        if (mode == 0)
-          k_pieces_grouped<0><<<gg, 256, 0, s>>>(npieces, G, nnz, pseg.as<int32_t>(), pstart.as<long long>(),
-                                                 starts.as<long long>(), r0.as<int32_t>(), r1.as<int32_t>(),
-                                                 bv.as<double>(), f0, f1, R, mw, pw, partial.as<double>(),
-                                                 pmask.as<uint32_t>(), direct);
-        else
-          k_pieces_grouped<1><<<gg, 256, 0, s>>>(npieces, G, nnz, pseg.as<int32_t>(), pstart.as<long long>(),
-                                                 starts.as<long long>(), r0.as<int32_t>(), r1.as<int32_t>(),
-                                                 bv.as<double>(), f0, f1, R, mw, pw, partial.as<double>(),
-                                                 pmask.as<uint32_t>(), direct);
-      } else if (mode == 0) {
-        if (R <= 16) launch_half(k_pieces<0, 1, 16>);
-        else if (jpl <= 1) launch(k_pieces<0, 1>);
-        else if (jpl == 2) launch(k_pieces<0, 2>);
-        else if (jpl == 4) launch(k_pieces<0, 4>);
-        else launch(k_pieces<0, 8>);
-      } else {
-        if (R <= 16) launch_half(k_pieces<1, 1, 16>);
-        else if (jpl <= 1) launch(k_pieces<1, 1>);
-        else if (jpl == 2) launch(k_pieces<1, 2>);
-        else if (jpl == 4) launch(k_pieces<1, 4>);
-        else launch(k_pieces<1, 8>);
-      }
+        kernel<<<gg, 256, 0, s>>>(npieces, G, nnz, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
+                                  r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>(), f0, f1, R, mw, pw,
+                                  partial.as<double>(), pmask.as<uint32_t>(), direct);
+      };
+      auto dispatch = [&](auto fma) {
+        constexpr bool F = decltype(fma)::value;
+        if (grouped) {
+          if (mode == 0) launch_grouped(k_pieces_grouped<0, F>);
+          else launch_grouped(k_pieces_grouped<1, F>);
+        } else if (mode == 0) {
+          if (R <= 16) launch_half(k_pieces<0, 1, 16, F>);
+          else if (jpl <= 1) launch(k_pieces<0, 1, 32, F>);
+          else if (jpl == 2) launch(k_pieces<0, 2, 32, F>);
+          else if (jpl == 4) launch(k_pieces<0, 4, 32, F>);
+          else launch(k_pieces<0, 8, 32, F>);
+        } else {
+          if (R <= 16) launch_half(k_pieces<1, 1, 16, F>);
+          else if (jpl <= 1) launch(k_pieces<1, 1, 32, F>);
+          else if (jpl == 2) launch(k_pieces<1, 2, 32, F>);
+          else if (jpl == 4) launch(k_pieces<1, 4, 32, F>);
+          else launch(k_pieces<1, 8, 32, F>);
+        }
+      };
+      if (tensor_sum_exact()) dispatch(std::false_type{});
+      else dispatch(std::true_type{});
       k_combine<<<(unsigned)((nseg + 255) / 256), 256, 0, s>>>(nseg, mode, poff.as<long long>(), partial.as<double>(),
                                                            pmask.as<uint32_t>(), R, j0, mw, pw, segval.as<double>(),
                                                            segmask.as<uint32_t>(), direct);
@@ -787,3 +819,8 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
 }
 
 }  // namespace spws
+
+extern "C" int spws_set_tensor_summation(int32_t mode) {
+  spws::clear_error();
+  return spws::set_tensor_sum(mode);
+}

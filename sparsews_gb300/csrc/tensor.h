@@ -44,6 +44,10 @@ struct CooOut {
 };
 
 int densify_factor(const DcsrDev& f, FactorDense* out, cudaStream_t s);
+
+// The bucket sums' arithmetic (spws_set_tensor_summation): true = the
+// reference's multiply-then-add, bit-exact; false = fused multiply-add.
+bool tensor_sum_exact();
 void free_factor(FactorDense* f, cudaStream_t s);
 
 // mode 0: MTTKRP A(i,j) = sum B(k,l,i) F0(k,j) F1(l,j)  -> COO (i, j)

@@ -86,6 +86,7 @@ def _lib():
         "spws_server_result_coo": ([C.c_void_p, C.c_int64, C.POINTER(CooDev)], C.c_int),
         "spws_server_release": ([C.c_void_p, C.c_int64], C.c_int),
         "spws_server_cancel": ([C.c_void_p, C.c_int64], C.c_int),
+        "spws_set_tensor_summation": ([C.c_int32], C.c_int),
         "spws_server_get_stats": ([C.c_void_p, C.POINTER(ServerStats)], C.c_int),
     }
     for name, (argt, rest) in sig.items():
@@ -174,6 +175,16 @@ def mttkrp_device(B, Cf, Df, keep=False):
         return _download_coo(out), ms.value
     finally:
         L.spws_coo_release(C.byref(out))
+
+
+SUM_FAST, SUM_EXACT = 0, 1
+
+
+def set_tensor_summation(mode):
+    """SUM_FAST (fused multiply-add, the default) or SUM_EXACT (the
+    reference's multiply-then-add, bit-exact); applies to every tensor entry
+    point of the library."""
+    check(_lib().spws_set_tensor_summation(mode))
 
 
 def coo_release(out):

@@ -83,7 +83,9 @@ def test_served_same_alone_and_in_mix(spws_lib):
 
     (rk, rj, rl), rv = oracle.ttm("hash", Bc, dims, Ff, w_cap=BIG)
     assert np.array_equal(ttm_alone[0][0], rk) and np.array_equal(ttm_alone[0][2], rl)
-    assert np.array_equal(ttm_alone[1], rv)
+    (_, _, _), scale = oracle.ttm("hash", Bc[:3] + (np.abs(Bc[3]),), dims, (Ff[0], Ff[1], np.abs(Ff[2]), Ff[3], Ff[4]),
+                                  w_cap=BIG)
+    assert_vals_close(ttm_alone[1], rv, scale, "served TTM vs oracle")
 
 
 def test_served_admission_holds_budget(spws_lib):

@@ -17,6 +17,16 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 BIG = 1 << 26  # oracle capacity that never flushes at these sizes
 
 
+@pytest.fixture
+def exact_sums(spws_lib):
+    """The reference's multiply-then-add arithmetic for the bucket sums
+    (bit-exact); the default fused multiply-add is restored afterwards."""
+    from sparsews_gb300 import served
+    served.set_tensor_summation(served.SUM_EXACT)
+    yield
+    served.set_tensor_summation(served.SUM_FAST)
+
+
 def csr(z, p):
     n, m = (int(x) for x in z[p + "_shape"])
     return z[p + "_pos"], z[p + "_crd"], z[p + "_vals"], n, m
@@ -28,10 +38,11 @@ def abs_f(F):
 
 @pytest.mark.parametrize("R", [4, 16])
 @pytest.mark.parametrize("method", ["hash", "bucket"])
-def test_mttkrp_golden(spws_lib, R, method):
+def test_mttkrp_golden(spws_lib, exact_sums, R, method):
     """Against the reference's own output. Its small default capacity flushes
     the workspace, which splits some sums, so values are compared within the
-    tolerance; against the never-flushing sequential order they are bit-exact."""
+    tolerance; against the never-flushing sequential order they are bit-exact
+    (with the reference's arithmetic selected)."""
     import sparsews_gb300 as sp
     z = np.load(os.path.join(GOLD, f"mttkrp_R{R}_s17.npz"))
     dims = tuple(int(x) for x in z["dims"])
@@ -46,7 +57,7 @@ def test_mttkrp_golden(spws_lib, R, method):
 
 
 @pytest.mark.parametrize("method", ["hash", "bucket"])
-def test_ttm_golden(spws_lib, method):
+def test_ttm_golden(spws_lib, exact_sums, method):
     import sparsews_gb300 as sp
     z = np.load(os.path.join(GOLD, "ttm_R4_s17.npz"))
     dims = tuple(int(x) for x in z["dims"])
@@ -138,10 +149,42 @@ def test_ttm_against_oracle(spws_lib, R):
     dims = (500, 300, 400)
     Cf = gen.dense_factor(300, R, seed=78)
     Bc = (i0, i2, i1, tv)
+    from sparsews_gb300 import served
     (gk, gj, gl), gv = sp.ttm(Bc, dims, Cf)
     (rk, rj, rl), rv = oracle.ttm("hash", Bc, dims, Cf, w_cap=BIG)
     assert np.array_equal(gk, rk) and np.array_equal(gj, rj) and np.array_equal(gl, rl)
-    assert np.array_equal(gv, rv)  # no bucket is split at this size: bit-exact
+    (_, _, _), scale = oracle.ttm("hash", (i0, i2, i1, np.abs(tv)), dims, abs_f(Cf), w_cap=BIG)
+    assert_vals_close(gv, rv, scale, "ttm, fused multiply-add")
+    served.set_tensor_summation(served.SUM_EXACT)
+    try:
+        (_, _, _), gx = sp.ttm(Bc, dims, Cf)
+    finally:
+        served.set_tensor_summation(served.SUM_FAST)
+    assert np.array_equal(gx, rv)  # no bucket is split at this size: bit-exact
+
+
+def test_mttkrp_fma_and_exact_sums(spws_lib):
+    """Both arithmetic modes against the oracle: the fused multiply-add within
+    the tolerance, the reference's arithmetic bit for bit; structure the same."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import served
+    i0, i1, i2, tv = gen.tensor3((2000, 600, 300), 50000, zipf_s=1.1, seed=85)
+    dims = (600, 300, 2000)
+    Cf, Df = gen.dense_factor(600, 32, seed=86), gen.dense_factor(300, 32, seed=87)
+    Bc = (i1, i2, i0, tv)
+    (ri, rj), rv = oracle.mttkrp("hash", Bc, dims, Cf, Df, w_cap=BIG)
+    (_, _), scale = oracle.mttkrp("hash", (i1, i2, i0, np.abs(tv)), dims, abs_f(Cf), abs_f(Df), w_cap=BIG)
+    (fi, fj), fv = sp.mttkrp(Bc, dims, Cf, Df)
+    assert np.array_equal(fi, ri) and np.array_equal(fj, rj)
+    assert_vals_close(fv, rv, scale, "mttkrp, fused multiply-add")
+    served.set_tensor_summation(served.SUM_EXACT)
+    try:
+        (xi, xj), xv = sp.mttkrp(Bc, dims, Cf, Df)
+    finally:
+        served.set_tensor_summation(served.SUM_FAST)
+    assert np.array_equal(xi, ri) and np.array_equal(xj, rj) and np.array_equal(xv, rv)
+    with pytest.raises(sp.SpwsError):
+        served.set_tensor_summation(7)
 
 
 def test_tensor_empty_and_invalid(spws_lib):
