@@ -121,11 +121,15 @@ __global__ void k_run_starts(int64_t n, const int32_t* __restrict__ head, const 
   if (head[p]) starts[hpos[p]] = p;
 }
 
-// One thread per run: sum the run left to right, emit (row, col, value).
+// One thread per run: sum the run left to right, emit (col, value). Runs are
+// in (row, column) order, so a row's runs are consecutive: the first run of
+// a row records its index in first[row], and the row's count is taken from
+// that by k_row_counts (no per-run atomic on a shared counter: the runs of a
+// heavy row would all serialise on it).
 __global__ void k_reduce_runs(int64_t nruns, int64_t n, const long long* __restrict__ starts,
                               const unsigned long long* __restrict__ keys, const unsigned long long* __restrict__ vals,
-                              int32_t ncols, int32_t r0, int32_t* __restrict__ out_crd, double* __restrict__ out_val,
-                              int32_t* __restrict__ rowcnt) {
+                              int32_t ncols, int32_t* __restrict__ out_crd, double* __restrict__ out_val,
+                              long long* __restrict__ first) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nruns) return;
   const long long s = starts[r];
@@ -133,9 +137,21 @@ __global__ void k_reduce_runs(int64_t nruns, int64_t n, const long long* __restr
   double v = __longlong_as_double((long long)vals[s]);
   for (long long q = s + 1; q < e; q++) v = __dadd_rn(v, __longlong_as_double((long long)vals[q]));
   const unsigned long long k = keys[s];
-  out_crd[r] = (int32_t)(k % (unsigned long long)ncols);
+  const unsigned long long row = k / (unsigned long long)ncols;
+  out_crd[r] = (int32_t)(k - row * (unsigned long long)ncols);
   out_val[r] = v;
-  atomicAdd(&rowcnt[r0 + (int32_t)(k / (unsigned long long)ncols)], 1);
+  if (r == 0 || keys[starts[r - 1]] / (unsigned long long)ncols != row) first[row] = r;
+}
+
+// The last run of each row writes the row's output count.
+__global__ void k_row_counts(int64_t nruns, const long long* __restrict__ starts,
+                             const unsigned long long* __restrict__ keys, int32_t ncols, int32_t r0,
+                             const long long* __restrict__ first, int32_t* __restrict__ rowcnt) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nruns) return;
+  const unsigned long long row = keys[starts[r]] / (unsigned long long)ncols;
+  if (r + 1 == nruns || keys[starts[r + 1]] / (unsigned long long)ncols != row)
+    rowcnt[r0 + (int32_t)row] = (int32_t)(r + 1 - first[row]);
 }
 
 int bits_for(unsigned long long max_key_exclusive) {
@@ -203,7 +219,11 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
     cuts.push_back(std::min(r1, nA));
   }
   long long max_chunk = 0;
-  for (size_t c = 0; c + 1 < cuts.size(); c++) max_chunk = std::max(max_chunk, hoff[cuts[c + 1]] - hoff[cuts[c]]);
+  int32_t max_rows = 1;
+  for (size_t c = 0; c + 1 < cuts.size(); c++) {
+    max_chunk = std::max(max_chunk, hoff[cuts[c + 1]] - hoff[cuts[c]]);
+    max_rows = std::max(max_rows, cuts[c + 1] - cuts[c]);
+  }
   const size_t cap = (size_t)std::max<long long>(max_chunk, 1);
 
   unsigned long long *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr;
@@ -216,6 +236,8 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
   SPWS_TRY(dalloc((void**)&head, sizeof(int32_t) * cap, s));
   SPWS_TRY(dalloc((void**)&hpos, sizeof(long long) * cap, s));
   SPWS_TRY(dalloc((void**)&starts, sizeof(long long) * cap, s));
+  long long* first = nullptr;  // per row of a chunk: its first run
+  SPWS_TRY(dalloc((void**)&first, sizeof(long long) * (size_t)max_rows, s));
 
   struct Part {
     int32_t* crd;
@@ -250,15 +272,17 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
     Part pt{nullptr, nullptr, nruns};
     if ((rc = dalloc((void**)&pt.crd, sizeof(int32_t) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
     if ((rc = dalloc((void**)&pt.val, sizeof(double) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
-    k_reduce_runs<<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, n, starts, ks, vs, ncols, r0, pt.crd, pt.val,
-                                                                  rowcnt);
-    count_launch(1);
+    // first run of each row of the chunk (rows without products keep the count 0 they started with)
+    k_reduce_runs<<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, n, starts, ks, vs, ncols, pt.crd, pt.val,
+                                                                  first);
+    k_row_counts<<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, starts, ks, ncols, r0, first, rowcnt);
+    count_launch(2);
     SPWS_CUDA(cudaGetLastError());
     parts.push_back(pt);
     nnz += nruns;
   }
   dfree(k0, s); dfree(v0, s); dfree(k1, s); dfree(v1, s);
-  dfree(head, s); dfree(hpos, s); dfree(starts, s);
+  dfree(head, s); dfree(hpos, s); dfree(starts, s); dfree(first, s);
   if (rc == SPWS_OK && nnz > INT32_MAX) {
     set_error("output has more than INT32_MAX nonzeros");
     rc = SPWS_ERR_CAPACITY;
