@@ -1091,12 +1091,13 @@ def bench_tensor(args):
                     else "spws_coo_csf_dcsr_bucket_compute") + " (taco_tensor_t, host arrays)"}
     cpu = None if args.no_cpu else tensor_cpu_baseline(args.workload, coo, dims, facs, args.cpu_tensor_nnz)
 
-    # FP64 term: the bucket sums are (b*C)*D + acc (MTTKRP) and b*C + acc (TTM) per
-    # leaf and column, kept as separate multiplies and adds for the reference's
-    # rounding: 3 or 2 FP64 instructions, against the FMA peak's two flops each
+    # FP64 term: per leaf and column the default (fused) bucket sums are
+    # fma(b*C, D, acc) for MTTKRP and fma(b, C, acc) for TTM: 2 or 1 FP64
+    # instructions, against the FMA peak's two flops each (the reference's
+    # separate multiplies and adds, the exact mode, would be 3 or 2)
     fp64 = C.c_double(0.0)
     fp64_peak = fp64.value if L.spws_measure_fp64(C.byref(fp64)) == 0 and fp64.value > 0 else None
-    ops = (3.0 if args.workload == "mttkrp" else 2.0) * R * nnz
+    ops = (2.0 if args.workload == "mttkrp" else 1.0) * R * nnz
     ceilings = {"hbm": alg / (bw * 1e9) * 1e3}
     if fp64_peak:
         ceilings["fp64_instructions"] = ops / (fp64_peak / 2.0 * 1e9) * 1e3

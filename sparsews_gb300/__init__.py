@@ -43,10 +43,11 @@ class BatchStats(C.Structure):
 class Tuning(C.Structure):
     """spws_tuning: zero fields take the defaults."""
     _fields_ = [("light_max", C.c_int32), ("long_min", C.c_int32), ("wide_windows", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("heavy_sums", C.c_int32)]
 
     def __repr__(self):
-        return f"Tuning(light_max={self.light_max}, long_min={self.long_min}, wide_windows={self.wide_windows})"
+        return (f"Tuning(light_max={self.light_max}, long_min={self.long_min}, wide_windows={self.wide_windows}, "
+                f"heavy_sums={self.heavy_sums})")
 
 
 class SpgemmStats(C.Structure):

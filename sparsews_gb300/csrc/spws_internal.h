@@ -76,6 +76,9 @@ struct SpgemmOpts {
   int light_max = 512;        // rows with fewer products go to the warp-per-row kernel (power of two <= 512)
   int long_min = 128;         // B-row slices this long are cut into pieces, shorter ones packed (<= 256)
   bool wide_windows = false;  // numeric windows of 18432 ranks at 1 CTA/SM instead of 5120 at 2 CTAs/SM
+  // Heavy rows' sums: 0 = FP64 reductions straight into C.vals (in L2);
+  // 1 = shared-memory rank windows (wide_windows picks their width).
+  int heavy_sums = 0;
   // Per A row, an amount subtracted from every column written for that row
   // (the batched form writes each instance's own columns); nullptr: none.
   const int32_t* col_shift = nullptr;

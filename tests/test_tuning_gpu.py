@@ -11,7 +11,9 @@ from sparsews_gb300 import gen
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = [(lm, ln, w) for w in (0, 1) for lm in (512, 256) for ln in (128, 64, 256)]
+# (light_max, long_min, wide_windows, heavy_sums): sums in C.vals, then the two shared-window widths
+CANDIDATES = [(lm, ln, 0, 0) for lm in (512, 256) for ln in (128, 64, 256)] + \
+    [(lm, ln, w, 1) for w in (0, 1) for lm in (512, 256) for ln in (128, 64, 256)]
 
 
 def hub_matrix(n=40000, seed=7):
@@ -35,24 +37,24 @@ def test_every_candidate_tuning_matches_oracle(spws_lib):
     ref = oracle.spgemm("taco", A, A)
     scale = oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2]
     assert np.diff(ref[0]).max() > 18432  # the hub rows need several windows of either size
-    for lm, ln, w in CANDIDATES:
-        C, st = sp.spgemm_device(d, d, tuning=sp.Tuning(lm, ln, w, 0))
+    for lm, ln, w, h in CANDIDATES:
+        C, st = sp.spgemm_device(d, d, tuning=sp.Tuning(lm, ln, w, h))
         got = C.download()
         C.release()
-        assert st.chunk_width == (18432 if w else 5120)
-        assert_csr_equal_structure(got, ref, f"tuning {lm},{ln},{w}")
-        assert_csr_close(got, ref, scale, f"tuning {lm},{ln},{w}")
+        assert st.chunk_width == (0 if h == 0 else (18432 if w else 5120))
+        assert_csr_equal_structure(got, ref, f"tuning {lm},{ln},{w},{h}")
+        assert_csr_close(got, ref, scale, f"tuning {lm},{ln},{w},{h}")
 
 
 def test_autotune_returns_a_candidate(spws_lib):
     import sparsews_gb300 as sp
     d = sp.DeviceCsr.upload(*gen.rmat(12, 16, seed=3))
     t, ms = sp.autotune(d, d)
-    assert (t.light_max, t.long_min, t.wide_windows) in CANDIDATES and ms > 0
+    assert (t.light_max, t.long_min, t.wide_windows, t.heavy_sums) in CANDIDATES and ms > 0
     insts = [gen.poisson_rows(n, 8.0, seed=n) for n in (300, 900, 2000, 4000)] * 3
     dev = [sp.DeviceCsr.upload(*A) for A in insts]
     tb, msb = sp.autotune_batched(dev, dev, sample=6)
-    assert (tb.light_max, tb.long_min, tb.wide_windows) in CANDIDATES and msb > 0
+    assert (tb.light_max, tb.long_min, tb.wide_windows, tb.heavy_sums) in CANDIDATES and msb > 0
     b = sp.spgemm_batched(dev, dev, tuning=tb)
     for i, A in enumerate(insts):
         got = b.download(i)
@@ -64,7 +66,7 @@ def test_autotune_returns_a_candidate(spws_lib):
 def test_invalid_tuning_rejected(spws_lib):
     import sparsews_gb300 as sp
     d = sp.DeviceCsr.upload(*gen.poisson_rows(100, 4.0, seed=1))
-    for bad in (sp.Tuning(300, 0, 0, 0), sp.Tuning(1024, 0, 0, 0), sp.Tuning(0, 512, 0, 0)):
+    for bad in (sp.Tuning(300, 0, 0, 0), sp.Tuning(1024, 0, 0, 0), sp.Tuning(0, 512, 0, 0), sp.Tuning(0, 0, 0, 2)):
         with pytest.raises(sp.SpwsError):
             sp.spgemm_device(d, d, tuning=bad)
 
