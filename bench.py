@@ -546,14 +546,14 @@ def batch_workload(count, seed=42):
     return gen.batch_instances(count, seed)
 
 
-def bench_batched(args):
+def run_batched(args, insts=None, tune=True):
     import sparsews_gb300 as sp
     from sparsews_gb300 import build, taco
     build.build()
     L = sp.lib()
     sp.check(L.spws_set_device(0))
     t0 = time.perf_counter()
-    insts = batch_workload(args.instances)
+    insts = insts if insts is not None else batch_workload(args.instances)
     gen_s = time.perf_counter() - t0
     dev = [sp.DeviceCsr.upload(*A) for A in insts]
     for _ in range(args.warmup):
@@ -634,7 +634,11 @@ def bench_batched(args):
                                 "sample": f"{k} random instances of the batch ({prods} products) on {threads} "
                                           f"threads, {secs:.1f} s",
                                 "gflops": 2.0 * prods / secs / 1e9}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def bench_batched(args):
+    print(json.dumps(run_batched(args)), flush=True)
 
 
 # (A*A)^T suite of the transposed-output comparison: output nnz from ~1e4 to

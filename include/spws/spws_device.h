@@ -156,13 +156,15 @@ int spws_batch_release(spws_batch* batch);
  *  long_min:     B-row slices at least this long are cut into 256-entry
  *                pieces, one warp each; shorter ones are packed into one
  *                lane-dense stream ([32, 256]; default 128).
- *  wide_windows: with heavy_sums = 1: 1 = numeric windows of 18432 output
- *                ranks with one CTA per SM; 0 = windows of 5120 ranks with
- *                two CTAs per SM.
- *  heavy_sums:   where the 512-thread kernel sums a heavy row: 0 (default) =
- *                FP64 reductions straight into C.vals, which the L2 executes
- *                (no rank windows, three CTAs per SM); 1 = shared-memory
- *                windows of output ranks, written out window by window. */
+ *  wide_windows: 1 = shared-memory windows of 18432 output ranks with one
+ *                CTA per SM; 0 = windows of 5120 ranks with two CTAs per SM.
+ *  heavy_sums:   how the 512-thread kernel sums a heavy row: 0 (default) =
+ *                rows of at most 16384 output entries by FP64 reductions
+ *                straight into C.vals, which the L2 executes (one pass, no
+ *                windows), larger rows in shared-memory windows of output
+ *                ranks; 1 = windows for every row; 2 = every row by
+ *                reductions into C.vals (three CTAs per SM; wide_windows
+ *                unused). */
 typedef struct spws_tuning {
   int32_t light_max;
   int32_t long_min;
@@ -171,8 +173,8 @@ typedef struct spws_tuning {
 } spws_tuning;
 
 /* Autotuner: runs the pipeline on A*B with every candidate tuning (light_max
- * in {256, 512} x long_min in {64, 128, 256} x {sums in C.vals, shared
- * windows of 5120 ranks, shared windows of 18432 ranks}),
+ * in {256, 512} x long_min in {64, 128, 256} x wide_windows in {0, 1} x
+ * heavy_sums in {0, 1}),
  * `repeats` times each (>= 1), and returns the fastest by wall time in *best
  * (and its time in *best_ms, may be NULL). The products are discarded. */
 int spws_autotune_spgemm(const spws_csr_dev* A, const spws_csr_dev* B, int32_t repeats, spws_tuning* best,

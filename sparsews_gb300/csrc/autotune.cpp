@@ -51,8 +51,8 @@ int to_opts(const spws_tuning* t, SpgemmOpts* o) {
     o->long_min = t->long_min;
   }
   o->wide_windows = t->wide_windows != 0;
-  if (t->heavy_sums != 0 && t->heavy_sums != 1) {
-    set_error("tuning.heavy_sums must be 0 (sums in C.vals) or 1 (shared-memory windows)");
+  if (t->heavy_sums < 0 || t->heavy_sums > 2) {
+    set_error("tuning.heavy_sums must be 0 (small rows in C.vals), 1 (windows) or 2 (all in C.vals)");
     return SPWS_ERR_INVALID;
   }
   o->heavy_sums = t->heavy_sums;
@@ -61,11 +61,10 @@ int to_opts(const spws_tuning* t, SpgemmOpts* o) {
 
 std::vector<spws_tuning> candidates() {
   std::vector<spws_tuning> c;
-  for (int lm : {512, 256})
-    for (int ln : {128, 64, 256}) c.push_back(spws_tuning{lm, ln, 0, 0});  // sums in C.vals
-  for (int wide : {0, 1})
-    for (int lm : {512, 256})
-      for (int ln : {128, 64, 256}) c.push_back(spws_tuning{lm, ln, wide, 1});  // shared-memory windows
+  for (int heavy : {0, 1})
+    for (int wide : {0, 1})
+      for (int lm : {512, 256})
+        for (int ln : {128, 64, 256}) c.push_back(spws_tuning{lm, ln, wide, heavy});
   return c;
 }
 

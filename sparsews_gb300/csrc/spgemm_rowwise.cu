@@ -195,6 +195,10 @@ struct PassArgs {
   long long yield_ns;
   int yield_ctas;
   int long_min;  // B-row slices at least this long are cut into pieces; shorter ones are packed (<= 256)
+  // k_numeric: spans with at most this many output ranks are summed by FP64
+  // reductions straight into C.vals (one pass, no windows); larger ones in
+  // shared-memory rank windows. 0: always windows.
+  int l2_rank_max;
   const int32_t* col_shift;  // per A row, subtracted from the written columns (nullptr: none)
 };
 
@@ -214,6 +218,8 @@ __device__ __forceinline__ int claim_or_yield(int* counter, const PassArgs& a, u
 constexpr int kPieceLen = 256;   // B entries per warp work piece of a long slice
 constexpr int kLongMin = 128;    // default: slices this long are cut into pieces; shorter ones are packed
 constexpr int kLongMinMax = 256; // packed stream length < 512 * 256 fits the 17-bit field of fill_batch
+constexpr int kL2RankMax = 16384; // default PassArgs::l2_rank_max: 128 KB of C.vals per CTA in L2
+static_assert(kL2RankMax < 65536, "L2-pass ranks are taken from the 16-bit word prefixes");
 static_assert(kThreads * (kLongMinMax - 1) < (1 << 17), "short slices (< long_min entries) fill at most 17 bits");
 constexpr int kChunkLen = 128;   // packed entries per warp work item (4 rounds of 32 lanes)
 
@@ -652,6 +658,31 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
         while (need-- > 0) word &= word - 1;
         return wlo + lo * 32 + (__ffs(word) - 1);
       };
+      if (nnz_w <= a.l2_rank_max) {
+        // One pass with the sums in C.vals (in L2): the span's output range
+        // is small enough that every CTA's range stays in L2 together
+        // (l2_rank_max ranks of 8 bytes per CTA), and the L2's FP64
+        // reductions outpace shared-memory FP64 atomics. No windows, so no
+        // B-slice clipping, no per-window batch set-up and no write-back.
+        // The zeroing stores precede every reduction (the barrier orders them).
+        double* cv = a.Cv + out;
+        for (int r = threadIdx.x; r < nnz_w; r += kThreads) cv[r] = 0.0;
+        __syncthreads();
+        const int32_t span_hi = multi ? span_end(wlo) : INT_MAX;
+        for (int32_t qb = q0; qb < q1; qb += kThreads) {
+          const BatchWork bw = load_batch(a, qb, q1, true, multi, wlo, span_hi, b, wsum);
+          // a rank below l2_rank_max <= 65535 follows from the 16-bit word prefixes alone
+          for_batch_entries<true>(b, bw, a.Bk, a.Bv, [&](int32_t col, double bv, double av) {
+            const int k = col - wlo;
+            const int w = k >> 5;
+            const uint16_t rank = (uint16_t)(wpre[w] + __popc(bm[w] & ((1u << (k & 31)) - 1u)));
+            atomicAdd(cv + rank, __dmul_rn(av, bv));
+          });
+          __syncthreads();
+        }
+        out += nnz_w;
+        continue;
+      }
       const int nwin = (nnz_w + ACC - 1) / ACC;
       const int nj = q1 - q0;
       const int32_t span_hi = multi ? span_end(wlo) : INT_MAX;
@@ -1326,7 +1357,7 @@ struct RowwisePlanImpl {
   int waves_sym = 1, waves_num = 1;
   int light_bucket = kLightBucket;
   bool wide = false;
-  int heavy_sums = 0;  // 0: k_numeric_l2 (sums in C.vals), 1: k_numeric (shared-memory rank windows)
+  int heavy_sums = 0;  // 0: k_numeric, small spans in C.vals; 1: k_numeric, windows only; 2: k_numeric_l2
 
   // CTA waves for a pass that runs `rate` products per microsecond, so that
   // each wave lasts about one time slice (1 = persistent launch).
@@ -1455,10 +1486,11 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   pa.err = &sm->err;
   pa.long_min = opt.long_min;
   pa.col_shift = opt.col_shift;
+  pa.l2_rank_max = opt.heavy_sums == 0 ? kL2RankMax : 0;
   RowKernelCfg& kc = P->kc;
   SPWS_TRY(row_kernel_cfg(ds->device, &kc));
   const int per_sym = kc.per_sym;
-  P->per_num = P->heavy_sums == 0 ? kc.per_num_l2 : (P->wide ? kc.per_num_wide : kc.per_num);
+  P->per_num = P->heavy_sums == 2 ? kc.per_num_l2 : (P->wide ? kc.per_num_wide : kc.per_num);
   // products per microsecond of the whole GPU, R-MAT-like rows: sizes the CTA waves of time-sliced launches
   constexpr double kSymRate = 5e5, kNumRate = 9e4;
   P->waves_sym = P->waves(kSymRate);
@@ -1513,7 +1545,7 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
   pa.Cv = C->vals;
   SPWS_CUDA(cudaEventRecord(P->ev[4], s));
   const int g_num = ds->sm_count * std::max(P->per_num, 1);
-  if (P->heavy_sums == 0)
+  if (P->heavy_sums == 2)
     k_numeric_l2<<<g_num * P->waves_num, kThreads, kNumL2Smem, s>>>(P->sliced(g_num, P->waves_num));
   else if (P->wide)
     k_numeric<kAccWide><<<g_num * P->waves_num, kThreads, kNumSmemWide, s>>>(P->sliced(g_num, P->waves_num));
@@ -1536,7 +1568,7 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
     cudaEventElapsedTime(&stats->ms_scan, P->ev[2], P->ev[3]);
     cudaEventElapsedTime(&stats->ms_numeric, P->ev[4], P->ev[5]);
     stats->ms_total = stats->ms_setup + stats->ms_symbolic + stats->ms_scan + stats->ms_numeric;
-    stats->chunk_width = P->heavy_sums == 0 ? 0 : (P->wide ? kAccWide : kAcc);
+    stats->chunk_width = P->heavy_sums == 2 ? 0 : (P->wide ? kAccWide : kAcc);
     stats->n_chunks = (C->ncols + kSpanBits - 1) / kSpanBits;
   }
   if (err) {
@@ -1556,7 +1588,7 @@ int rowwise_plan_launch_numeric(RowwisePlan* plan, cudaStream_t s) {
   const int g_num = ds->sm_count * std::max(P->per_num, 1);
   PassArgs pa = P->pa;
   pa.counter = &P->sm->counter[1];
-  if (P->heavy_sums == 0)
+  if (P->heavy_sums == 2)
     k_numeric_l2<<<g_num, kThreads, kNumL2Smem, s>>>(pa);
   else if (P->wide)
     k_numeric<kAccWide><<<g_num, kThreads, kNumSmemWide, s>>>(pa);
@@ -1722,9 +1754,10 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.rowcnt = rowcnt;
   pa.err = &hd->err;
   pa.long_min = kLongMin;
+  pa.l2_rank_max = kL2RankMax;
   RowKernelCfg kc;
   SPWS_TRY(row_kernel_cfg(dev, &kc));
-  const int per_sym = kc.per_sym, per_num = kc.per_num_l2;
+  const int per_sym = kc.per_sym, per_num = kc.per_num;
   k_symbolic<<<sms * std::max(per_sym, 1), kThreads, kSymSmem, s>>>(pa);
   count_launch(1);
   SPWS_CUDA(cudaGetLastError());
@@ -1753,7 +1786,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.Cp = C_pos;
   pa.Ck = C_crd;
   pa.Cv = C_vals;
-  k_numeric_l2<<<sms * std::max(per_num, 1), kThreads, kNumL2Smem, s>>>(pa);
+  k_numeric<kAcc><<<sms * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
   count_launch(1);
   SPWS_CUDA(cudaGetLastError());
   SPWS_TRY(launch_light<true>(pa, hd->tier, &hd->counter[5], kc, sms, 1, 0, s));

@@ -11,9 +11,8 @@ from sparsews_gb300 import gen
 
 pytestmark = pytest.mark.gpu
 
-# (light_max, long_min, wide_windows, heavy_sums): sums in C.vals, then the two shared-window widths
-CANDIDATES = [(lm, ln, 0, 0) for lm in (512, 256) for ln in (128, 64, 256)] + \
-    [(lm, ln, w, 1) for w in (0, 1) for lm in (512, 256) for ln in (128, 64, 256)]
+# (light_max, long_min, wide_windows, heavy_sums) of the autotuner
+CANDIDATES = [(lm, ln, w, h) for h in (0, 1) for w in (0, 1) for lm in (512, 256) for ln in (128, 64, 256)]
 
 
 def hub_matrix(n=40000, seed=7):
@@ -37,11 +36,11 @@ def test_every_candidate_tuning_matches_oracle(spws_lib):
     ref = oracle.spgemm("taco", A, A)
     scale = oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2]
     assert np.diff(ref[0]).max() > 18432  # the hub rows need several windows of either size
-    for lm, ln, w, h in CANDIDATES:
+    for lm, ln, w, h in CANDIDATES + [(512, 128, 0, 2)]:
         C, st = sp.spgemm_device(d, d, tuning=sp.Tuning(lm, ln, w, h))
         got = C.download()
         C.release()
-        assert st.chunk_width == (0 if h == 0 else (18432 if w else 5120))
+        assert st.chunk_width == (0 if h == 2 else (18432 if w else 5120))
         assert_csr_equal_structure(got, ref, f"tuning {lm},{ln},{w},{h}")
         assert_csr_close(got, ref, scale, f"tuning {lm},{ln},{w},{h}")
 
@@ -66,7 +65,7 @@ def test_autotune_returns_a_candidate(spws_lib):
 def test_invalid_tuning_rejected(spws_lib):
     import sparsews_gb300 as sp
     d = sp.DeviceCsr.upload(*gen.poisson_rows(100, 4.0, seed=1))
-    for bad in (sp.Tuning(300, 0, 0, 0), sp.Tuning(1024, 0, 0, 0), sp.Tuning(0, 512, 0, 0), sp.Tuning(0, 0, 0, 2)):
+    for bad in (sp.Tuning(300, 0, 0, 0), sp.Tuning(1024, 0, 0, 0), sp.Tuning(0, 512, 0, 0), sp.Tuning(0, 0, 0, 3)):
         with pytest.raises(sp.SpwsError):
             sp.spgemm_device(d, d, tuning=bad)
 
