@@ -159,12 +159,13 @@ int spws_batch_release(spws_batch* batch);
  *  wide_windows: 1 = shared-memory windows of 18432 output ranks with one
  *                CTA per SM; 0 = windows of 5120 ranks with two CTAs per SM.
  *  heavy_sums:   how the 512-thread kernel sums a heavy row: 0 (default) =
- *                rows of at most 16384 output entries by FP64 reductions
- *                straight into C.vals, which the L2 executes (one pass, no
- *                windows), larger rows in shared-memory windows of output
- *                ranks; 1 = windows for every row; 2 = every row by
- *                reductions into C.vals (three CTAs per SM; wide_windows
- *                unused). */
+ *                FP64 reductions straight into C.vals, which the L2
+ *                executes: rows of up to 16384 output entries in one pass,
+ *                larger ones in windows of 16384 ranks (so the CTAs' live
+ *                output ranges stay in L2), three CTAs per SM, wide_windows
+ *                unused; 1 = shared-memory windows of output ranks, written
+ *                out window by window; 2 = shared-memory windows, with rows
+ *                of up to 16384 output entries summed in C.vals in one pass. */
 typedef struct spws_tuning {
   int32_t light_max;
   int32_t long_min;

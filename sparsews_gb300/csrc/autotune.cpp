@@ -52,7 +52,7 @@ int to_opts(const spws_tuning* t, SpgemmOpts* o) {
   }
   o->wide_windows = t->wide_windows != 0;
   if (t->heavy_sums < 0 || t->heavy_sums > 2) {
-    set_error("tuning.heavy_sums must be 0 (small rows in C.vals), 1 (windows) or 2 (all in C.vals)");
+    set_error("tuning.heavy_sums must be 0 (sums in C.vals), 1 (shared windows) or 2 (shared windows, small rows in C.vals)");
     return SPWS_ERR_INVALID;
   }
   o->heavy_sums = t->heavy_sums;
@@ -61,10 +61,11 @@ int to_opts(const spws_tuning* t, SpgemmOpts* o) {
 
 std::vector<spws_tuning> candidates() {
   std::vector<spws_tuning> c;
-  for (int heavy : {0, 1})
-    for (int wide : {0, 1})
-      for (int lm : {512, 256})
-        for (int ln : {128, 64, 256}) c.push_back(spws_tuning{lm, ln, wide, heavy});
+  for (int lm : {512, 256})
+    for (int ln : {128, 64, 256}) c.push_back(spws_tuning{lm, ln, 0, 0});  // sums in C.vals
+  for (int wide : {0, 1})
+    for (int lm : {512, 256})
+      for (int ln : {128, 64, 256}) c.push_back(spws_tuning{lm, ln, wide, 1});  // shared windows
   return c;
 }
 

@@ -526,12 +526,19 @@ __global__ void __launch_bounds__(kThreads, 3) k_symbolic(PassArgs a) {
   }
 }
 
-// Numeric pass (see the file comment), with windows of ACC ranks.
-template <int ACC>
-__global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassArgs a) {
+// Numeric pass (see the file comment). L2W = false: windows of ACC ranks
+// summed in shared memory (spans of at most a.l2_rank_max ranks go to C.vals
+// in one pass). L2W = true: every sum goes straight into C.vals by FP64
+// reductions, which the L2 executes; spans of more than kL2RankMax ranks in
+// windows of kL2RankMax ranks, so a CTA's live output range (128 KB) and all
+// CTAs' together stay in L2. With no shared accumulator, three CTAs fit on an
+// SM. The reductions outpace shared-memory FP64 atomics on GB300.
+template <int ACC, bool L2W>
+__global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_numeric(PassArgs a) {
+  constexpr int WIN = L2W ? kL2RankMax : ACC;  // ranks per window
   extern __shared__ __align__(16) unsigned char smem[];
-  double* acc = reinterpret_cast<double*>(smem);                             // ACC
-  uint32_t* bm = reinterpret_cast<uint32_t*>(smem + sizeof(double) * ACC);   // kSpanWords
+  double* acc = reinterpret_cast<double*>(smem);                                         // ACC (shared sums)
+  uint32_t* bm = reinterpret_cast<uint32_t*>(smem + (L2W ? 0 : sizeof(double) * ACC));  // kSpanWords
   uint16_t* wpre = reinterpret_cast<uint16_t*>(bm + kSpanWords);             // kSpanWords
   Batch& b = *reinterpret_cast<Batch*>(reinterpret_cast<unsigned char*>(wpre + kSpanWords));
   int32_t* bnd = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(&b) + sizeof(Batch));  // kBoundInts
@@ -540,7 +547,8 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
   __shared__ int s_idx;
   __shared__ int32_t s_cols[2];
   __shared__ int32_t s_wcol[kMaxWin + 1];
-  for (int q = threadIdx.x; q < ACC; q += kThreads) acc[q] = 0.0;
+  if (!L2W)
+    for (int q = threadIdx.x; q < ACC; q += kThreads) acc[q] = 0.0;
   const int nwork = *a.nheavy;
   const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   // Rows are claimed one ahead: while row i is being summed, the stored
@@ -658,7 +666,7 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
         while (need-- > 0) word &= word - 1;
         return wlo + lo * 32 + (__ffs(word) - 1);
       };
-      if (nnz_w <= a.l2_rank_max) {
+      if (nnz_w <= (L2W ? WIN : a.l2_rank_max)) {
         // One pass with the sums in C.vals (in L2): the span's output range
         // is small enough that every CTA's range stays in L2 together
         // (l2_rank_max ranks of 8 bytes per CTA), and the L2's FP64
@@ -683,7 +691,7 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
         out += nnz_w;
         continue;
       }
-      const int nwin = (nnz_w + ACC - 1) / ACC;
+      const int nwin = (nnz_w + WIN - 1) / WIN;
       const int nj = q1 - q0;
       const int32_t span_hi = multi ? span_end(wlo) : INT_MAX;
       // Several windows and one batch of j's: find every (j, window) slice
@@ -692,7 +700,7 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
       const bool prebound = nwin > 1 && nwin <= kMaxWin && nj <= kThreads && nj * (nwin + 1) <= kBoundInts;
       if (prebound) {
         for (int w = threadIdx.x; w <= nwin; w += kThreads)
-          s_wcol[w] = w == 0 ? wlo : (w == nwin ? span_hi : col_of_rank(w * ACC));
+          s_wcol[w] = w == 0 ? wlo : (w == nwin ? span_hi : col_of_rank(w * WIN));
         __syncthreads();
         for (int it = threadIdx.x; it < nj * (nwin + 1); it += kThreads) {
           const int t = it / (nwin + 1), w = it - t * (nwin + 1);
@@ -725,9 +733,12 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
         for (int t = threadIdx.x; t < nj; t += kThreads) bnd[t] = __ldg(a.Bp + __ldg(a.Aj + q0 + t));
         __syncthreads();
       }
-      // values, one window of ACC ranks at a time
-      for (int r0 = 0, win = 0; r0 < nnz_w; r0 += ACC, win++) {
-        const int r1 = min(nnz_w, r0 + ACC);
+      // values, one window of WIN ranks at a time
+      for (int r0 = 0, win = 0; r0 < nnz_w; r0 += WIN, win++) {
+        const int r1 = min(nnz_w, r0 + WIN);
+        if (L2W) {  // the window's sums start at zero in C.vals (ordered before the reductions by a barrier below)
+          for (int r = r0 + threadIdx.x; r < r1; r += kThreads) a.Cv[out + r] = 0.0;
+        }
         const bool whole = r0 == 0 && r1 == nnz_w;
         int32_t clo = wlo, chi = span_hi;
         if (!whole && !prebound) {  // columns of ranks r0 and r1 bound the window
@@ -775,23 +786,29 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
           } else {
             bw = load_batch(a, qb, q1, true, clip, clo, chi, b, wsum);
           }
-          // The window offset rank - r0 lies in [0, ACC), below 2^16, so it
+          // The window offset rank - r0 lies in [0, WIN), below 2^16, so it
           // follows from the 16-bit word prefixes alone, modulo 2^16 (no
           // group base needed).
           const uint16_t r0_16 = (uint16_t)r0;
+          double* cw = a.Cv + out + r0;
           for_batch_entries<true>(b, bw, a.Bk, a.Bv, [&](int32_t col, double bv, double av) {
             const int k = col - wlo;
             const int w = k >> 5;
             const uint16_t off = (uint16_t)(wpre[w] + __popc(bm[w] & ((1u << (k & 31)) - 1u)) - r0_16);
-            atomicAdd(&acc[off], __dmul_rn(av, bv));
+            if (L2W)
+              atomicAdd(cw + off, __dmul_rn(av, bv));
+            else
+              atomicAdd(&acc[off], __dmul_rn(av, bv));
           });
           __syncthreads();
         }
-        for (int r = r0 + threadIdx.x; r < r1; r += kThreads) {
-          a.Cv[out + r] = acc[r - r0];
-          acc[r - r0] = 0.0;
+        if (!L2W) {
+          for (int r = r0 + threadIdx.x; r < r1; r += kThreads) {
+            a.Cv[out + r] = acc[r - r0];
+            acc[r - r0] = 0.0;
+          }
+          __syncthreads();
         }
-        __syncthreads();
       }
       out += nnz_w;
     }
@@ -799,138 +816,6 @@ __global__ void __launch_bounds__(kThreads, ACC <= kAcc ? 2 : 1) k_numeric(PassA
   }
 }
 
-
-// Numeric pass with the row's sums kept in C.vals itself (in L2) instead of
-// shared-memory rank windows: the row's output range is zeroed, then every
-// product is added to C.vals[row start + rank] with a fire-and-forget FP64
-// reduction (red.global.add.f64), which the L2 slices execute. On GB300 the L2
-// reductions sustain more products per second than shared-memory FP64 atomics
-// (measured with a row-like access pattern: 271 vs 195 G/s), and with no
-// window there is no window loop: each B-row slice is read once per row (no
-// clipping searches per window, no per-window batch set-up, no write-back),
-// and without the 40 KB accumulator three CTAs fit on an SM. The row's output
-// range stays in L2 while it is summed, so it still reaches DRAM once.
-__global__ void __launch_bounds__(kThreads, 3) k_numeric_l2(PassArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint32_t* bm = reinterpret_cast<uint32_t*>(smem);               // kSpanWords
-  uint16_t* wpre = reinterpret_cast<uint16_t*>(bm + kSpanWords);  // kSpanWords
-  Batch& b = *reinterpret_cast<Batch*>(reinterpret_cast<unsigned char*>(wpre + kSpanWords));
-  __shared__ uint32_t gbase[kGroups];
-  __shared__ int wsum[kWarps];
-  __shared__ int s_idx;
-  const int nwork = *a.nheavy;
-  const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
-  int next = claim(a.counter, &s_idx, a, t0);
-  for (;;) {
-    const int idx = next;
-    if (idx >= nwork) break;
-    const int32_t i = a.order[idx];
-    const RowInfo ri = a.info[i];
-    const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
-    const bool multi = (long long)ri.hi - ri.lo + 1 > kSpanBits;
-    const int32_t row_end = a.Cp[i + 1];
-    const int32_t shift = a.col_shift ? a.col_shift[i] : 0;
-    int32_t out = a.Cp[i];
-    next = claim(a.counter, &s_idx, a, t0);
-    for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
-      const int32_t wlo = (int32_t)wl;
-      const int nw = words_in(wl, ri.hi);
-      const int nq = (nw + 3) >> 2;
-      uint4* bm4 = reinterpret_cast<uint4*>(bm);
-      if (a.bmstore && !multi) {  // the symbolic pass left this row's bitmap
-        const uint4* src = reinterpret_cast<const uint4*>(a.bmstore + a.bmoff[i]);
-#pragma unroll 4
-        for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = src[w];
-        __syncthreads();
-        if (next < nwork) {  // prefetch the next row's stored bitmap into L2
-          const int32_t ni = a.order[next];
-          const RowInfo nr = a.info[ni];
-          if ((long long)nr.hi - nr.lo + 1 <= kSpanBits) {
-            const uint32_t* nsrc = a.bmstore + a.bmoff[ni];
-            const int nwn = words_in(nr.lo, nr.hi);
-            for (int w = threadIdx.x * 32; w < nwn; w += kThreads * 32)
-              asm volatile("prefetch.global.L2 [%0];" ::"l"(nsrc + w));
-          }
-        }
-      } else {
-        for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = make_uint4(0u, 0u, 0u, 0u);
-        __syncthreads();
-        build_bitmap(a, q0, q1, wlo, multi, bm, b, wsum);
-      }
-
-      // Word prefixes and the row's columns in order (as in k_numeric).
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      const int chunk = (nq + kWarps - 1) / kWarps;
-      const int c0 = min(nq, warp * chunk), c1 = min(nq, c0 + chunk);
-      int wc = 0;
-      for (int g = c0 + lane; g < c1; g += 32) {
-        const uint4 v = bm4[g];
-        wc += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, o);
-      int nnz_w;
-      int run = block_excl_scan(lane == 0 ? wc : 0, wsum, &nnz_w);
-      run = __shfl_sync(0xffffffffu, run, 0);
-      if (out + nnz_w > row_end) {  // never write past the row the symbolic pass sized (uniform)
-        if (threadIdx.x == 0) atomicExch(a.err, 1);
-        break;
-      }
-      for (int gb = c0; gb < c1; gb += 32) {
-        const int g = gb + lane;
-        const uint4 v = g < c1 ? bm4[g] : make_uint4(0u, 0u, 0u, 0u);
-        const uint32_t words[4] = {v.x, v.y, v.z, v.w};
-        const int tot = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
-        int incl = tot;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        int r = run + incl - tot;
-        if (g < c1) {
-          if (((4 * g) & (kGroupWords - 1)) == 0) gbase[(4 * g) / kGroupWords] = (uint32_t)r;
-          const int p1 = r + __popc(v.x), p2 = p1 + __popc(v.y), p3 = p2 + __popc(v.z);
-          *reinterpret_cast<uint2*>(wpre + 4 * g) =
-              make_uint2((uint32_t)(uint16_t)r | ((uint32_t)(uint16_t)p1 << 16),
-                         (uint32_t)(uint16_t)p2 | ((uint32_t)(uint16_t)p3 << 16));
-        }
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-          uint32_t word = words[k];
-          const int32_t col0 = wlo + (4 * g + k) * 32 - shift;
-          while (word) {
-            const int bit = __ffs(word) - 1;
-            word &= word - 1;
-            a.Ck[out + r] = col0 + bit;
-            r++;
-          }
-        }
-        run += __shfl_sync(0xffffffffu, incl, 31);
-      }
-      // the row's sums start at zero (these stores precede every reduction
-      // below: the barrier orders them for the whole CTA)
-      double* cv = a.Cv + out;
-      for (int r = threadIdx.x; r < nnz_w; r += kThreads) cv[r] = 0.0;
-      __syncthreads();
-      const int32_t span_hi = multi ? span_end(wlo) : INT_MAX;
-      for (int32_t qb = q0; qb < q1; qb += kThreads) {
-        const BatchWork bw = load_batch(a, qb, q1, true, multi, wlo, span_hi, b, wsum);
-        for_batch_entries<true>(b, bw, a.Bk, a.Bv, [&](int32_t col, double bv, double av) {
-          const int k = col - wlo;
-          const int w = k >> 5;
-          const uint32_t base = gbase[w / kGroupWords];
-          const uint32_t rank =
-              base + (uint16_t)(wpre[w] - (uint16_t)base) + (uint32_t)__popc(bm[w] & ((1u << (k & 31)) - 1u));
-          atomicAdd(cv + rank, __dmul_rn(av, bv));
-        });
-        __syncthreads();
-      }
-      out += nnz_w;
-    }
-    if (threadIdx.x == 0 && out != row_end) atomicExch(a.err, 1);
-  }
-}
 
 // Light rows (fewer than 512 products): one warp per row, no CTA barriers.
 // The row's products are staged in shared memory as (column << 32 | flat
@@ -1213,7 +1098,8 @@ constexpr size_t num_smem(int acc) {
          sizeof(int32_t) * kBoundInts;
 }
 constexpr size_t kNumSmemWide = num_smem(kAccWide);
-constexpr size_t kNumL2Smem = sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords + sizeof(Batch);
+constexpr size_t kNumL2Smem = sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords + sizeof(Batch) +
+                               sizeof(int32_t) * kBoundInts;  // k_numeric<kAcc, true>: no shared accumulator
 constexpr size_t kNumSmem = sizeof(double) * kAcc + sizeof(uint32_t) * kSpanWords + sizeof(uint16_t) * kSpanWords +
                             sizeof(Batch) + sizeof(int32_t) * kBoundInts;
 
@@ -1300,17 +1186,18 @@ int row_kernel_cfg(int device, RowKernelCfg* out) {
   RowKernelCfg& c = cfg[device];
   if (!c.init) {
     SPWS_CUDA(cudaFuncSetAttribute(k_symbolic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem));
-    SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAcc>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
-    SPWS_CUDA(cudaFuncSetAttribute(k_numeric_l2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumL2Smem));
-    SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAccWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAcc, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumSmem));
+    SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAcc, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNumL2Smem));
+    SPWS_CUDA(cudaFuncSetAttribute(k_numeric<kAccWide, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kNumSmemWide));
     SPWS_TRY(light_cfg<false>(&c));
     SPWS_TRY(light_cfg<true>(&c));
     SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sym, k_symbolic, kThreads, kSymSmem));
-    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num, k_numeric<kAcc>, kThreads, kNumSmem));
-    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num_l2, k_numeric_l2, kThreads, kNumL2Smem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num, k_numeric<kAcc, false>, kThreads, kNumSmem));
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num_l2, k_numeric<kAcc, true>, kThreads,
+                                                            kNumL2Smem));
     c.per_num_l2 = std::max(c.per_num_l2, 1);
-    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num_wide, k_numeric<kAccWide>, kThreads,
+    SPWS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_num_wide, k_numeric<kAccWide, false>, kThreads,
                                                             kNumSmemWide));
     c.per_sym = std::max(c.per_sym, 1);
     c.per_num = std::max(c.per_num, 1);
@@ -1319,6 +1206,16 @@ int row_kernel_cfg(int device, RowKernelCfg* out) {
   }
   *out = c;
   return SPWS_OK;
+}
+
+// The numeric pass's heavy-row kernel for a heavy_sums choice (see SpgemmOpts).
+void launch_numeric(int heavy_sums, bool wide, int grid, const PassArgs& pa, cudaStream_t s) {
+  if (heavy_sums == 0)
+    k_numeric<kAcc, true><<<grid, kThreads, kNumL2Smem, s>>>(pa);
+  else if (wide)
+    k_numeric<kAccWide, false><<<grid, kThreads, kNumSmemWide, s>>>(pa);
+  else
+    k_numeric<kAcc, false><<<grid, kThreads, kNumSmem, s>>>(pa);
 }
 
 struct RowwisePlanImpl {
@@ -1357,7 +1254,7 @@ struct RowwisePlanImpl {
   int waves_sym = 1, waves_num = 1;
   int light_bucket = kLightBucket;
   bool wide = false;
-  int heavy_sums = 0;  // 0: k_numeric, small spans in C.vals; 1: k_numeric, windows only; 2: k_numeric_l2
+  int heavy_sums = 0;  // 0: sums in C.vals (L2 windows); 1: shared windows; 2: shared windows, small spans in C.vals
 
   // CTA waves for a pass that runs `rate` products per microsecond, so that
   // each wave lasts about one time slice (1 = persistent launch).
@@ -1486,11 +1383,11 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   pa.err = &sm->err;
   pa.long_min = opt.long_min;
   pa.col_shift = opt.col_shift;
-  pa.l2_rank_max = opt.heavy_sums == 0 ? kL2RankMax : 0;
+  pa.l2_rank_max = opt.heavy_sums == 2 ? kL2RankMax : 0;
   RowKernelCfg& kc = P->kc;
   SPWS_TRY(row_kernel_cfg(ds->device, &kc));
   const int per_sym = kc.per_sym;
-  P->per_num = P->heavy_sums == 2 ? kc.per_num_l2 : (P->wide ? kc.per_num_wide : kc.per_num);
+  P->per_num = P->heavy_sums == 0 ? kc.per_num_l2 : (P->wide ? kc.per_num_wide : kc.per_num);
   // products per microsecond of the whole GPU, R-MAT-like rows: sizes the CTA waves of time-sliced launches
   constexpr double kSymRate = 5e5, kNumRate = 9e4;
   P->waves_sym = P->waves(kSymRate);
@@ -1545,12 +1442,7 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
   pa.Cv = C->vals;
   SPWS_CUDA(cudaEventRecord(P->ev[4], s));
   const int g_num = ds->sm_count * std::max(P->per_num, 1);
-  if (P->heavy_sums == 2)
-    k_numeric_l2<<<g_num * P->waves_num, kThreads, kNumL2Smem, s>>>(P->sliced(g_num, P->waves_num));
-  else if (P->wide)
-    k_numeric<kAccWide><<<g_num * P->waves_num, kThreads, kNumSmemWide, s>>>(P->sliced(g_num, P->waves_num));
-  else
-    k_numeric<kAcc><<<g_num * P->waves_num, kThreads, kNumSmem, s>>>(P->sliced(g_num, P->waves_num));
+  launch_numeric(P->heavy_sums, P->wide, g_num * P->waves_num, P->sliced(g_num, P->waves_num), s);
   count_launch(1);
   SPWS_CUDA(cudaGetLastError());
   SPWS_TRY(launch_light<true>(pa, P->sm->tier, &P->sm->counter[5], P->kc, ds->sm_count, P->waves_num, P->yield_ns,
@@ -1568,7 +1460,7 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
     cudaEventElapsedTime(&stats->ms_scan, P->ev[2], P->ev[3]);
     cudaEventElapsedTime(&stats->ms_numeric, P->ev[4], P->ev[5]);
     stats->ms_total = stats->ms_setup + stats->ms_symbolic + stats->ms_scan + stats->ms_numeric;
-    stats->chunk_width = P->heavy_sums == 2 ? 0 : (P->wide ? kAccWide : kAcc);
+    stats->chunk_width = P->heavy_sums == 0 ? kL2RankMax : (P->wide ? kAccWide : kAcc);
     stats->n_chunks = (C->ncols + kSpanBits - 1) / kSpanBits;
   }
   if (err) {
@@ -1588,12 +1480,7 @@ int rowwise_plan_launch_numeric(RowwisePlan* plan, cudaStream_t s) {
   const int g_num = ds->sm_count * std::max(P->per_num, 1);
   PassArgs pa = P->pa;
   pa.counter = &P->sm->counter[1];
-  if (P->heavy_sums == 2)
-    k_numeric_l2<<<g_num, kThreads, kNumL2Smem, s>>>(pa);
-  else if (P->wide)
-    k_numeric<kAccWide><<<g_num, kThreads, kNumSmemWide, s>>>(pa);
-  else
-    k_numeric<kAcc><<<g_num, kThreads, kNumSmem, s>>>(pa);
+  launch_numeric(P->heavy_sums, P->wide, g_num, pa, s);
   SPWS_CUDA(cudaGetLastError());
   return launch_light<true>(pa, P->sm->tier, &P->sm->counter[5], P->kc, ds->sm_count, 1, 0, s);
 }
@@ -1754,10 +1641,10 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.rowcnt = rowcnt;
   pa.err = &hd->err;
   pa.long_min = kLongMin;
-  pa.l2_rank_max = kL2RankMax;
+  pa.l2_rank_max = 0;
   RowKernelCfg kc;
   SPWS_TRY(row_kernel_cfg(dev, &kc));
-  const int per_sym = kc.per_sym, per_num = kc.per_num;
+  const int per_sym = kc.per_sym, per_num = kc.per_num_l2;
   k_symbolic<<<sms * std::max(per_sym, 1), kThreads, kSymSmem, s>>>(pa);
   count_launch(1);
   SPWS_CUDA(cudaGetLastError());
@@ -1786,7 +1673,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   pa.Cp = C_pos;
   pa.Ck = C_crd;
   pa.Cv = C_vals;
-  k_numeric<kAcc><<<sms * std::max(per_num, 1), kThreads, kNumSmem, s>>>(pa);
+  launch_numeric(0, false, sms * std::max(per_num, 1), pa, s);
   count_launch(1);
   SPWS_CUDA(cudaGetLastError());
   SPWS_TRY(launch_light<true>(pa, hd->tier, &hd->counter[5], kc, sms, 1, 0, s));

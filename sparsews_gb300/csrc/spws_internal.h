@@ -76,10 +76,10 @@ struct SpgemmOpts {
   int light_max = 512;        // rows with fewer products go to the warp-per-row kernel (power of two <= 512)
   int long_min = 128;         // B-row slices this long are cut into pieces, shorter ones packed (<= 256)
   bool wide_windows = false;  // numeric windows of 18432 ranks at 1 CTA/SM instead of 5120 at 2 CTAs/SM
-  // Heavy rows' sums: 0 = rows with small outputs by FP64 reductions straight
-  // into C.vals (in L2), the others in shared-memory rank windows; 1 = windows
-  // for every heavy row (wide_windows picks their width); 2 = every heavy row
-  // in C.vals (k_numeric_l2, three CTAs per SM).
+  // Heavy rows' sums: 0 = FP64 reductions straight into C.vals (in L2), in
+  // windows of 16384 output ranks for larger rows, three CTAs per SM; 1 =
+  // shared-memory rank windows (wide_windows picks their width); 2 = shared
+  // windows, with rows of at most 16384 outputs in C.vals in one pass.
   int heavy_sums = 0;
   // Per A row, an amount subtracted from every column written for that row
   // (the batched form writes each instance's own columns); nullptr: none.

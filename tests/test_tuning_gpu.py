@@ -12,7 +12,8 @@ from sparsews_gb300 import gen
 pytestmark = pytest.mark.gpu
 
 # (light_max, long_min, wide_windows, heavy_sums) of the autotuner
-CANDIDATES = [(lm, ln, w, h) for h in (0, 1) for w in (0, 1) for lm in (512, 256) for ln in (128, 64, 256)]
+CANDIDATES = [(lm, ln, 0, 0) for lm in (512, 256) for ln in (128, 64, 256)] + \
+    [(lm, ln, w, 1) for w in (0, 1) for lm in (512, 256) for ln in (128, 64, 256)]
 
 
 def hub_matrix(n=40000, seed=7):
@@ -40,7 +41,7 @@ def test_every_candidate_tuning_matches_oracle(spws_lib):
         C, st = sp.spgemm_device(d, d, tuning=sp.Tuning(lm, ln, w, h))
         got = C.download()
         C.release()
-        assert st.chunk_width == (0 if h == 2 else (18432 if w else 5120))
+        assert st.chunk_width == (16384 if h == 0 else (18432 if w else 5120))
         assert_csr_equal_structure(got, ref, f"tuning {lm},{ln},{w},{h}")
         assert_csr_close(got, ref, scale, f"tuning {lm},{ln},{w},{h}")
 
