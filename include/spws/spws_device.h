@@ -52,7 +52,7 @@ typedef struct spws_spgemm_stats {
 /* Statistics of a batched SpGEMM. */
 typedef struct spws_batch_stats {
   int32_t instances;  /* products in the batch */
-  int32_t groups;     /* row-wise pipeline runs (each group's output fits int32 positions) */
+  int32_t groups;     /* row-wise pipeline runs over the batch (1: every instance's rows in one) */
   int64_t products;   /* scalar products over the batch */
   int64_t nnz;        /* output nonzeros over the batch */
   float ms_kernels;   /* device time of the row-wise pipelines */
@@ -93,7 +93,7 @@ int spws_spgemm_csr_device(const spws_csr_dev* A, const spws_csr_dev* B, spws_cs
  * allowed. It has no counterpart in the reference, whose kernels run on the
  * CPU and allocate with malloc.
  *
- * Limit: its scratch is one fixed device array of about 6 MiB, sized for A
+ * Limit: its scratch is one fixed device array of about 8 MiB, sized for A
  * with at most 262144 rows; a larger A is rejected with SPWS_ERR_CAPACITY.
  * Every GPU that loads the library holds that array until the process exits.
  * The first call on a device looks up the array's device address with that
@@ -138,12 +138,14 @@ int spws_spgemm_t_device(const spws_csr_dev* At, const spws_csr_dev* B, int32_t 
 int spws_set_device(int device);
 
 /* Batched SpGEMM: C[i] = A[i] * B[i] for `count` independent products of
- * uneven sizes, run as one row-wise pipeline over block-diagonal operands
- * (every instance's rows share the same cost-ordered work queue), split into
- * as few groups as int32 output positions allow. C[i] are views into memory
- * owned by *batch: read them with spws_csr_download, never pass them to
- * spws_csr_release, and free them all with spws_batch_release. No counterpart
- * in the reference (its kernels take one product per call). */
+ * uneven sizes, run as one row-wise pipeline over block-diagonal operands:
+ * every instance's rows share one cost-ordered work queue, one persistent
+ * launch per pass covers them all, and 64-bit positions place the outputs in
+ * one pool (the batch's total may exceed 2^31 entries; each instance's may
+ * not). C[i] are views into memory owned by *batch: read them with
+ * spws_csr_download, never pass them to spws_csr_release, and free them all
+ * with spws_batch_release. No counterpart in the reference (its kernels take
+ * one product per call). */
 int spws_spgemm_batched(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
                         spws_batch** batch, spws_batch_stats* stats);
 int spws_batch_release(spws_batch* batch);
@@ -191,12 +193,17 @@ int spws_spgemm_batched_tuned(int32_t count, const spws_csr_dev* A, const spws_c
                               spws_batch** batch, const spws_tuning* tuning, spws_batch_stats* stats);
 
 /* A batch kept for re-solving: spws_batch_plan_create runs the batched
- * product like spws_spgemm_batched and keeps every group's symbolic result
- * (output structure, row order, column bitmaps) and a CUDA graph of the
- * numeric work. spws_batch_plan_execute replays that graph with one launch:
- * it reads the instances' current values (same A_i / B_i arrays, structure
- * unchanged) and rewrites the values of the C views in place. The views
- * belong to the plan until spws_batch_plan_release. */
+ * product like spws_spgemm_batched, keeps its buffers, and captures the whole
+ * solve in one CUDA graph: assembling the block-diagonal operands from the
+ * instances' arrays, row analysis and ordering, the symbolic pass, the
+ * position scan, the numeric pass and the split into per-instance positions.
+ * spws_batch_plan_execute replays it with one graph launch from the
+ * instances' current arrays (the same A_i / B_i arrays) and rewrites the C
+ * views in place; the output structure must stay the one the plan was made
+ * with (new values are the intended use). The graph checks this on the
+ * device: if the output would no longer fit the views' places, nothing is
+ * written and the call returns SPWS_ERR_CAPACITY. The views belong to the
+ * plan until spws_batch_plan_release. */
 typedef struct spws_batch_plan spws_batch_plan;
 int spws_batch_plan_create(int32_t count, const spws_csr_dev* A, const spws_csr_dev* B, spws_csr_dev* C,
                            const spws_tuning* tuning, spws_batch_plan** plan, spws_batch_stats* stats);

@@ -419,9 +419,11 @@ def spgemm_batched(As, Bs, tuning=None):
 
 
 class BatchPlan:
-    """A batch kept for re-solving with new values (spws_batch_plan_*):
-    execute() replays the captured numeric graph and rewrites the views'
-    values from the instances' current values."""
+    """A batch kept for re-solving (spws_batch_plan_*): execute() replays the
+    captured graph of the whole solve (operand assembly, symbolic pass,
+    scan, numeric pass, per-instance split) from the instances' current
+    arrays and rewrites the views in place; the output structure must stay
+    the one the plan was made with (new values), else SPWS_ERR_CAPACITY."""
 
     def __init__(self, As, Bs, tuning=None):
         L = lib()

@@ -4,13 +4,15 @@
 // The instances are laid side by side as block-diagonal super-operands
 // A* = diag(A_1..A_m) and B* = diag(B_1..B_m) (columns of A_i and B_i shifted
 // by the widths of the instances before them), so A* x B* = diag(C_1..C_m).
-// One row-wise pipeline over A* then orders every instance's rows together by
-// cost (heavy rows to CTAs, light rows to warps) and runs them in the same
-// launches. Instances are grouped so that a group's output positions fit
-// int32, the position type of taco_tensor_t; a group is a row range of A*.
-// The product of a group is split back into per-instance CSR views whose
-// positions start at 0; the kernels write each row's columns shifted back by
-// its instance's column offset, so the columns are the instance's own.
+// One row-wise pipeline over A* orders every instance's rows together by cost
+// and runs them in the same persistent launches: one symbolic launch and one
+// numeric launch for the heavy rows of every instance (a CTA claims rows from
+// the one cost-ordered queue) and one launch per light-row tier. A device
+// scan of the rows' output counts gives 64-bit positions into one output
+// pool, so the batch's total output may exceed 2^31 entries; each instance's
+// own int32 positions (starting at 0) and its offset into the pool follow
+// from them on the device. The kernels write each row's columns shifted back
+// by its instance's column offset, so the columns are the instance's own.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -71,26 +73,54 @@ __global__ void k_cat_ent(int count, const Inst* __restrict__ in, const long lon
   vals[e] = t.vals[k];
 }
 
-// Per-instance positions of a group's product: instance i owns rows
-// [ro_i, ro_i + n_i) of the group result; its own array starts at
-// out_off_i = ro_i + i (one extra end entry per instance).
-__global__ void k_split_pos(int count, const Inst* __restrict__ ia, const long long* __restrict__ row_offs,
-                            int first, int32_t group_row0, int32_t group_rows, const int32_t* __restrict__ gpos,
-                            int32_t* __restrict__ opos, long long* __restrict__ inst_nnz_off) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // row within the group, or an end entry
-  if (r >= group_rows) return;
-  const int i = find_inst(row_offs, count, group_row0 + r);
+// Per-instance positions from the batch's 64-bit positions gpos: instance i
+// owns super rows [row_off_i, row_off_i + n_i), and its own position array
+// starts at row_off_i + i (one extra end entry per instance). An instance's
+// offset into the output pool goes to inst_nnz_off[i]; with check set, it
+// must equal the offset the plan was made with (*bad = 1 otherwise: the
+// batch's structure changed under a replay), and an instance's output must
+// fit int32 positions (*bad = 2 otherwise).
+__global__ void k_split_pos64(int count, const Inst* __restrict__ ia, const long long* __restrict__ row_offs,
+                              int32_t total_rows, const long long* __restrict__ gpos, int32_t* __restrict__ opos,
+                              long long* __restrict__ inst_nnz_off, const long long* __restrict__ check,
+                              int* __restrict__ bad, const int* __restrict__ abort) {
+  if (abort && *abort) return;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= total_rows) return;
+  const int i = find_inst(row_offs, count, r);
   const Inst t = ia[i];
-  const int32_t lr = (int32_t)(group_row0 + r - t.row_off);  // row within the instance
-  const int32_t gr0 = t.row_off - group_row0;                // instance's first row within the group
-  const int32_t base = gpos[gr0];
-  const int64_t at = (int64_t)gr0 + (i - first);
-  opos[at + lr] = gpos[r] - base;
+  const int32_t lr = (int32_t)(r - t.row_off);
+  const long long base = gpos[t.row_off];
+  const int64_t at = (int64_t)t.row_off + i;
+  opos[at + lr] = (int32_t)(gpos[r] - base);
   if (lr == t.rows - 1) {
-    opos[at + t.rows] = gpos[gr0 + t.rows] - base;
+    const long long end = gpos[(int64_t)t.row_off + t.rows] - base;
+    if (end > INT32_MAX) atomicExch(bad, 2);
+    opos[at + t.rows] = (int32_t)end;
     inst_nnz_off[i] = base;
+    if (check && check[i] != base) atomicExch(bad, 1);
   }
-  if (lr == 0 && t.rows == 0) inst_nnz_off[i] = base;
+}
+
+// Instances with no rows: their single position entry and their offset.
+__global__ void k_split_empty(int count, const Inst* __restrict__ ia, const long long* __restrict__ gpos,
+                              int32_t* __restrict__ opos, long long* __restrict__ inst_nnz_off,
+                              const int* __restrict__ abort) {
+  if (abort && *abort) return;
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= count) return;
+  const Inst t = ia[i];
+  if (t.rows != 0) return;
+  opos[(int64_t)t.row_off + i] = 0;
+  inst_nnz_off[i] = gpos[t.row_off];
+}
+
+// One thread: *bad = 1 unless the batch's output total is still `want` (a
+// replay whose last instances changed size).
+__global__ void k_check_total(const long long* __restrict__ total, long long want, int* __restrict__ bad,
+                              const int* __restrict__ abort) {
+  if (abort && *abort) return;
+  if (*total != want) atomicExch(bad, 1);
 }
 
 // Column shift of every super-matrix row: the column offset of its
@@ -103,65 +133,21 @@ __global__ void k_row_shift(int count, const Inst* __restrict__ ib, const long l
   shift[r] = ib[find_inst(row_offs, count, r)].col_off;
 }
 
-// Products of each A row, summed per instance (an upper bound of the
-// instance's output nonzeros, used to cut the batch into int32-sized groups).
-// Thread per row; a warp's rows are consecutive, so each instance they touch
-// is a contiguous run of lanes: a segmented reduction within the warp leaves
-// the run's total on its first lane, and one atomic per run per warp goes to
-// the instance's counter (one atomic per row serialised on the few counters
-// of large instances: 6 ms for the 1024-instance batch).
-__global__ void k_inst_products(int count, const long long* __restrict__ row_offs, int32_t total_rows,
-                                const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
-                                const int32_t* __restrict__ Bp, unsigned long long* __restrict__ prods) {
-  const int lane = threadIdx.x & 31;
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = r < total_rows;
-  unsigned long long p = 0;
-  int inst = -1;
-  if (valid) {
-    for (int32_t q = Ap[r]; q < Ap[r + 1]; q++) {
-      const int32_t j = Aj[q];
-      p += (unsigned long long)(Bp[j + 1] - Bp[j]);
-    }
-    inst = find_inst(row_offs, count, r);
-  }
-  // lane l ends with the sum over lanes [l, 32) of its own run
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned long long op = __shfl_down_sync(0xffffffffu, p, o);
-    const int oi = __shfl_down_sync(0xffffffffu, inst, o);
-    if (lane + o < 32 && oi == inst) p += op;
-  }
-  const int prev = __shfl_up_sync(0xffffffffu, inst, 1);
-  if (valid && p && (lane == 0 || prev != inst)) atomicAdd(&prods[inst], p);
-}
-
-__global__ void k_zero_rows(int count, const Inst* __restrict__ ia, int first, int last,
-                            long long* __restrict__ inst_nnz_off, int32_t group_row0, const int32_t* __restrict__ gpos,
-                            int32_t* __restrict__ opos) {
-  // instances with no rows still need their single position entry and offset
-  const int i = first + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (i >= last) return;
-  const Inst t = ia[i];
-  if (t.rows != 0) return;
-  const int32_t gr0 = t.row_off - group_row0;
-  opos[(int64_t)gr0 + (i - first)] = 0;
-  inst_nnz_off[i] = gpos[gr0];
-}
-
 }  // namespace
 
 struct BatchReplay {
   cudaStream_t s = nullptr;
-  std::vector<void*> owned;  // assembled operands and instance tables
-  std::vector<RowwisePlan> plans;
+  std::vector<void*> owned;  // assembled operands, instance tables, plan-side arrays
+  RowwisePlan plan;
+  bool have_plan = false;
+  int* bad = nullptr;        // split check: structure changed / instance too large
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int kernels = 0;  // kernel nodes per replay
   ~BatchReplay() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    for (auto& p : plans) rowwise_plan_free(&p);
+    if (have_plan) rowwise_plan_free(&plan);
     for (void* p : owned) dfree(p, s);
     if (s) cudaStreamSynchronize(s);
   }
@@ -175,21 +161,28 @@ int batch_replay_execute(BatchReplay* r, float* ms) {
   SPWS_CUDA(cudaGraphLaunch(r->exec, r->s));
   SPWS_CUDA(cudaEventRecord(e1, r->s));
   count_launch(r->kernels);
-  std::vector<int> errs(r->plans.size(), 0);
-  for (size_t g = 0; g < r->plans.size(); g += 16) {  // readback batches of at most 16
+  int err = 0, abort = 0, bad = 0;
+  if (r->have_plan) {
     Readback rb(r->s);
-    for (size_t k = g; k < std::min(r->plans.size(), g + 16); k++)
-      if (const int* e = rowwise_plan_err(&r->plans[k])) SPWS_TRY(rb.get(&errs[k], e, sizeof(int)));
+    if (const int* e = rowwise_plan_err(&r->plan)) SPWS_TRY(rb.get(&err, e, sizeof(int)));
+    if (const int* e = rowwise_plan_abort(&r->plan)) SPWS_TRY(rb.get(&abort, e, sizeof(int)));
+    SPWS_TRY(rb.get(&bad, r->bad, sizeof(int)));
     SPWS_TRY(rb.wait());
+  } else {
+    SPWS_CUDA(cudaStreamSynchronize(r->s));
   }
   if (ms) cudaEventElapsedTime(ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  for (int e : errs)
-    if (e) {
-      set_error("numeric pass wrote a different number of entries than the symbolic pass counted");
-      return SPWS_ERR_CUDA;
-    }
+  if (abort || bad) {
+    set_error("the instances' arrays changed since the plan was made (operands that fail the checks, or an output "
+              "that no longer fits the views' places): the views are not valid; make a new plan");
+    return SPWS_ERR_CAPACITY;
+  }
+  if (err) {
+    set_error("numeric pass wrote a different number of entries than the symbolic pass counted");
+    return SPWS_ERR_CUDA;
+  }
   return SPWS_OK;
 }
 
@@ -235,6 +228,7 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
   Inst *dia = nullptr, *dib = nullptr;
   long long *darow = nullptr, *dannz = nullptr, *dbrow = nullptr, *dbnnz = nullptr, *dnnzoff = nullptr;
   int32_t* dshift = nullptr;
+  int* dbad = nullptr;
   SPWS_TRY(dalloc((void**)&dia, sizeof(Inst) * count, s));
   SPWS_TRY(dalloc((void**)&dib, sizeof(Inst) * count, s));
   SPWS_TRY(dalloc((void**)&darow, sizeof(long long) * count, s));
@@ -242,6 +236,8 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
   SPWS_TRY(dalloc((void**)&dbrow, sizeof(long long) * count, s));
   SPWS_TRY(dalloc((void**)&dbnnz, sizeof(long long) * count, s));
   SPWS_TRY(dalloc((void**)&dnnzoff, sizeof(long long) * count, s));
+  SPWS_TRY(dalloc((void**)&dbad, sizeof(int), s));
+  SPWS_CUDA(cudaMemsetAsync(dbad, 0, sizeof(int), s));
   SPWS_CUDA(cudaMemcpyAsync(dia, ia.data(), sizeof(Inst) * count, cudaMemcpyHostToDevice, s));
   SPWS_CUDA(cudaMemcpyAsync(dib, ib.data(), sizeof(Inst) * count, cudaMemcpyHostToDevice, s));
   SPWS_CUDA(cudaMemcpyAsync(darow, arow.data(), sizeof(long long) * count, cudaMemcpyHostToDevice, s));
@@ -268,64 +264,41 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
     k_row_shift<<<(unsigned)((ar + 255) / 256), 256, 0, s>>>(count, dib, darow, (int32_t)ar, dshift);
     count_launch(1);
   }
-  k_cat_pos<<<(unsigned)((ar + 256) / 256), 256, 0, s>>>(count, dia, darow, (int32_t)ar, az, Ab.pos);
-  k_cat_pos<<<(unsigned)((br + 256) / 256), 256, 0, s>>>(count, dib, dbrow, (int32_t)br, bz, Bb.pos);
-  if (az > 0) k_cat_ent<<<(unsigned)((az + 255) / 256), 256, 0, s>>>(count, dia, dannz, az, Ab.crd, Ab.vals);
-  if (bz > 0) k_cat_ent<<<(unsigned)((bz + 255) / 256), 256, 0, s>>>(count, dib, dbnnz, bz, Bb.crd, Bb.vals);
-  count_launch(4);
+  // the assembly: positions and entries of both super-operands
+  auto assemble = [&](cudaStream_t st) -> int {
+    k_cat_pos<<<(unsigned)((ar + 256) / 256), 256, 0, st>>>(count, dia, darow, (int32_t)ar, az, Ab.pos);
+    k_cat_pos<<<(unsigned)((br + 256) / 256), 256, 0, st>>>(count, dib, dbrow, (int32_t)br, bz, Bb.pos);
+    int k = 2;
+    if (az > 0) {
+      k_cat_ent<<<(unsigned)((az + 255) / 256), 256, 0, st>>>(count, dia, dannz, az, Ab.crd, Ab.vals);
+      k++;
+    }
+    if (bz > 0) {
+      k_cat_ent<<<(unsigned)((bz + 255) / 256), 256, 0, st>>>(count, dib, dbnnz, bz, Bb.crd, Bb.vals);
+      k++;
+    }
+    return k;
+  };
+  count_launch(assemble(s));
   SPWS_CUDA(cudaGetLastError());
   // the instances may come from anywhere: check the assembled operands once
   int rc = validate_csr_device(Ab.pos, Ab.crd, Ab.nrows, Ab.ncols, Ab.nnz, "batched A", s);
   if (rc == SPWS_OK) rc = validate_csr_device(Bb.pos, Bb.crd, Bb.nrows, Bb.ncols, Bb.nnz, "batched B", s);
 
-  // Group instances so that each group's products (an upper bound of its
-  // output) stay below 2^31 and its positions fit int32.
-  std::vector<int> gstart;
-  std::vector<unsigned long long> iprod(count, 0);
-  if (rc == SPWS_OK) {
-    unsigned long long* dprod = nullptr;
-    SPWS_TRY(dalloc((void**)&dprod, sizeof(unsigned long long) * count, s));
-    SPWS_CUDA(cudaMemsetAsync(dprod, 0, sizeof(unsigned long long) * count, s));
-    if (ar > 0) {
-      k_inst_products<<<(unsigned)((ar + 255) / 256), 256, 0, s>>>(count, darow, (int32_t)ar, Ab.pos, Ab.crd, Bb.pos,
-                                                                 dprod);
-      count_launch(1);
-    }
-    SPWS_CUDA(cudaMemcpyAsync(iprod.data(), dprod, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, s));
-    SPWS_CUDA(cudaStreamSynchronize(s));
-    dfree(dprod, s);
-    gstart.push_back(0);
-    unsigned long long acc = 0;
-    for (int i = 0; i < count; i++) {
-      if (iprod[i] > (unsigned long long)INT32_MAX) {
-        // one instance alone may still fit: its real output can be smaller
-        // than its products; the pipeline checks the exact count
-      }
-      if (i > gstart.back() && acc + iprod[i] > (unsigned long long)INT32_MAX) {
-        gstart.push_back(i);
-        acc = 0;
-      }
-      acc += iprod[i];
-    }
-    gstart.push_back(count);
-  }
-
-  // results: one shared allocation per array for the whole batch
+  // one pipeline over every instance's rows, 64-bit positions into one pool
   int32_t* opos = nullptr;
-  SPWS_TRY(dalloc((void**)&opos, sizeof(int32_t) * ((size_t)ar + count), s));
-  std::vector<spws_csr_dev> parts;
-  std::vector<RowwisePlan> plans;
-  long long total_nnz = 0, total_products = 0;
-  float ms_kernels = 0.f;
-  for (size_t g = 0; rc == SPWS_OK && g + 1 < gstart.size(); g++) {
-    const int first = gstart[g], last = gstart[g + 1];
-    const int32_t row0 = (int32_t)arow[first];
-    const int32_t rows = (int32_t)((last < count ? arow[last] : ar) - row0);
+  if (rc == SPWS_OK) rc = dalloc((void**)&opos, sizeof(int32_t) * ((size_t)ar + count), s);
+  spws_csr_dev Cg{};
+  spws_spgemm_stats st{};
+  RowwisePlan plan;
+  bool have_plan = false;
+  std::vector<long long> nnzoff(count);
+  if (rc == SPWS_OK) {
     CsrView Av;
-    Av.nrows = rows;
+    Av.nrows = Ab.nrows;
     Av.ncols = Ab.ncols;
     Av.nnz = Ab.nnz;
-    Av.pos = Ab.pos + row0;
+    Av.pos = Ab.pos;
     Av.crd = Ab.crd;
     Av.vals = Ab.vals;
     CsrView Bv;
@@ -335,119 +308,122 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
     Bv.pos = Bb.pos;
     Bv.crd = Bb.crd;
     Bv.vals = Bb.vals;
-    spws_csr_dev Cg{};
-    spws_spgemm_stats st{};
-    RowwisePlan plan;
     SpgemmOpts gopt = opt;
-    gopt.col_shift = dshift + row0;  // columns come out per instance
+    gopt.col_shift = dshift;  // columns come out per instance
+    gopt.wide_positions = true;
     rc = rowwise_plan_symbolic(Av, Bv, &Cg, gopt, &plan, s);
+    have_plan = true;
     if (rc == SPWS_OK) rc = rowwise_plan_numeric(&plan, &Cg, &st);
-    if (rc != SPWS_OK || !replay) {
-      rowwise_plan_free(&plan);
-    } else {
-      plans.push_back(plan);
-    }
-    if (rc != SPWS_OK) {
-      dfree(Cg.pos, s);
-      dfree(Cg.crd, s);
-      dfree(Cg.vals, s);
-      break;
-    }
-    total_nnz += Cg.nnz;
-    total_products += st.products;
-    ms_kernels += st.ms_total;
-    if (rows > 0) {
-      k_split_pos<<<(unsigned)((rows + 255) / 256), 256, 0, s>>>(count, dia, darow, first, row0, rows, Cg.pos,
-                                                                 opos + row0 + first, dnnzoff);
-      count_launch(1);
-    }
-    k_zero_rows<<<(unsigned)((last - first + 255) / 256), 256, 0, s>>>(count, dia, first, last, dnnzoff, row0, Cg.pos,
-                                                                      opos + row0 + first);
-    count_launch(1);
-    SPWS_CUDA(cudaGetLastError());
-    parts.push_back(Cg);
   }
-  std::vector<long long> nnzoff(count);
+  const long long* gpos = have_plan && rc == SPWS_OK ? rowwise_plan_pos64(&plan) : nullptr;
+  auto split = [&](cudaStream_t sst, const long long* check, const int* abort) -> int {
+    int k = 0;
+    if (ar > 0 && gpos) {
+      k_split_pos64<<<(unsigned)((ar + 255) / 256), 256, 0, sst>>>(count, dia, darow, (int32_t)ar, gpos, opos, dnnzoff,
+                                                                   check, dbad, abort);
+      k++;
+    }
+    if (gpos) {
+      k_split_empty<<<(unsigned)((count + 255) / 256), 256, 0, sst>>>(count, dia, gpos, opos, dnnzoff, abort);
+      k++;
+      if (check) {
+        k_check_total<<<1, 1, 0, sst>>>(gpos + ar, Cg.nnz, dbad, abort);
+        k++;
+      }
+    } else {  // no rows at all: every instance is empty (errors surface at the next check)
+      cudaMemsetAsync(opos, 0, sizeof(int32_t) * ((size_t)ar + count), sst);
+      cudaMemsetAsync(dnnzoff, 0, sizeof(long long) * count, sst);
+    }
+    count_launch(k);
+    return k;
+  };
+  int bad = 0;
   if (rc == SPWS_OK) {
+    split(s, nullptr, nullptr);
+    SPWS_CUDA(cudaGetLastError());
     SPWS_CUDA(cudaMemcpyAsync(nnzoff.data(), dnnzoff, sizeof(long long) * count, cudaMemcpyDeviceToHost, s));
+    SPWS_CUDA(cudaMemcpyAsync(&bad, dbad, sizeof(int), cudaMemcpyDeviceToHost, s));
     SPWS_CUDA(cudaEventRecord(e1, s));
     SPWS_CUDA(cudaStreamSynchronize(s));
-    // per-instance views into the group results; the first instance of each
-    // group owns its group's crd/vals arrays and the first instance of the
-    // batch owns opos
-    for (size_t g = 0; g + 1 < gstart.size(); g++) {
-      const int first = gstart[g], last = gstart[g + 1];
-      for (int i = first; i < last; i++) {
-        C[i].nrows = A[i].nrows;
-        C[i].ncols = B[i].ncols;
-        C[i].pos = opos + arow[i] + i;
-        C[i].crd = parts[g].crd + nnzoff[i];
-        C[i].vals = parts[g].vals + nnzoff[i];
-        const long long end = (i + 1 < last) ? nnzoff[i + 1] : parts[g].nnz;
-        C[i].nnz = end - nnzoff[i];
-      }
-      if (!replay) dfree(parts[g].pos, s);  // a replay's numeric kernels read the group positions again
+    if (bad == 2) {
+      set_error("batched: an instance's output has more than INT32_MAX nonzeros");
+      rc = SPWS_ERR_CAPACITY;
     }
-  } else {
-    for (auto& p : parts) {
-      dfree(p.pos, s);
-      dfree(p.crd, s);
-      dfree(p.vals, s);
+  }
+  if (rc == SPWS_OK) {
+    for (int i = 0; i < count; i++) {  // per-instance views into the pool
+      C[i].nrows = A[i].nrows;
+      C[i].ncols = B[i].ncols;
+      C[i].pos = opos + arow[i] + i;
+      C[i].crd = Cg.crd + nnzoff[i];
+      C[i].vals = Cg.vals + nnzoff[i];
+      const long long end = i + 1 < count ? nnzoff[i + 1] : Cg.nnz;
+      C[i].nnz = end - nnzoff[i];
     }
-    dfree(opos, s);
   }
   if (stats && rc == SPWS_OK) {
     stats->instances = count;
-    stats->groups = (int32_t)(gstart.size() - 1);
-    stats->products = total_products;
-    stats->nnz = total_nnz;
-    stats->ms_kernels = ms_kernels;
+    stats->groups = 1;
+    stats->products = st.products;
+    stats->nnz = Cg.nnz;
+    stats->ms_kernels = st.ms_total;
     cudaEventElapsedTime(&stats->ms_total, e0, e1);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc == SPWS_OK && replay) {
-    // Capture the numeric work of the whole batch: gather the instances'
-    // current values into the super-operands and rerun every group's numeric
-    // kernels into the same C arrays.
+    // The whole solve in one CUDA graph: assemble the super-operands from the
+    // instances' current arrays, rerun the row-wise pipeline into the plan's
+    // buffers (row analysis, ordering, symbolic pass, scan, numeric pass) and
+    // split the positions per instance. The instances' structure must be the
+    // one the plan was made with (the views keep their places in the pool);
+    // the graph's own checks report otherwise.
     auto* r = new BatchReplay();
     r->s = s;
-    r->plans = plans;
-    plans.clear();
-    r->owned = {dia, dib, darow, dannz, dbrow, dbnnz, dnnzoff, dshift, Ab.pos, Ab.crd, Ab.vals,
-                Bb.pos, Bb.crd, Bb.vals};
-    for (auto& p : parts) r->owned.push_back(p.pos);
-    cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-    int crc = ce == cudaSuccess ? SPWS_OK : SPWS_ERR_CUDA;
+    r->plan = plan;
+    r->have_plan = true;
+    have_plan = false;
+    r->bad = dbad;
+    r->owned = {dia,    dib,    darow,  dannz,  dbrow,  dbnnz, dnnzoff, dshift,
+                Ab.pos, Ab.crd, Ab.vals, Bb.pos, Bb.crd, Bb.vals, dbad};
+    long long* check = nullptr;  // the offsets the views were made with
+    int crc = dalloc((void**)&check, sizeof(long long) * count, s);
     if (crc == SPWS_OK) {
-      if (az > 0) {
-        k_cat_ent<<<(unsigned)((az + 255) / 256), 256, 0, s>>>(count, dia, dannz, az, Ab.crd, Ab.vals);
-        r->kernels++;
-      }
-      if (bz > 0) {
-        k_cat_ent<<<(unsigned)((bz + 255) / 256), 256, 0, s>>>(count, dib, dbnnz, bz, Bb.crd, Bb.vals);
-        r->kernels++;
-      }
-      for (size_t g = 0; crc == SPWS_OK && g + 1 < gstart.size(); g++) {
-        crc = rowwise_plan_launch_numeric(&r->plans[g], s);
-        r->kernels += 2;
+      r->owned.push_back(check);
+      if (cudaMemcpyAsync(check, dnnzoff, sizeof(long long) * count, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess) {
+        (void)cudaGetLastError();
+        set_error("batched: copying the pool offsets failed");
+        crc = SPWS_ERR_CUDA;
       }
     }
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ee = cudaStreamEndCapture(s, &graph);
-    r->graph = graph;
-    if (crc == SPWS_OK && ee == cudaSuccess && graph)
-      ce = cudaGraphInstantiate(&r->exec, graph, 0);
-    else
-      ce = ee != cudaSuccess ? ee : cudaErrorUnknown;
+    cudaError_t ce = crc == SPWS_OK ? cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) : cudaSuccess;
+    if (crc == SPWS_OK && ce != cudaSuccess) crc = SPWS_ERR_CUDA;
+    if (crc == SPWS_OK) {
+      SPWS_CUDA(cudaMemsetAsync(dbad, 0, sizeof(int), s));
+      r->kernels += assemble(s);
+      // the instances' current arrays are checked on the device before any
+      // kernel follows their indices (a failure aborts the replay)
+      const long long l0 = (long long)spws_launch_count();
+      validate_csr_launch(Ab.pos, Ab.crd, Ab.nrows, Ab.ncols, Ab.nnz, dbad, s);
+      validate_csr_launch(Bb.pos, Bb.crd, Bb.nrows, Bb.ncols, Bb.nnz, dbad, s);
+      crc = rowwise_plan_launch_full(&r->plan, s, dbad);
+      r->kernels += (int)((long long)spws_launch_count() - l0);
+      if (crc == SPWS_OK) r->kernels += split(s, check, rowwise_plan_abort(&r->plan));
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+      r->graph = graph;
+      if (crc == SPWS_OK && ee == cudaSuccess && graph)
+        ce = cudaGraphInstantiate(&r->exec, graph, 0);
+      else
+        ce = ee != cudaSuccess ? ee : cudaErrorUnknown;
+    }
     if (crc != SPWS_OK || ce != cudaSuccess) {
       (void)cudaGetLastError();
-      if (crc == SPWS_OK) set_error(std::string("capturing the batch's numeric graph failed: ") + cudaGetErrorString(ce));
-      delete r;  // frees the group positions and operands with it
-      for (auto& p : parts) {
-        dfree(p.crd, s);
-        dfree(p.vals, s);
-      }
+      if (crc == SPWS_OK) set_error(std::string("capturing the batch's graph failed: ") + cudaGetErrorString(ce));
+      delete r;  // frees the plan and operands with it
+      dfree(Cg.crd, s);
+      dfree(Cg.vals, s);
       dfree(opos, s);
       rc = crc != SPWS_OK ? crc : SPWS_ERR_CUDA;
     } else {
@@ -456,21 +432,24 @@ int spgemm_batched(int count, const spws_csr_dev* A, const spws_csr_dev* B, spws
     dia = dib = nullptr;
     darow = dannz = dbrow = dbnnz = dnnzoff = nullptr;
     dshift = nullptr;
+    dbad = nullptr;
     Ab.pos = Ab.crd = Bb.pos = Bb.crd = nullptr;
     Ab.vals = Bb.vals = nullptr;
+  } else if (rc != SPWS_OK) {
+    dfree(Cg.crd, s);
+    dfree(Cg.vals, s);
+    dfree(opos, s);
   }
-  for (auto& p : plans) rowwise_plan_free(&p);
+  if (have_plan) rowwise_plan_free(&plan);
   dfree(dia, s); dfree(dib, s); dfree(darow, s); dfree(dannz, s); dfree(dbrow, s); dfree(dbnnz, s); dfree(dnnzoff, s);
-  dfree(dshift, s);
+  dfree(dshift, s); dfree(dbad, s);
   dfree(Ab.pos, s); dfree(Ab.crd, s); dfree(Ab.vals, s);
   dfree(Bb.pos, s); dfree(Bb.crd, s); dfree(Bb.vals, s);
   if (rc == SPWS_OK && owner) {
     owner->stream = s;
     owner->blocks.push_back(opos);
-    for (size_t g = 0; g + 1 < gstart.size(); g++) {
-      owner->blocks.push_back(parts[g].crd);
-      owner->blocks.push_back(parts[g].vals);
-    }
+    owner->blocks.push_back(Cg.crd);
+    owner->blocks.push_back(Cg.vals);
   }
   return rc;
 }

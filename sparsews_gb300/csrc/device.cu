@@ -177,6 +177,11 @@ void launch_validate_csr(int32_t n, int64_t nnz, int32_t ncols, const int32_t* p
 
 }  // namespace
 
+void validate_csr_launch(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz, int* bad,
+                         cudaStream_t s) {
+  if (nrows > 0) launch_validate_csr(nrows, nnz, ncols, pos, crd, bad, s);
+}
+
 int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
                         const char* what, cudaStream_t s) {
   if (nrows < 0 || ncols < 0 || nnz < 0 || nnz > INT32_MAX) {

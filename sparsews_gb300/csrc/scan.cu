@@ -2,9 +2,11 @@
 //
 // Three launches over tiles of 2048 counts: per-tile sums, a single-CTA scan
 // of the tile sums, and a per-tile scan that adds the tile's prefix. Sums are
-// carried in 64 bits; the caller checks the 64-bit total against INT32_MAX
-// before trusting the int32 positions (the output positions of the row-wise
-// SpGEMM are int32, as in the reference's taco_tensor_t).
+// carried in 64 bits and written as int64 positions (what the row kernels
+// index C with, so a batch's pooled output may exceed 2^31 entries) and/or as
+// int32 positions, which the caller trusts only once it has checked the
+// 64-bit total against INT32_MAX (the positions of the reference's
+// taco_tensor_t are int32).
 #include "spws_internal.h"
 
 namespace spws {
@@ -72,9 +74,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(long long* __re
   if (threadIdx.x == 0) *total = carry;
 }
 
+// Writes the positions as int32 (out, when given: valid while the total fits)
+// and as int64 (out64, when given).
 __global__ void __launch_bounds__(kScanThreads) k_tile_scan(const int32_t* __restrict__ in, int64_t n,
                                                             const long long* __restrict__ tile_prefix,
-                                                            int32_t* __restrict__ out,
+                                                            int32_t* __restrict__ out, long long* __restrict__ out64,
                                                             const long long* __restrict__ total) {
   const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanPer;
   long long v[kScanPer];
@@ -91,52 +95,48 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_scan(const int32_t* __res
 #pragma unroll
   for (int q = 0; q < kScanPer; q++) {
     int64_t idx = base + q;
-    if (idx < n) out[idx] = (int32_t)run;
+    if (idx < n) {
+      if (out) out[idx] = (int32_t)run;
+      if (out64) out64[idx] = run;
+    }
     run += v[q];
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = (int32_t)(*total);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (out) out[n] = (int32_t)(*total);
+    if (out64) out64[n] = *total;
+  }
+}
+
+__global__ void k_store_zero_pos(int32_t* out, long long* out64, long long* total) {
+  if (out) *out = 0;
+  if (out64) *out64 = 0;
+  *total = 0;
 }
 
 }  // namespace
 
-int scan_counts_i32(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev, cudaStream_t s) {
+int scan_positions(const int32_t* counts, int32_t* out, long long* out64, int64_t n, long long* total_dev,
+                   long long* tile_scratch, cudaStream_t s) {
   const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
   if (ntiles == 0) {
-    SPWS_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), s));
-    SPWS_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(long long), s));
+    k_store_zero_pos<<<1, 1, 0, s>>>(out, out64, total_dev);
+    count_launch(1);
+    SPWS_CUDA(cudaGetLastError());
     return SPWS_OK;
   }
-  long long* tile = nullptr;
-  SPWS_TRY(dalloc((void**)&tile, sizeof(long long) * ntiles, s));
+  long long* tile = tile_scratch;
+  if (!tile) SPWS_TRY(dalloc((void**)&tile, sizeof(long long) * ntiles, s));
   k_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile);
   k_scan_tile_sums<<<1, kScanThreads, 0, s>>>(tile, ntiles, total_dev);
-  k_tile_scan<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile, out, total_dev);
+  k_tile_scan<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile, out, out64, total_dev);
   count_launch(3);
   SPWS_CUDA(cudaGetLastError());
-  dfree(tile, s);
+  if (!tile_scratch) dfree(tile, s);
   return SPWS_OK;
 }
 
-}  // namespace spws
-
-namespace spws {
-
-// Same scan as scan_counts_i32, with the per-tile sums kept in `tile_scratch`
-// (at least ceil(n / 2048) entries) instead of a pool allocation.
-int scan_counts_i32_into(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev,
-                         long long* tile_scratch, cudaStream_t s) {
-  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
-  if (ntiles == 0) {
-    SPWS_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), s));
-    SPWS_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(long long), s));
-    return SPWS_OK;
-  }
-  k_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile_scratch);
-  k_scan_tile_sums<<<1, kScanThreads, 0, s>>>(tile_scratch, ntiles, total_dev);
-  k_tile_scan<<<(unsigned)ntiles, kScanThreads, 0, s>>>(counts, n, tile_scratch, out, total_dev);
-  count_launch(3);
-  SPWS_CUDA(cudaGetLastError());
-  return SPWS_OK;
+int scan_counts_i32(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev, cudaStream_t s) {
+  return scan_positions(counts, out, nullptr, n, total_dev, nullptr, s);
 }
 
 }  // namespace spws

@@ -233,31 +233,33 @@ __global__ void __launch_bounds__(kScanT) k_scan_tiles(const T* __restrict__ in,
 }
 
 template <typename T>
-int scan64_impl(const T* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s) {
+int scan64_impl(const T* in, long long* out, int64_t n, long long* total_dev, long long* tile_scratch,
+                cudaStream_t s) {
   const int64_t nt = (n + kScanTile - 1) / kScanTile;
   if (nt == 0) {
     if (total_dev) SPWS_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(long long), s));
     return SPWS_OK;
   }
-  long long* ts = nullptr;
-  SPWS_TRY(dalloc((void**)&ts, sizeof(long long) * nt, s));
+  long long* ts = tile_scratch;
+  if (!ts) SPWS_TRY(dalloc((void**)&ts, sizeof(long long) * nt, s));
   k_sum_tiles<T><<<(unsigned)nt, kScanT, 0, s>>>(in, n, ts);
   k_scan_sums<<<1, kScanT, 0, s>>>(ts, nt, total_dev);
   k_scan_tiles<T><<<(unsigned)nt, kScanT, 0, s>>>(in, n, ts, out);
   count_launch(3);
   SPWS_CUDA(cudaGetLastError());
-  dfree(ts, s);
+  if (!tile_scratch) dfree(ts, s);
   return SPWS_OK;
 }
 
 }  // namespace
 
-int scan_i32_to_i64(const int32_t* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s) {
-  return scan64_impl<int32_t>(in, out, n, total_dev, s);
+int scan_i32_to_i64(const int32_t* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s,
+                    long long* tile_scratch) {
+  return scan64_impl<int32_t>(in, out, n, total_dev, tile_scratch, s);
 }
 
 int scan_i64(const long long* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s) {
-  return scan64_impl<long long>(in, out, n, total_dev, s);
+  return scan64_impl<long long>(in, out, n, total_dev, nullptr, s);
 }
 
 int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigned long long* keys_tmp,

@@ -5,7 +5,9 @@
 
 namespace spws {
 // Exclusive scans; *total_dev (may be null) receives the sum.
-int scan_i32_to_i64(const int32_t* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s);
+// tile_scratch: ceil(n / 2048) entries for the tile sums (null: allocated).
+int scan_i32_to_i64(const int32_t* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s,
+                    long long* tile_scratch = nullptr);
 int scan_i64(const long long* in, long long* out, int64_t n, long long* total_dev, cudaStream_t s);
 
 // Stable sort of n (key, payload) pairs by bits [begin_bit, key_bits) of key

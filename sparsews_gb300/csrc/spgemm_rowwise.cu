@@ -72,7 +72,8 @@ __device__ __forceinline__ int cost_bucket(long long p) { return p <= 0 ? 0 : 64
 __global__ void k_row_info(int32_t nA, const int32_t* __restrict__ Ap, const int32_t* __restrict__ Aj,
                            const int32_t* __restrict__ Bp, const int32_t* __restrict__ Bk, RowInfo* __restrict__ info,
                            int* __restrict__ hist, unsigned long long* __restrict__ total_products,
-                           int* __restrict__ err) {
+                           int* __restrict__ err, const int* __restrict__ abort) {
+  if (abort && *abort) return;  // a relaunched plan whose operands failed their checks
   __shared__ int h[kBuckets];
   __shared__ unsigned long long tp;
   for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) h[b] = 0;
@@ -167,6 +168,18 @@ __global__ void k_bitmap_words(int32_t nA, const RowInfo* __restrict__ info, int
                                                                             : 0;
 }
 
+// One thread: sets *abort when *count exceeds cap; with reset, zeroes *count
+// afterwards (the scan's total field is reused by the next scan).
+__global__ void k_check_capacity(long long* count, long long cap, int* abort, int reset) {
+  if (*count > cap) *abort = 1;
+  if (reset) *count = 0;
+}
+
+// One thread: *flag = 1 when *cond is nonzero.
+__global__ void k_raise_if(const int* cond, int* flag) {
+  if (*cond) *flag = 1;
+}
+
 struct PassArgs {
   const int32_t* Ap;
   const int32_t* Aj;
@@ -181,7 +194,7 @@ struct PassArgs {
   int* counter;
   int* light_counter;
   int32_t* rowcnt;     // symbolic output
-  const int32_t* Cp;   // numeric input
+  const long long* Cp; // numeric input: C's row positions, 64-bit (a batch's pooled output may pass 2^31)
   int32_t* Ck;         // numeric output
   double* Cv;          // numeric output
   int* err;            // set on internal inconsistency
@@ -200,6 +213,9 @@ struct PassArgs {
   // shared-memory rank windows. 0: always windows.
   int l2_rank_max;
   const int32_t* col_shift;  // per A row, subtracted from the written columns (nullptr: none)
+  // When set and nonzero, the kernels return at once: a replayed plan whose
+  // operands outgrew the buffers it was made with (see k_check_capacity).
+  const int* abort;
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -222,6 +238,7 @@ constexpr int kL2RankMax = 16384; // default PassArgs::l2_rank_max: 128 KB of C.
 static_assert(kL2RankMax < 65536, "L2-pass ranks are taken from the 16-bit word prefixes");
 static_assert(kThreads * (kLongMinMax - 1) < (1 << 17), "short slices (< long_min entries) fill at most 17 bits");
 constexpr int kChunkLen = 128;   // packed entries per warp work item (4 rounds of 32 lanes)
+constexpr int kStageInts = 320;  // per warp: C.crd staging of the bitmap walk (in the batch + bound table)
 
 // Shared staging of one batch of j's. Every thread t loads one B-row slice
 // (start s[t], length len[t], A value a[t]). Long slices (>= kLongMin
@@ -239,6 +256,9 @@ struct Batch {
   int16_t slot[kThreads];
   unsigned long long wsum[kWarps];  // per-warp totals of fill_batch's scan
 };
+
+static_assert(kWarps * kStageInts * sizeof(int32_t) <= sizeof(Batch) + sizeof(int32_t) * kBoundInts,
+              "the walk's C.crd staging fits the batch and the bound table");
 
 // Work of one loaded batch: pieces of long slices, then chunks of the
 // packed short-slice stream.
@@ -494,6 +514,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_symbolic(PassArgs a) {
   Batch& b = *reinterpret_cast<Batch*>(smem + sizeof(uint32_t) * kSpanWords);
   __shared__ int wsum[kWarps];
   __shared__ int s_idx;
+  if (a.abort && *a.abort) return;
   const int nwork = *a.nheavy;
   const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
@@ -547,6 +568,7 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
   __shared__ int s_idx;
   __shared__ int32_t s_cols[2];
   __shared__ int32_t s_wcol[kMaxWin + 1];
+  if (a.abort && *a.abort) return;
   if (!L2W)
     for (int q = threadIdx.x; q < ACC; q += kThreads) acc[q] = 0.0;
   const int nwork = *a.nheavy;
@@ -562,9 +584,9 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
     const RowInfo ri = a.info[i];
     const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
     const bool multi = (long long)ri.hi - ri.lo + 1 > kSpanBits;
-    const int32_t row_end = a.Cp[i + 1];
+    const long long row_end = a.Cp[i + 1];
     const int32_t shift = a.col_shift ? a.col_shift[i] : 0;
-    int32_t out = a.Cp[i];
+    long long out = a.Cp[i];
     next = claim(a.counter, &s_idx, a, t0);
     for (long long wl = ri.lo; wl <= ri.hi; wl += kSpanBits) {
       const int32_t wlo = (int32_t)wl;
@@ -615,6 +637,8 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
       }
       // The same walk stores each word's prefix and writes its columns, in
       // order, at their ranks. Words past nw inside the last group are zero.
+      // the warp's staging area: the batch and bound table, idle during the walk
+      int32_t* stage = reinterpret_cast<int32_t*>(&b) + warp * kStageInts;
       for (int gb = c0; gb < c1; gb += 32) {
         const int g = gb + lane;
         const uint4 v = g < c1 ? bm4[g] : make_uint4(0u, 0u, 0u, 0u);
@@ -627,6 +651,12 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
           if (lane >= o) incl += y;
         }
         int r = run + incl - tot;
+        const int step_total = __shfl_sync(0xffffffffu, incl, 31);
+        // The step's columns are one contiguous run of C.crd; a lane's own
+        // columns are a short piece of it. They go through the warp's
+        // staging area first (when they fit), so that the stores to C.crd
+        // are made by consecutive lanes at consecutive addresses.
+        const bool staged = step_total <= kStageInts;  // warp-uniform
         if (g < c1) {
           if (((4 * g) & (kGroupWords - 1)) == 0) gbase[(4 * g) / kGroupWords] = (uint32_t)r;
           const int p1 = r + __popc(v.x), p2 = p1 + __popc(v.y), p3 = p2 + __popc(v.z);
@@ -635,6 +665,7 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
               make_uint2((uint32_t)(uint16_t)r | ((uint32_t)(uint16_t)p1 << 16),
                          (uint32_t)(uint16_t)p2 | ((uint32_t)(uint16_t)p3 << 16));
         }
+        int32_t* dst = staged ? stage - run : a.Ck + out;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
           uint32_t word = words[k];
@@ -642,11 +673,16 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
           while (word) {
             const int bit = __ffs(word) - 1;
             word &= word - 1;
-            a.Ck[out + r] = col0 + bit;
+            dst[r] = col0 + bit;
             r++;
           }
         }
-        run += __shfl_sync(0xffffffffu, incl, 31);
+        if (staged) {
+          __syncwarp();
+          for (int t = lane; t < step_total; t += 32) a.Ck[out + run + t] = stage[t];
+          __syncwarp();
+        }
+        run += step_total;
       }
       __syncthreads();
       // prefix of word w: the group's 32-bit base plus the 16-bit difference
@@ -830,6 +866,7 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
   unsigned long long* key = reinterpret_cast<unsigned long long*>(smem) + (size_t)warp * STAGE;
   double* val = reinterpret_cast<double*>(smem + sizeof(unsigned long long) * STAGE * kLightWarps) +
                 (size_t)warp * STAGE;
+  if (a.abort && *a.abort) return;
   const int lo_idx = *a.nheavy, hi_idx = *a.nwork;
   const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
@@ -878,7 +915,7 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light(PassArgs a) {
     }
     // runs of equal columns; values in the sorted (visiting) order
     int rank = 0;
-    const int32_t out = NUMERIC ? a.Cp[i] : 0;
+    const long long out = NUMERIC ? a.Cp[i] : 0;
     for (int b0 = 0; b0 < n; b0 += 32) {
       const int p = b0 + lane;
       const uint32_t col = p < n ? (uint32_t)(key[p] >> 32) : 0u;
@@ -957,6 +994,7 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light_hash(PassArgs a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int32_t* hk = reinterpret_cast<int32_t*>(smem) + (size_t)warp * H;
   double* hv = reinterpret_cast<double*>(smem + sizeof(int32_t) * H * kLightWarps) + (size_t)warp * H;
+  if (a.abort && *a.abort) return;
   const int lo_idx = *a.nheavy, hi_idx = *a.nwork;
   const unsigned long long t0 = a.yield_ctas ? global_ns() : 0;
   for (;;) {
@@ -1070,7 +1108,7 @@ __global__ void __launch_bounds__(kLightWarps * 32) k_light_hash(PassArgs a) {
       warp_sort_pairs<2>(kc, kv);
     else
       warp_sort_pairs<4>(kc, kv);
-    const int32_t out = a.Cp[i];
+    const long long out = a.Cp[i];
     const int32_t shift = a.col_shift ? a.col_shift[i] : 0;
 #pragma unroll
     for (int e = 0; e < 4; e++) {
@@ -1229,6 +1267,7 @@ struct RowwisePlanImpl {
     // tiers, [5..7] light numeric tiers
     int counter[8];
     int err;
+    int abort;  // a relaunch outgrew the plan's buffers (k_check_capacity)
     unsigned long long products;
     long long nnz;
   };
@@ -1242,6 +1281,12 @@ struct RowwisePlanImpl {
   int32_t* rowcnt = nullptr;
   int32_t* bmwords = nullptr;
   long long* bmoff = nullptr;
+  long long* pos64 = nullptr;  // C's row positions as int64, what the numeric kernels index with
+  long long* tiles = nullptr;  // tile sums of the two scans (ceil(rows / 2048))
+  long long cap_words = 0;     // bitmap store and output entries the plan was sized for
+  long long cap_nnz = 0;
+  int32_t* pos32 = nullptr;    // C->pos (int32), or null with wide positions
+  bool wide_pos = false;
   uint32_t* bmstore = nullptr;
   size_t bmstore_bytes = 0;
   PassArgs pa{};
@@ -1281,13 +1326,15 @@ struct RowwisePlanImpl {
     dfree(rowcnt, s);
     dfree(bmwords, s);
     dfree(bmoff, s);
+    dfree(pos64, s);
+    dfree(tiles, s);
     dfree(bmstore, s);
   }
 };
 
 size_t rowwise_scratch_bytes(int32_t nrows) {
   return sizeof(RowwisePlanImpl::Small) + (size_t)std::max(nrows, 1) * (sizeof(RowInfo) + 3 * sizeof(int32_t) +
-                                                                         sizeof(long long)) + 4096;
+                                                                         2 * sizeof(long long)) + 4096;
 }
 
 // Phase 1: row analysis, cost order, symbolic pass, scan into C->pos.
@@ -1311,9 +1358,11 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   for (auto& e : P->ev) SPWS_CUDA(cudaEventCreate(&e));
   P->have_events = true;
   SPWS_CUDA(cudaEventRecord(P->ev[0], s));
-  SPWS_TRY(dalloc((void**)&C->pos, sizeof(int32_t) * ((size_t)nA + 1), s));
+  P->wide_pos = opt.wide_positions;
+  if (!P->wide_pos) SPWS_TRY(dalloc((void**)&C->pos, sizeof(int32_t) * ((size_t)nA + 1), s));
+  P->pos32 = C->pos;
   if (nA == 0) {
-    SPWS_CUDA(cudaMemsetAsync(C->pos, 0, sizeof(int32_t), s));
+    if (C->pos) SPWS_CUDA(cudaMemsetAsync(C->pos, 0, sizeof(int32_t), s));
     P->empty = true;
     plan->nnz = 0;
     plan->products = 0;
@@ -1323,12 +1372,13 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   SPWS_TRY(dalloc((void**)&P->info, sizeof(RowInfo) * (size_t)nA, s));
   SPWS_TRY(dalloc((void**)&P->order, sizeof(int32_t) * (size_t)nA, s));
   SPWS_TRY(dalloc((void**)&P->rowcnt, sizeof(int32_t) * (size_t)nA, s));
+  SPWS_TRY(dalloc((void**)&P->tiles, sizeof(long long) * (((size_t)nA + 2047) / 2048 + 1), s));
   SPWS_CUDA(cudaMemsetAsync(P->sm, 0, sizeof(RowwisePlanImpl::Small), s));
   SPWS_CUDA(cudaMemsetAsync(P->rowcnt, 0, sizeof(int32_t) * (size_t)nA, s));
   auto* sm = P->sm;
 
   k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A.pos, A.crd, B.pos, B.crd, P->info, sm->hist,
-                                                      &sm->products, &sm->err);
+                                                      &sm->products, &sm->err, &sm->abort);
   P->light_bucket = light_bucket_of(opt.light_max);
   P->wide = opt.wide_windows;
   P->heavy_sums = opt.heavy_sums;
@@ -1344,7 +1394,7 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   SPWS_TRY(dalloc((void**)&P->bmoff, sizeof(long long) * (size_t)nA, s));
   k_bitmap_words<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, P->bmwords, P->light_bucket);
   count_launch(1);
-  SPWS_TRY(scan_i32_to_i64(P->bmwords, P->bmoff, nA, &sm->nnz, s));
+  SPWS_TRY(scan_i32_to_i64(P->bmwords, P->bmoff, nA, &sm->nnz, s, P->tiles));
   long long words = 0;
   Readback rb(s);
   SPWS_TRY(rb.get(&words, &sm->nnz, sizeof(words)));
@@ -1383,6 +1433,7 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   pa.err = &sm->err;
   pa.long_min = opt.long_min;
   pa.col_shift = opt.col_shift;
+  pa.abort = &sm->abort;
   pa.l2_rank_max = opt.heavy_sums == 2 ? kL2RankMax : 0;
   RowKernelCfg& kc = P->kc;
   SPWS_TRY(row_kernel_cfg(ds->device, &kc));
@@ -1399,7 +1450,8 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
   SPWS_TRY(launch_light<false>(pa, sm->tier, &sm->counter[2], kc, ds->sm_count, P->waves_sym, P->yield_ns, s));
   SPWS_CUDA(cudaEventRecord(P->ev[2], s));
 
-  SPWS_TRY(scan_counts_i32(P->rowcnt, C->pos, nA, &sm->nnz, s));
+  SPWS_TRY(dalloc((void**)&P->pos64, sizeof(long long) * ((size_t)nA + 1), s));
+  SPWS_TRY(scan_positions(P->rowcnt, P->pos32, P->pos64, nA, &sm->nnz, P->tiles, s));
   SPWS_CUDA(cudaEventRecord(P->ev[3], s));
 
   int err = 0;
@@ -1411,10 +1463,12 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
     set_error("a row of A has 2^31 or more products");
     return SPWS_ERR_CAPACITY;
   }
-  if (P->nnz > INT32_MAX) {
+  if (P->nnz > INT32_MAX && !P->wide_pos) {
     set_error("output has more than INT32_MAX nonzeros; taco_tensor_t positions are int32");
     return SPWS_ERR_CAPACITY;
   }
+  P->cap_words = P->bmstore ? words : 0;
+  P->cap_nnz = P->nnz;
   plan->nnz = P->nnz;
   plan->products = (int64_t)P->products;
   plan->scratch_bytes = rowwise_scratch_bytes(nA) + P->bmstore_bytes;
@@ -1437,7 +1491,7 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
   SPWS_TRY(dalloc((void**)&C->vals, sizeof(double) * (size_t)std::max<long long>(nnz, 1), s));
   PassArgs& pa = P->pa;
   pa.counter = &P->sm->counter[1];
-  pa.Cp = C->pos;
+  pa.Cp = P->pos64;
   pa.Ck = C->crd;
   pa.Cv = C->vals;
   SPWS_CUDA(cudaEventRecord(P->ev[4], s));
@@ -1470,19 +1524,53 @@ int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* 
   return SPWS_OK;
 }
 
-int rowwise_plan_launch_numeric(RowwisePlan* plan, cudaStream_t s) {
+int rowwise_plan_launch_full(RowwisePlan* plan, cudaStream_t s, const int* invalid) {
   RowwisePlanImpl* P = static_cast<RowwisePlanImpl*>(plan->impl);
   if (P->empty) return SPWS_OK;
   DeviceState* ds = nullptr;
   SPWS_TRY(device_state(&ds));
-  SPWS_CUDA(cudaMemsetAsync(&P->sm->counter[1], 0, sizeof(int), s));
-  SPWS_CUDA(cudaMemsetAsync(&P->sm->counter[5], 0, sizeof(int) * kLightTiers, s));
-  const int g_num = ds->sm_count * std::max(P->per_num, 1);
+  const int32_t nA = P->A.nrows;
+  auto* sm = P->sm;
+  SPWS_CUDA(cudaMemsetAsync(sm, 0, sizeof(RowwisePlanImpl::Small), s));
+  SPWS_CUDA(cudaMemsetAsync(P->rowcnt, 0, sizeof(int32_t) * (size_t)nA, s));
+  if (invalid) {  // operands that failed their checks: every kernel below returns at once
+    k_raise_if<<<1, 1, 0, s>>>(invalid, &sm->abort);
+    count_launch(1);
+  }
+  k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, P->A.pos, P->A.crd, P->B.pos, P->B.crd, P->info, sm->hist,
+                                                      &sm->products, &sm->err, &sm->abort);
+  k_order_offsets<<<1, 32, 0, s>>>(sm->hist, sm->cursor, &sm->nwork, &sm->nheavy, P->light_bucket, sm->tier);
+  k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, sm->cursor, P->order);
+  k_bitmap_words<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, P->info, P->bmwords, P->light_bucket);
+  count_launch(4);
+  SPWS_TRY(scan_i32_to_i64(P->bmwords, P->bmoff, nA, &sm->nnz, s, P->tiles));
+  // the bitmaps must fit the store the plan made (none: rebuilt, nothing to check)
+  k_check_capacity<<<1, 1, 0, s>>>(&sm->nnz, P->bmstore ? P->cap_words : LLONG_MAX, &sm->abort, 1);
   PassArgs pa = P->pa;
-  pa.counter = &P->sm->counter[1];
+  pa.counter = &sm->counter[0];
+  const int g_sym = ds->sm_count * std::max(P->kc.per_sym, 1);
+  k_symbolic<<<g_sym, kThreads, kSymSmem, s>>>(pa);
+  count_launch(2);
+  SPWS_TRY(launch_light<false>(pa, sm->tier, &sm->counter[2], P->kc, ds->sm_count, 1, 0, s));
+  SPWS_TRY(scan_positions(P->rowcnt, P->pos32, P->pos64, nA, &sm->nnz, P->tiles, s));
+  // and the output must fit C's arrays
+  k_check_capacity<<<1, 1, 0, s>>>(&sm->nnz, P->cap_nnz, &sm->abort, 0);
+  pa.counter = &sm->counter[1];
+  const int g_num = ds->sm_count * std::max(P->per_num, 1);
   launch_numeric(P->heavy_sums, P->wide, g_num, pa, s);
+  count_launch(2);
   SPWS_CUDA(cudaGetLastError());
-  return launch_light<true>(pa, P->sm->tier, &P->sm->counter[5], P->kc, ds->sm_count, 1, 0, s);
+  return launch_light<true>(pa, sm->tier, &sm->counter[5], P->kc, ds->sm_count, 1, 0, s);
+}
+
+const int* rowwise_plan_abort(const RowwisePlan* plan) {
+  const RowwisePlanImpl* P = static_cast<const RowwisePlanImpl*>(plan->impl);
+  return P->empty ? nullptr : &P->sm->abort;
+}
+
+const long long* rowwise_plan_pos64(const RowwisePlan* plan) {
+  const RowwisePlanImpl* P = static_cast<const RowwisePlanImpl*>(plan->impl);
+  return P->empty ? nullptr : P->pos64;
 }
 
 const int* rowwise_plan_err(const RowwisePlan* plan) {
@@ -1522,7 +1610,8 @@ constexpr int64_t kNoAllocMaxRows = int64_t(1) << 18;  // rows of A the array is
 constexpr size_t kNoAllocHead = 1024;                   // counters, flags, totals
 constexpr size_t kNoAllocTiles = (size_t)((kNoAllocMaxRows + 2047) / 2048);
 constexpr size_t kNoAllocBytes = kNoAllocHead + sizeof(RowInfo) * kNoAllocMaxRows +
-                                 2 * sizeof(int32_t) * kNoAllocMaxRows + sizeof(long long) * kNoAllocTiles;
+                                 2 * sizeof(int32_t) * kNoAllocMaxRows + sizeof(long long) * kNoAllocTiles +
+                                 sizeof(long long) * (kNoAllocMaxRows + 1);
 
 struct NoAllocHead {
   int hist[kBuckets];
@@ -1538,7 +1627,7 @@ struct NoAllocHead {
 };
 static_assert(sizeof(NoAllocHead) <= kNoAllocHead, "head block too small");
 
-// The scratch itself: about 6 MiB, held by every device that loads the
+// The scratch itself: about 8 MiB, held by every device that loads the
 // library until the process exits. Host code must not use this name as an
 // address; it gets the device address from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
@@ -1600,6 +1689,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   int32_t* order = reinterpret_cast<int32_t*>(info + kNoAllocMaxRows);
   int32_t* rowcnt = order + kNoAllocMaxRows;
   long long* tiles = reinterpret_cast<long long*>(rowcnt + kNoAllocMaxRows);
+  long long* pos64 = tiles + kNoAllocTiles;  // C's row positions as int64, for the numeric kernels
 
   const cudaStream_t s = cudaStreamPerThread;
   const int32_t nA = A->nrows;
@@ -1620,7 +1710,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   SPWS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 
   k_row_info<<<(unsigned)((nA + 7) / 8), 256, 0, s>>>(nA, A->pos, A->crd, B->pos, B->crd, info, hd->hist,
-                                                      &hd->products, &hd->err);
+                                                      &hd->products, &hd->err, nullptr);
   k_order_offsets<<<1, 32, 0, s>>>(hd->hist, hd->cursor, &hd->nwork, &hd->nheavy, kLightBucket, hd->tier);
   k_order_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(nA, info, hd->cursor, order);
   count_launch(3);
@@ -1649,7 +1739,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
   count_launch(1);
   SPWS_CUDA(cudaGetLastError());
   SPWS_TRY(launch_light<false>(pa, hd->tier, &hd->counter[2], kc, sms, 1, 0, s));
-  SPWS_TRY(scan_counts_i32_into(rowcnt, C_pos, nA, &hd->nnz, tiles, s));
+  SPWS_TRY(scan_positions(rowcnt, C_pos, pos64, nA, &hd->nnz, tiles, s));
 
   long long nnz = 0;
   int err = 0;
@@ -1670,7 +1760,7 @@ extern "C" int spws_spgemm_csr_noalloc(const spws_csr_dev* A, const spws_csr_dev
     return SPWS_ERR_CAPACITY;
   }
   pa.counter = &hd->counter[1];
-  pa.Cp = C_pos;
+  pa.Cp = pos64;
   pa.Ck = C_crd;
   pa.Cv = C_vals;
   launch_numeric(0, false, sms * std::max(per_num, 1), pa, s);

@@ -84,6 +84,10 @@ struct SpgemmOpts {
   // Per A row, an amount subtracted from every column written for that row
   // (the batched form writes each instance's own columns); nullptr: none.
   const int32_t* col_shift = nullptr;
+  // C's positions only as int64 (rowwise_plan_pos64): the output may exceed
+  // INT32_MAX entries (the batched form's pooled output) and C->pos is not
+  // allocated.
+  bool wide_positions = false;
 };
 
 // Device CSR view used by the kernels (pointers on the device).
@@ -133,12 +137,22 @@ int rowwise_plan_symbolic(const CsrView& A, const CsrView& B, spws_csr_dev* C, c
                           RowwisePlan* plan, cudaStream_t s);
 int rowwise_plan_numeric(RowwisePlan* plan, spws_csr_dev* C, spws_spgemm_stats* stats);
 void rowwise_plan_free(RowwisePlan* plan);
-// After rowwise_plan_numeric: launch the numeric kernels again on `s` into the
-// same C arrays (new values, same structure). Allocates nothing and does not
-// synchronise, so it can be captured in a CUDA graph; 2 kernels.
-int rowwise_plan_launch_numeric(RowwisePlan* plan, cudaStream_t s);
+// After rowwise_plan_numeric: launch the whole pipeline again on `s` (row
+// analysis, ordering, symbolic pass, scan, numeric pass) into the plan's
+// buffers and the same C arrays, from the operands' current contents.
+// Allocates nothing and does not synchronise, so it can be captured in a CUDA
+// graph. If the operands now need more bitmap store or output entries than
+// the plan was made with, a device check sets the plan's abort flag
+// (rowwise_plan_abort) and the kernels after it do nothing.
+// `invalid` (nullable): a device flag, set when the operands failed their
+// checks; then every kernel returns at once and the abort flag is raised.
+int rowwise_plan_launch_full(RowwisePlan* plan, cudaStream_t s, const int* invalid = nullptr);
 // Device flag the numeric kernels set on an inconsistency (nullptr: empty plan).
 const int* rowwise_plan_err(const RowwisePlan* plan);
+// Device flag set when a relaunch outgrew the plan (nullptr: empty plan).
+const int* rowwise_plan_abort(const RowwisePlan* plan);
+// C's row positions as int64 on the device (nrows + 1; nullptr: empty plan).
+const long long* rowwise_plan_pos64(const RowwisePlan* plan);
 // Scratch bound of a plan before its bitmaps (bytes), for admission.
 size_t rowwise_scratch_bytes(int32_t nrows);
 
@@ -185,8 +199,10 @@ void batch_replay_free(BatchReplay* r);
 // the total also returned through `total_dev` (int64, device) so callers can
 // detect overflow of int32 positions.
 int scan_counts_i32(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev, cudaStream_t s);
-// The same scan with its per-tile sums in caller-provided scratch (ceil(n/2048) entries).
-int scan_counts_i32_into(const int32_t* counts, int32_t* out, int64_t n, long long* total_dev,
-                         long long* tile_scratch, cudaStream_t s);
+// Exclusive scan of n counts into n + 1 positions, written as int32 into out
+// and/or as int64 into out64 (either may be null); *total_dev gets the sum.
+// tile_scratch (ceil(n / 2048) entries, or null to allocate) holds the tile sums.
+int scan_positions(const int32_t* counts, int32_t* out, long long* out64, int64_t n, long long* total_dev,
+                   long long* tile_scratch, cudaStream_t s);
 
 }  // namespace spws

@@ -13,4 +13,9 @@ int validate_csr_device(const int32_t* pos, const int32_t* crd, int32_t nrows, i
 // calling thread's page-locked staging buffer, so that nothing is allocated.
 int validate_csr_device_flag(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz,
                              const char* what, int* bad, cudaStream_t s, bool staged = true);
+// The device checks alone (positions monotone within [0, nnz], columns in
+// range and strictly increasing): sets *bad on a violation, no host read, so
+// it can run inside a captured graph.
+void validate_csr_launch(const int32_t* pos, const int32_t* crd, int32_t nrows, int32_t ncols, int64_t nnz, int* bad,
+                         cudaStream_t s);
 }  // namespace spws

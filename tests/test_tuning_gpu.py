@@ -98,3 +98,68 @@ def test_batch_plan_replay_new_values(spws_lib):
             assert_csr_equal_structure(got, ref, f"replay {rnd} inst {i}")
             assert_csr_close(got, ref, oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2], f"replay {rnd} inst {i}")
     plan.release()
+
+
+def _cudart():
+    """The CUDA runtime the library is linked with, for writing into its device arrays."""
+    import ctypes
+    import glob
+    import os
+    for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            pass
+    for p in glob.glob(os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64", "libcudart.so*")):
+        return ctypes.CDLL(p)
+    pytest.skip("CUDA runtime not found")
+
+
+def _write_device(rt, dst, arr):
+    import ctypes
+    arr = np.ascontiguousarray(arr)
+    assert rt.cudaMemcpy(ctypes.c_void_p(dst), arr.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(arr.nbytes),
+                         1) == 0  # host to device
+
+
+def test_batch_plan_replay_guards_structure(spws_lib):
+    """The plan's graph re-solves from the instances' current arrays. A valid
+    but different structure either still fits the views (then the result is
+    that structure's product) or is refused with SPWS_ERR_CAPACITY; an
+    out-of-range column is caught on the device before any kernel follows it,
+    and the library stays usable."""
+    import ctypes
+    import sparsews_gb300 as sp
+    rt = _cudart()
+    insts = [gen.poisson_rows(n, 6.0, seed=500 + n) for n in (300, 700, 1500)]
+    dev = [sp.DeviceCsr.upload(*A) for A in insts]
+    plan = sp.BatchPlan(dev, dev)
+    # a new structure for instance 1 with the same row lengths
+    A = insts[1]
+    rng = np.random.default_rng(9)
+    crd = np.concatenate([np.sort(rng.choice(A[3], A[0][r + 1] - A[0][r], replace=False))
+                          for r in range(A[3])]).astype(np.int32)
+    _write_device(rt, dev[1].m.crd, crd)
+    new = (A[0], crd, A[2], A[3], A[4])
+    try:
+        plan.execute()
+        got = plan.download(1)
+        assert_csr_close(got, oracle.spgemm("taco", new, new), oracle.spgemm("taco", abs_csr(new), abs_csr(new))[2],
+                         "replay with a new structure that fits")
+    except sp.SpwsError as e:
+        assert e.status == 4
+    # an out-of-range column
+    bad = crd.copy()
+    bad[0] = 1 << 30
+    _write_device(rt, dev[1].m.crd, bad)
+    with pytest.raises(sp.SpwsError) as e:
+        plan.execute()
+    assert e.value.status == 4
+    plan.release()
+    # still usable
+    ok = gen.poisson_rows(400, 5.0, seed=77)
+    d2 = sp.DeviceCsr.upload(*ok)
+    b = sp.spgemm_batched([d2], [d2])
+    assert_csr_close(b.download(0), oracle.spgemm("taco", ok, ok), oracle.spgemm("taco", abs_csr(ok), abs_csr(ok))[2],
+                     "after a refused replay")
+    b.release()
