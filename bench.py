@@ -536,17 +536,83 @@ def bench_spws(args, ws, rank, local, dist):
         line["cpu_baseline"] = cpu
     if parity is not None:
         line["parity"] = parity
+    if ws == 1 and not args.no_forms:
+        dA.release()  # the other forms' operands take the device next
+        line["forms"] = forms_summary(args)
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ the other forms, summarised
+def forms_summary(args):
+    """Bounded runs of the batched, served and tensor workloads for the
+    default line (about two minutes): each summary keeps its metric, the
+    one-at-a-time comparisons and its clocks; the full runs are
+    --workload batched / served / mttkrp / ttm."""
+    import copy
+    out = {}
+    t0 = time.perf_counter()
+    a = copy.copy(args)
+    a.instances, a.wave_gb, a.steps, a.warmup, a.plain_sample, a.no_cpu = 1024, 0.0, 2, 1, 64, True
+    b = run_batched(a, tune=False)
+    out["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "gflops", "graph_replay", "one_at_a_time",
+                                        "clocks")}
+    out["batched"]["instances"] = b["config"]["instances"]
+    a = copy.copy(args)
+    a.served_requests, a.served_rates, a.warmup, a.no_cpu, a.plain_sample = 200, [0.5], 1, True, 16
+    sv = run_served_bench(a)
+    half = [r for r in sv["runs"] if r["rate"] != "saturating"][0]
+    out["served"] = {"value": sv["value"], "unit": sv["unit"], "requests": sv["config"]["requests_per_run"],
+                     "p50_ms_at_0.5x": half["p50_ms"], "p99_ms_at_0.5x": half["p99_ms"],
+                     "small_p99_ms_at_0.5x": half["small"]["p99_ms"], "one_at_a_time": sv["one_at_a_time"],
+                     "clocks": sv["clocks"]}
+    for w in ("mttkrp", "ttm"):
+        a = copy.copy(args)
+        a.workload, a.steps, a.warmup, a.e2e_steps, a.rank = w, 5, 2, 1, 32
+        a.cpu_tensor_nnz = 1_000_000 if w == "mttkrp" else 100_000
+        t = run_tensor(a)
+        out[w] = {k: t.get(k) for k in ("value", "unit", "ms_per_step", "device_ms_per_step", "roofline", "e2e",
+                                        "cpu_baseline", "clocks")}
+        out[w]["rank"] = 32
+    out["seconds"] = time.perf_counter() - t0
+    return out
 
 
 # ------------------------------------------------------------------ batched form
 def batch_workload(count, seed=42):
-    """The batched config (sparsews_gb300.gen.batch_instances)."""
+    """The batched config (sparsews_gb300.gen.batch_instances), generated by
+    spawned worker processes (seeded per instance: the same instances)."""
     from sparsews_gb300 import gen
-    return gen.batch_instances(count, seed)
+    return gen.batch_instances(count, seed, workers=min(16, os.cpu_count() or 1))
+
+
+def batch_waves(insts, wave_bytes):
+    """Consecutive groups of instances whose outputs, bounded by 12 bytes per
+    scalar product (an upper bound of the output entries), each fit
+    wave_bytes: the batch is solved wave by wave so that no more than one
+    wave's output is resident (0: one wave)."""
+    if wave_bytes <= 0:
+        return [list(range(len(insts)))]
+    waves, cur, acc = [], [], 0
+    for t, A in enumerate(insts):
+        b = 12 * int(np.diff(A[0]).astype(np.int64)[A[1]].sum())
+        if cur and acc + b > wave_bytes:
+            waves.append(cur)
+            cur, acc = [], 0
+        cur.append(t)
+        acc += b
+    if cur:
+        waves.append(cur)
+    return waves
 
 
 def run_batched(args, insts=None, tune=True):
+    """The batched config: args.instances products solved as output-bounded
+    waves (args.wave_gb of output each at most, from a products bound), each
+    wave one batched call (one row-wise pipeline over every instance of the
+    wave), timed per step over all waves; then each wave again through its
+    plan's captured CUDA graph of the whole solve; against one-at-a-time
+    device calls over every instance and one-at-a-time TACO-ABI calls on a
+    sample. The output of a wave is released before the next wave runs."""
     import sparsews_gb300 as sp
     from sparsews_gb300 import build, taco
     build.build()
@@ -555,78 +621,104 @@ def run_batched(args, insts=None, tune=True):
     t0 = time.perf_counter()
     insts = insts if insts is not None else batch_workload(args.instances)
     gen_s = time.perf_counter() - t0
+    n = len(insts)
     dev = [sp.DeviceCsr.upload(*A) for A in insts]
+    waves = batch_waves(insts, int(args.wave_gb * 1e9))
+
+    def solve_all(tuning=None):
+        st_all = []
+        for w in waves:
+            b = sp.spgemm_batched([dev[i] for i in w], [dev[i] for i in w], tuning=tuning)
+            st_all.append(b.stats)
+            b.release()
+        return st_all
+
     for _ in range(args.warmup):
-        sp.spgemm_batched(dev, dev).release()
+        solve_all()
     walls, stats = [], None
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
             t0 = time.perf_counter()
-            b = sp.spgemm_batched(dev, dev)
+            stats = solve_all()
             walls.append(time.perf_counter() - t0)
-            stats = b.stats
-            b.release()
     wall = sum(walls) / len(walls)
-    # autotuned (on a sample of the batch), then the same timed loop
-    t0 = time.perf_counter()
-    tuning, _ = sp.autotune_batched(dev, dev, sample=0)
-    tune_s = time.perf_counter() - t0
-    twalls = []
-    for it in range(args.warmup + args.steps):
-        sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+    products = sum(x.products for x in stats)
+    nnz = sum(x.nnz for x in stats)
+    ms_kernels = sum(x.ms_kernels for x in stats)
+    tuned = None
+    if tune:  # autotuned on a sample of the first wave, then the same timed loop
         t0 = time.perf_counter()
-        b = sp.spgemm_batched(dev, dev, tuning=tuning)
-        if it >= args.warmup:
+        w0 = waves[0]
+        tuning, _ = sp.autotune_batched([dev[i] for i in w0], [dev[i] for i in w0], sample=min(256, len(w0)))
+        tune_s = time.perf_counter() - t0
+        for _ in range(args.warmup):
+            solve_all(tuning)
+        twalls = []
+        for _ in range(args.steps):
+            sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+            t0 = time.perf_counter()
+            solve_all(tuning)
             twalls.append(time.perf_counter() - t0)
-        b.release()
-    twall = sum(twalls) / len(twalls)
-    # re-solve with new values through a batch plan (captured numeric graph)
-    plan = sp.BatchPlan(dev, dev, tuning)
-    for _ in range(args.warmup):
-        plan.execute()
-    rwalls = []
-    for _ in range(args.steps):
-        sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
-        t0 = time.perf_counter()
-        plan.execute()
-        rwalls.append(time.perf_counter() - t0)
-    plan.release()
-    rwall = sum(rwalls) / len(rwalls)
+        twall = sum(twalls) / len(twalls)
+        tuned = {"tuning": {"light_max": tuning.light_max, "long_min": tuning.long_min,
+                            "wide_windows": tuning.wide_windows, "heavy_sums": tuning.heavy_sums},
+                 "solves_per_s": n / twall, "ms_per_step": twall * 1e3, "tuning_s": tune_s}
+    # the whole solve replayed from each wave's plan (one graph launch per wave;
+    # the plan is made, replayed and released wave by wave)
+    gms, gwalls = [], []
+    for w in waves:
+        plan = sp.BatchPlan([dev[i] for i in w], [dev[i] for i in w])
+        for _ in range(args.warmup):
+            plan.execute()
+        best = []
+        for _ in range(args.steps):
+            sp.check(L.spws_flush_l2(L2_FLUSH_BYTES))
+            t0 = time.perf_counter()
+            best.append(plan.execute())
+            gwalls.append(time.perf_counter() - t0)
+        gms.append(sum(best) / len(best))
+        plan.release()
+    gwall = sum(gwalls) / args.steps
     # one-at-a-time through the same device-resident entry point, and through
-    # the reference-compatible TACO entry point with host arrays
+    # the reference-compatible TACO entry point with host arrays (a sample)
     t0 = time.perf_counter()
     for d in dev:
         c, _ = sp.spgemm_device(d, d)
         c.release()
     seq_dev = time.perf_counter() - t0
-    nplain = min(len(insts), args.plain_sample)
+    nplain = min(n, args.plain_sample)
+    pick = np.random.default_rng(3).choice(n, nplain, replace=False)
     t0 = time.perf_counter()
-    for A in insts[:nplain]:
+    for t in pick:
+        A = insts[t]
         At = taco.csr(*A)
         Ct = taco.init_dc(A[3], A[4])
         sp.check(L.spws_csr_csr_hash_compute(Ct.ptr(), At.ptr(), At.ptr(), 0))
         taco.take_csr(Ct, A[3], L.spws_free)
-    seq_abi = (time.perf_counter() - t0) / nplain * len(insts)
-    n = len(insts)
+    seq_abi = (time.perf_counter() - t0) / nplain * n
     line = {"metric": "batched_spgemm_solves_per_s", "value": n / wall, "unit": "solves/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": "batched_spgemm_AixAi", "instances": n, "n_range": [256, 65536],
-                       "row_nnz": "Poisson(8)", "mix": "even uniform, odd R-MAT", "groups": stats.groups,
+                       "row_nnz": "Poisson(8)", "mix": "even uniform, odd R-MAT", "waves": len(waves),
+                       "wave_output_bound_gb": args.wave_gb,
                        "l2": "flushed between timed steps"},
-            "gflops": 2.0 * stats.products / wall / 1e9, "products": int(stats.products), "nnz_C": int(stats.nnz),
-            "device_ms_kernels": stats.ms_kernels,
-            "autotuned": {"tuning": {"light_max": tuning.light_max, "long_min": tuning.long_min,
-                                     "wide_windows": tuning.wide_windows},
-                          "solves_per_s": n / twall, "ms_per_step": twall * 1e3, "tuning_s": tune_s},
-            "replay_new_values": {"what": "numeric re-solve of the same batch structure with new values, "
-                                          "one CUDA graph launch (symbolic pass reused)",
-                                  "solves_per_s": n / rwall, "ms_per_step": rwall * 1e3},
+            "gflops": 2.0 * products / wall / 1e9, "products": int(products), "nnz_C": int(nnz),
+            "device_ms_kernels": ms_kernels,
+            "graph_replay": {"what": "the whole solve (operand assembly, row analysis, symbolic pass, scan, "
+                                     "numeric pass, per-instance split) replayed from each wave's plan, one "
+                                     "CUDA graph launch per wave",
+                             "solves_per_s": n / gwall, "ms_per_step": gwall * 1e3, "device_ms": sum(gms),
+                             "speedup_vs_device_entry": seq_dev / gwall},
             "one_at_a_time": {"device_entry_solves_per_s": n / seq_dev,
                               "taco_abi_solves_per_s": n / seq_abi, "taco_abi_sample": nplain,
                               "speedup_vs_device_entry": seq_dev / wall, "speedup_vs_taco_abi": seq_abi / wall},
             "clocks": clk.summary(), "generation_s": gen_s}
+    if tuned is not None:
+        line["autotuned"] = tuned
+    for d in dev:
+        d.release()
     if not args.no_cpu:
         threads = os.cpu_count() or 1
         k, prods, secs = cpu_instances(insts, threads, args.cpu_batch_products)
@@ -992,7 +1084,18 @@ def bench_profile_case(args):
     print(json.dumps(out), flush=True)
 
 
-def bench_tensor(args):
+_TENSOR_CACHE = {}
+
+
+def tensor_config():
+    """The tensor config's COO (generated once per process)."""
+    from sparsews_gb300 import gen
+    if "t" not in _TENSOR_CACHE:
+        _TENSOR_CACHE["t"] = gen.tensor3(TENSOR["dims"], TENSOR["nnz"], zipf_s=TENSOR["zipf_s"], seed=TENSOR["seed"])
+    return _TENSOR_CACHE["t"]
+
+
+def run_tensor(args):
     """The tensor config: a 50,000 x 40,000 x 20,000 COO tensor with 20M
     nonzeros (mode-1 slices Zipf s=1.1, other modes uniform, values U(0,1]),
     seeded synthetic. mttkrp: A(i,j) = sum B(k,l,i) C(k,j) D(l,j) on mode 1
@@ -1007,7 +1110,7 @@ def bench_tensor(args):
     sp.check(L.spws_set_device(0))
     t0 = time.perf_counter()
     d0, d1, d2 = TENSOR["dims"]
-    i0, i1, i2, tv = gen.tensor3(TENSOR["dims"], TENSOR["nnz"], zipf_s=TENSOR["zipf_s"], seed=TENSOR["seed"])
+    i0, i1, i2, tv = tensor_config()
     R = args.rank
     if args.workload == "mttkrp":
         coo, dims = (i1, i2, i0, tv), (d1, d2, d0)
@@ -1122,7 +1225,11 @@ def bench_tensor(args):
             "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e, "generation_s": gen_s}
     if cpu is not None:
         line["cpu_baseline"] = cpu
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def bench_tensor(args):
+    print(json.dumps(run_tensor(args)), flush=True)
 
 
 def tensor_sample(coo, target_nnz, seed=7):
@@ -1244,7 +1351,7 @@ def latency_summary(done):
     return out
 
 
-def bench_served(args):
+def run_served_bench(args):
     import sparsews_gb300 as sp
     from sparsews_gb300 import build, served, taco
     build.build()
@@ -1345,7 +1452,11 @@ def bench_served(args):
             "clocks": clk.summary(), "generation_s": gen_s}
     if not args.no_cpu:
         line["cpu_baseline"] = served_cpu_baseline(small, big, tensors, factor)
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def bench_served(args):
+    print(json.dumps(run_served_bench(args)), flush=True)
 
 
 def served_cpu_baseline(small, big, tensors, factor):
@@ -1396,8 +1507,9 @@ def main():
                              "profile"])
     ap.add_argument("--case", default="coord", choices=["coord", "outer", "mttkrp", "ttm", "transpose", "batched"],
                     help="profile workload: the kernel family to run (small case for ncu)")
-    ap.add_argument("--instances", type=int, default=1024,
-                    help="batched workload: number of products (4096 holds ~220 GB of output at once)")
+    ap.add_argument("--instances", type=int, default=4096, help="batched workload: number of products")
+    ap.add_argument("--wave-gb", type=float, default=64.0,
+                    help="batched workload: output bound of one wave (GB; 4096 instances hold ~217 GB in all)")
     ap.add_argument("--plain-sample", type=int, default=512, help="batched workload: one-at-a-time ABI sample")
     ap.add_argument("--scale", type=int, default=None, help="R-MAT scale (default 18); smaller for profiling")
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -1405,6 +1517,8 @@ def main():
     ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
                     help="products per step of the reference arm (all cores)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="default workload: skip the batched / served / tensor summaries")
     ap.add_argument("--cpu-batch-products", type=int, default=300_000_000,
                     help="batched workload: products in the CPU-baseline sample (all host cores)")
     ap.add_argument("--transpose-cpu-products", type=int, default=30_000_000,

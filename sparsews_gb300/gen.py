@@ -174,16 +174,24 @@ def csr_transpose(pos, crd, vals, nrow, ncol):
     return np.cumsum(tpos).astype(np.int32), rows[order].astype(np.int32), np.asarray(vals)[order]
 
 
-def batch_instances(count, seed=42):
+def _batch_instance(args):
+    t, n, seed = args
+    if t % 2 == 0:
+        return poisson_rows(int(n), 8.0, seed=seed * 100003 + t)
+    return rmat_n(int(n), 8.0, seed=seed * 100003 + t)
+
+
+def batch_instances(count, seed=42, workers=1):
     """The batched config: n_i log-uniform in [256, 65536], Poisson(8)
     distinct columns per row; even instances uniform, odd ones R-MAT
-    (a, b, c = .57, .19, .19). Seeded per instance."""
+    (a, b, c = .57, .19, .19). Seeded per instance, so the result does not
+    depend on `workers` (> 1: generated by that many spawned processes)."""
     rng = np.random.default_rng(seed)
     ns = np.exp(rng.uniform(np.log(256), np.log(65536), count)).astype(np.int64)
-    out = []
-    for t, n in enumerate(ns):
-        if t % 2 == 0:
-            out.append(poisson_rows(int(n), 8.0, seed=seed * 100003 + t))
-        else:
-            out.append(rmat_n(int(n), 8.0, seed=seed * 100003 + t))
-    return out
+    jobs = [(t, int(n), seed) for t, n in enumerate(ns)]
+    if workers <= 1 or count < 64:
+        return [_batch_instance(j) for j in jobs]
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_batch_instance, jobs, chunksize=16))
