@@ -189,11 +189,16 @@ def run_cpu(A, rows, threads, kind):
     return time.perf_counter() - t0
 
 
+def row_products(A, B):
+    """Scalar products of each row of A*B (the sum of the B-row lengths its entries select)."""
+    pos = A[0].astype(np.int64)
+    cs = np.concatenate([[0], np.cumsum(np.diff(B[0].astype(np.int64))[A[1]])])
+    return cs[pos[1:]] - cs[pos[:-1]]
+
+
 def heaviest_rows(A, k):
     """The k rows of A with the most products (A times A)."""
-    pos = A[0].astype(np.int64)
-    cs = np.concatenate([[0], np.cumsum(np.diff(pos)[A[1]])])
-    rowp = cs[pos[1:]] - cs[pos[:-1]]
+    rowp = row_products(A, A)
     return np.sort(np.argsort(-rowp, kind="stable")[:k])
 
 
@@ -438,11 +443,19 @@ def bench_spws(args, ws, rank, local, dist):
     compulsory = 2 * (4 * (nA + 1) + 12 * len(A[1])) + 4 * (nA + 1) + 12 * nnzC  # A, B (= A), C
     fp64 = C.c_double(0.0)
     fp64_peak = fp64.value if L.spws_measure_fp64(C.byref(fp64)) == 0 and fp64.value > 0 else None
+    l2r = C.c_double(0.0)
+    l2_red = l2r.value if L.spws_measure_l2_red(C.byref(l2r)) == 0 and l2r.value > 0 else None
     peak, peak_src = measured_peaks()
     ceilings = {"hbm": alg_bytes / (peak * 1e9) * 1e3}
-    if fp64_peak:
-        ceilings["fp64_fma"] = 2.0 * products / (fp64_peak * 1e9) * 1e3
-        ceilings["fp64_mul_add"] = 4.0 * products / (fp64_peak * 1e9) * 1e3
+    # Rows below the light threshold (512 products) are summed in registers:
+    # a multiply and an add on the SM's FP64 pipe per product. The heavy rows'
+    # products are multiplied on the SM and added by the L2 (one reduction each).
+    rowp = row_products(A, A)
+    light = int(rowp[rowp < 512].sum())
+    if fp64_peak:  # the FP64 peak counts an FMA as two flops: instructions/s = peak / 2
+        ceilings["fp64_instructions"] = (products + light) / (fp64_peak / 2.0 * 1e9) * 1e3
+    if l2_red:
+        ceilings["l2_reductions"] = (products - light) / (l2_red * 1e9) * 1e3
     achieved = alg_bytes / (ms_num * 1e-3) / 1e9
     dev_flops = 2.0 * products / (ms_dev * 1e-3) / 1e9
 
@@ -506,7 +519,7 @@ def bench_spws(args, ws, rank, local, dist):
         "dtype": "f64",
         "data": "synthetic (seeded R-MAT generator, numpy PCG64 seed 42)",
         "config": {**cfg, "parallelism": f"replicas{ws}", "l2": "flushed between timed steps (512 MiB write)",
-                   "accumulate": "fp64 shared-memory atomics"},
+                   "accumulate": "fp64 reductions into C.vals in L2 (heavy rows), warp-private sums (light rows)"},
         "device_ms_per_step": ms_dev,
         "device_gflops": dev_flops,
         "phase_ms": {"symbolic": ms_sym, "numeric": ms_num,
@@ -517,10 +530,12 @@ def bench_spws(args, ws, rank, local, dist):
                      "frac": achieved / peak, "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "traffic": profiled_traffic(args.workload),
-                     # the ceiling is max(bytes / BW, flops / FP64 peak); which term binds. The FP64
-                     # peak counts an FMA as two flops; a product summed by an atomic add is a
-                     # multiply and an add, two FP64 instructions, so its floor is twice that.
+                     # the ceiling is the largest of bytes / HBM copy rate, FP64 instructions /
+                     # FP64 instruction rate and L2 reductions / L2 reduction rate (both rates
+                     # measured on this GPU by the library's probes); which term binds.
                      "fp64_peak_gflops": fp64_peak,
+                     "l2_red_gops": l2_red,
+                     "light_row_products": light,
                      "ceiling_ms": ceilings,
                      "binding": max(ceilings, key=lambda k: ceilings[k] or 0.0),
                      "frac_of_binding_ceiling": max(v or 0.0 for v in ceilings.values()) / ms_num,

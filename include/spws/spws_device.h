@@ -157,7 +157,7 @@ int spws_batch_release(spws_batch* batch);
  *                (a power of two in [32, 512]; default 512).
  *  long_min:     B-row slices at least this long are cut into 256-entry
  *                pieces, one warp each; shorter ones are packed into one
- *                lane-dense stream ([32, 256]; default 128).
+ *                lane-dense stream ([32, 256]; default 64).
  *  wide_windows: 1 = shared-memory windows of 18432 output ranks with one
  *                CTA per SM; 0 = windows of 5120 ranks with two CTAs per SM.
  *  heavy_sums:   how the 512-thread kernel sums a heavy row: 0 (default) =
@@ -233,6 +233,12 @@ int spws_flush_l2(size_t bytes);
  * every SM runs eight independent FMA chains per thread for about 10 ms. The
  * FP64 term of the roofline the benchmarks report. */
 int spws_measure_fp64(double* gflops);
+
+/* Rate of FP64 reductions (red.global.add.f64) into an L2-resident range, in
+ * G reductions/s: three 512-thread CTAs per SM, each adding at scattered
+ * offsets of its own 128 KB window (the numeric pass's pattern for heavy
+ * rows). The reduction term of the row-wise roofline. */
+int spws_measure_l2_red(double* gops);
 
 /* Page-lock / unlock a host range so copies to and from it run at DMA speed. */
 int spws_host_pin(void* p, size_t bytes);

@@ -111,6 +111,7 @@ def lib():
         "spws_inject_alloc_failure": ([C.c_longlong], None),
         "spws_flush_l2": ([C.c_size_t], C.c_int),
         "spws_measure_fp64": ([C.POINTER(C.c_double)], C.c_int),
+        "spws_measure_l2_red": ([C.POINTER(C.c_double)], C.c_int),
         "spws_host_pin": ([C.c_void_p, C.c_size_t], C.c_int),
         "spws_host_unpin": ([C.c_void_p], C.c_int),
         "spws_spgemm_batched": ([C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p),

@@ -268,10 +268,53 @@ __global__ void k_fp64_fma(int iters, double* sink) {
   if (s == -1.0) *sink = s;
 }
 
+// FP64 reductions into an L2-resident range, in the numeric pass's pattern:
+// each CTA adds into its own window of kRedWindow doubles (128 KB, the heavy
+// rows' window) at scattered offsets, one reduction per thread and step.
+constexpr int kRedWindow = 16384;
+__global__ void k_l2_red(int iters, double* win) {
+  double* w = win + (size_t)blockIdx.x * kRedWindow;
+  unsigned h = threadIdx.x * 2654435761u + blockIdx.x * 40503u;
+  for (int i = 0; i < iters; i++) {
+    h = h * 1664525u + 1013904223u;  // a linear congruential walk over the window
+    atomicAdd(w + (h >> 18), 1.0);     // top 14 bits: an offset below kRedWindow
+  }
+}
+static_assert(kRedWindow == 1 << 14, "the offset takes the top 14 bits of the walk");
+
 }  // namespace
 }  // namespace spws
 
 extern "C" {
+
+int spws_measure_l2_red(double* gops) {
+  if (!gops) return SPWS_ERR_INVALID;
+  spws::DeviceState* ds = nullptr;
+  SPWS_TRY(spws::device_state(&ds));
+  const int threads = 512, blocks = ds->sm_count * 3, iters = 2048;
+  double* win = nullptr;
+  const size_t bytes = sizeof(double) * spws::kRedWindow * (size_t)blocks;
+  SPWS_TRY(spws::dalloc((void**)&win, bytes, ds->stream));
+  SPWS_CUDA(cudaMemsetAsync(win, 0, bytes, ds->stream));
+  cudaEvent_t e0, e1;
+  SPWS_CUDA(cudaEventCreate(&e0));
+  SPWS_CUDA(cudaEventCreate(&e1));
+  float ms = 0.f;
+  for (int rep = 0; rep < 2; rep++) {  // the first run warms up clocks and the L2
+    SPWS_CUDA(cudaEventRecord(e0, ds->stream));
+    spws::k_l2_red<<<blocks, threads, 0, ds->stream>>>(iters, win);
+    spws::count_launch(1);
+    SPWS_CUDA(cudaEventRecord(e1, ds->stream));
+    SPWS_CUDA(cudaEventSynchronize(e1));
+    SPWS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  spws::dfree(win, ds->stream);
+  const double ops = (double)iters * threads * (double)blocks;
+  *gops = ms > 0.f ? ops / ((double)ms * 1e-3) / 1e9 : 0.0;
+  return SPWS_OK;
+}
 
 int spws_measure_fp64(double* gflops) {
   if (!gflops) return SPWS_ERR_INVALID;

@@ -5,9 +5,10 @@
 // format conversions (transposes).
 //
 // One pass per 8-bit digit: per-tile histograms (tile = 4096 items), a scan
-// of the histograms in digit-major order, and a scatter that ranks the items
-// of each 256-item round with warp ballots (a multisplit) so equal digits keep
-// their input order; passes are therefore stable and the sort is stable.
+// of the histograms in digit-major order, and a scatter in which each warp
+// ranks its own contiguous 512 items with warp ballots (a multisplit) so
+// equal digits keep their input order; passes are therefore stable and the
+// sort is stable.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -48,68 +49,52 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long
   hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Scatter of one tile: items are ranked round by round (a warp multisplit:
-// lanes holding the same digit found with one ballot per digit bit, then a
-// prefix over the warps), placed digit-sorted into shared memory at
-// tile-local positions (the tile's own digit histogram, scanned, gives each
-// digit's start), and written out from there in slot order, so consecutive
-// threads store consecutive addresses of the same digit's run instead of one
-// scattered 8-byte store per item. Ranks follow input order within a digit:
-// the pass is stable.
+// Scatter of one tile. Warp w owns the tile's items [512w, 512w + 512), in
+// input order, and ranks them 32 at a time (lanes holding the same digit
+// found with one ballot per digit bit) against its own per-digit counters,
+// with no CTA barrier; one prefix over the warps per digit then gives each
+// warp its slots within every digit's run of the tile. Items are placed
+// digit-sorted into shared memory and written out from there in slot order,
+// so consecutive threads store consecutive addresses of the same digit's run
+// instead of one scattered 8-byte store per item. Slots follow input order
+// within a digit: the pass is stable. Payloads are read only when the items
+// are placed, so a thread holds 16 keys and 16 ranks (two to a register) and
+// three CTAs fit an SM (75 KB of shared memory each).
+constexpr int kWarpItems = kTile / kSortWarps;  // 512
+constexpr int kWarpRounds = kWarpItems / 32;   // 16
 constexpr size_t kScatterSmem = 2 * sizeof(unsigned long long) * kTile;
 
-__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long* __restrict__ kin,
-                                                                const unsigned long long* __restrict__ vin,
-                                                                unsigned long long* __restrict__ kout,
-                                                                unsigned long long* __restrict__ vout, int64_t n,
-                                                                int shift, int64_t ntiles,
-                                                                const long long* __restrict__ offs,
-                                                                const int* __restrict__ hist) {
+__global__ void __launch_bounds__(kSortThreads, 3) k_radix_scatter(const unsigned long long* __restrict__ kin,
+                                                                   const unsigned long long* __restrict__ vin,
+                                                                   unsigned long long* __restrict__ kout,
+                                                                   unsigned long long* __restrict__ vout, int64_t n,
+                                                                   int shift, int64_t ntiles,
+                                                                   const long long* __restrict__ offs,
+                                                                   const int* __restrict__ hist) {
   extern __shared__ unsigned long long stage[];  // keys [kTile], then payloads [kTile]
-  __shared__ long long base[kBins];
-  __shared__ int lstart[kBins];
-  __shared__ int run[kBins];
-  __shared__ int wcnt[kSortWarps][kBins];
+  __shared__ long long dbase[kBins];             // digit d: output offset minus its tile-local start
+  __shared__ int wcnt[kSortWarps][kBins];        // per warp and digit: count, then first slot
   __shared__ int wsum[kSortWarps];
   unsigned long long* sk = stage;
   unsigned long long* sv = stage + kTile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t tile0 = (int64_t)blockIdx.x * kTile;
-  unsigned long long kr[kRounds], vr[kRounds];
+  const int64_t w0 = tile0 + (int64_t)warp * kWarpItems + lane;
+  unsigned long long kr[kWarpRounds];
 #pragma unroll
-  for (int r = 0; r < kRounds; r++) {
-    const int64_t idx = tile0 + (int64_t)r * kSortThreads + threadIdx.x;
+  for (int r = 0; r < kWarpRounds; r++) {
+    const int64_t idx = w0 + 32 * r;
     kr[r] = idx < n ? kin[idx] : 0ull;
-    vr[r] = idx < n ? vin[idx] : 0ull;
   }
-  base[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
-  {  // tile-local digit starts: exclusive scan of this tile's histogram
-    const int c = hist[(int64_t)threadIdx.x * ntiles + blockIdx.x];
-    int v = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += y;
-    }
-    if (lane == 31) wsum[warp] = v;
-    __syncthreads();
-    int before = 0;
-#pragma unroll
-    for (int w = 0; w < kSortWarps; w++)
-      if (w < warp) before += wsum[w];
-    lstart[threadIdx.x] = before + v - c;
-    run[threadIdx.x] = 0;
-  }
-#pragma unroll
-  for (int w = 0; w < kSortWarps; w++) wcnt[w][threadIdx.x] = 0;
-  __syncthreads();
+  for (int d = lane; d < kBins; d += 32) wcnt[warp][d] = 0;
+  __syncwarp();
   const unsigned lt = (1u << lane) - 1u;
+  // the item's rank among this warp's items of its digit (< 512), two per register
+  unsigned pos[kWarpRounds / 2];
 #pragma unroll
-  for (int r = 0; r < kRounds; r++) {
-    const int64_t idx = tile0 + (int64_t)r * kSortThreads + threadIdx.x;
-    const bool valid = idx < n;
+  for (int r = 0; r < kWarpRounds; r++) {
+    const bool valid = w0 + 32 * r < n;
     const int d = (int)((kr[r] >> shift) & (kBins - 1));
-    // lanes of this warp holding the same digit
     unsigned eq = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
     for (int b = 0; b < kRadixBits; b++) {
@@ -118,36 +103,54 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned l
       eq &= bit ? m : ~m;
     }
     const int rank = __popc(eq & lt);
-    if (valid && rank == 0) wcnt[warp][d] = __popc(eq);
-    __syncthreads();
-    int rtotal;
-    {  // thread t owns digit t: prefix over warps
-      int acc = 0;
-#pragma unroll
-      for (int w = 0; w < kSortWarps; w++) {
-        const int c = wcnt[w][threadIdx.x];
-        wcnt[w][threadIdx.x] = acc;
-        acc += c;
-      }
-      rtotal = acc;
-    }
-    __syncthreads();
-    if (valid) {
-      const int slot = lstart[d] + run[d] + wcnt[warp][d] + rank;
-      sk[slot] = kr[r];
-      sv[slot] = vr[r];
-    }
-    __syncthreads();
-    run[threadIdx.x] += rtotal;
-#pragma unroll
-    for (int w = 0; w < kSortWarps; w++) wcnt[w][threadIdx.x] = 0;
-    __syncthreads();
+    const int before = valid ? wcnt[warp][d] : 0;
+    __syncwarp();  // every lane of the digit has read its counter
+    if (valid && rank == 0) wcnt[warp][d] = before + __popc(eq);
+    __syncwarp();
+    const unsigned pr = (unsigned)(before + rank);
+    pos[r / 2] = (r & 1) ? (pos[r / 2] | (pr << 16)) : pr;
   }
+  {  // thread t owns digit t: its tile-local start, then each warp's first slot
+    const int c = hist[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+    int v = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    if (lane == 31) wsum[warp] = v;
+    __syncthreads();  // also publishes every warp's counters
+    int before = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++)
+      if (w < warp) before += wsum[w];
+    const int lstart = before + v - c;
+    dbase[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x] - lstart;
+    int acc = lstart;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++) {
+      const int x = wcnt[w][threadIdx.x];
+      wcnt[w][threadIdx.x] = acc;
+      acc += x;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kWarpRounds; r++) {
+    const int64_t idx = w0 + 32 * r;
+    if (idx < n) {
+      const int d = (int)((kr[r] >> shift) & (kBins - 1));
+      const int slot = wcnt[warp][d] + (int)((pos[r / 2] >> (16 * (r & 1))) & 0xffffu);
+      sk[slot] = kr[r];
+      sv[slot] = vin[idx];
+    }
+  }
+  __syncthreads();
   const int count = (int)(n - tile0 < kTile ? n - tile0 : kTile);
   for (int j = threadIdx.x; j < count; j += kSortThreads) {
     const unsigned long long k = sk[j];
     const int d = (int)((k >> shift) & (kBins - 1));
-    const long long p = base[d] + (j - lstart[d]);
+    const long long p = dbase[d] + j;
     kout[p] = k;
     vout[p] = sv[j];
   }

@@ -232,7 +232,7 @@ __device__ __forceinline__ int claim_or_yield(int* counter, const PassArgs& a, u
 }
 
 constexpr int kPieceLen = 256;   // B entries per warp work piece of a long slice
-constexpr int kLongMin = 128;    // default: slices this long are cut into pieces; shorter ones are packed
+constexpr int kLongMin = 64;     // default: slices this long are cut into pieces; shorter ones are packed
 constexpr int kLongMinMax = 256; // packed stream length < 512 * 256 fits the 17-bit field of fill_batch
 constexpr int kL2RankMax = 16384; // default PassArgs::l2_rank_max: 128 KB of C.vals per CTA in L2
 static_assert(kL2RankMax < 65536, "L2-pass ranks are taken from the 16-bit word prefixes");
@@ -565,6 +565,7 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
   int32_t* bnd = reinterpret_cast<int32_t*>(reinterpret_cast<unsigned char*>(&b) + sizeof(Batch));  // kBoundInts
   __shared__ uint32_t gbase[kGroups];
   __shared__ int wsum[kWarps];
+  __shared__ int stepcnt[kSpanWords / 128];  // set bits per walk step (32 groups of 4 words)
   __shared__ int s_idx;
   __shared__ int32_t s_cols[2];
   __shared__ int32_t s_wcol[kMaxWin + 1];
@@ -593,10 +594,30 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
       const int nw = words_in(wl, ri.hi);
       const int nq = (nw + 3) >> 2;
       uint4* bm4 = reinterpret_cast<uint4*>(bm);
-      if (a.bmstore && !multi) {  // the symbolic pass left this row's bitmap
+      // The walk below goes through the span in steps of 32 16-byte groups
+      // of words (one group per lane), step s taken by warp s mod kWarps:
+      // interleaved, so every warp gets about the same number of set bits
+      // even where the row's columns crowd into part of its span (R-MAT rows
+      // hold a third of their columns in the span's first sixteenth).
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      const int nsteps = (nq + 31) >> 5;  // <= 64
+      const bool stored = a.bmstore && !multi;
+      if (stored) {  // the symbolic pass left this row's bitmap
+        // each warp loads its own steps and counts their bits on the way
         const uint4* src = reinterpret_cast<const uint4*>(a.bmstore + a.bmoff[i]);
 #pragma unroll 4
-        for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = src[w];
+        for (int st = warp; st < nsteps; st += kWarps) {
+          const int g = st * 32 + lane;
+          int c = 0;
+          if (g < nq) {
+            const uint4 v = src[g];
+            bm4[g] = v;
+            c = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+          if (lane == 0) stepcnt[st] = c;
+        }
         __syncthreads();
         if (next < nwork) {  // one 128-byte line per thread and step
           const int32_t ni = a.order[next];
@@ -612,36 +633,53 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
         for (int w = threadIdx.x; w < nq; w += kThreads) bm4[w] = make_uint4(0u, 0u, 0u, 0u);
         __syncthreads();
         build_bitmap(a, q0, q1, wlo, multi, bm, b, wsum);
+        for (int st = warp; st < nsteps; st += kWarps) {
+          const int g = st * 32 + lane;
+          int c = 0;
+          if (g < nq) {
+            const uint4 v = bm4[g];
+            c = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+          if (lane == 0) stepcnt[st] = c;
+        }
+        __syncthreads();
       }
 
-      // Per-word prefix of set bits and the row's columns in order. Warp w
-      // owns a contiguous chunk of 16-byte groups of words and walks it 32
-      // groups at a time, one group (four words) per lane: one warp scan per
-      // 128 words, and the lanes' C.crd stores are contiguous across the warp.
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      const int chunk = (nq + kWarps - 1) / kWarps;
-      const int c0 = min(nq, warp * chunk), c1 = min(nq, c0 + chunk);
-      int wc = 0;
-      for (int g = c0 + lane; g < c1; g += 32) {
-        const uint4 v = bm4[g];
-        wc += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
-      }
+      // Every warp scans the step counts itself (two per lane; read before
+      // the walk's closing barrier, written again only after it): step s
+      // starts at rank sbase(s), the span holds nnz_w columns.
+      const int sc0 = lane < nsteps ? stepcnt[lane] : 0;
+      const int sc1 = lane + 32 < nsteps ? stepcnt[lane + 32] : 0;
+      int si0 = sc0, si1 = sc1;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) wc += __shfl_xor_sync(0xffffffffu, wc, o);
-      int nnz_w;
-      int run = block_excl_scan(lane == 0 ? wc : 0, wsum, &nnz_w);  // prefix of warp totals
-      run = __shfl_sync(0xffffffffu, run, 0);
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y0 = __shfl_up_sync(0xffffffffu, si0, o);
+        const int y1 = __shfl_up_sync(0xffffffffu, si1, o);
+        if (lane >= o) {
+          si0 += y0;
+          si1 += y1;
+        }
+      }
+      const int half0 = __shfl_sync(0xffffffffu, si0, 31);
+      const int nnz_w = half0 + __shfl_sync(0xffffffffu, si1, 31);
+      const int se0 = si0 - sc0, se1 = half0 + si1 - sc1;  // exclusive starts of steps lane, lane + 32
       if (out + nnz_w > row_end) {  // never write past the row the symbolic pass sized (uniform)
         if (threadIdx.x == 0) atomicExch(a.err, 1);
         break;
       }
-      // The same walk stores each word's prefix and writes its columns, in
-      // order, at their ranks. Words past nw inside the last group are zero.
+      // The walk stores each word's prefix of set bits and writes the row's
+      // columns, in order, at their ranks: one warp scan per step of 128
+      // words, and the lanes' C.crd stores are contiguous across the warp.
+      // Words past nw inside the last group are zero.
       // the warp's staging area: the batch and bound table, idle during the walk
       int32_t* stage = reinterpret_cast<int32_t*>(&b) + warp * kStageInts;
-      for (int gb = c0; gb < c1; gb += 32) {
-        const int g = gb + lane;
-        const uint4 v = g < c1 ? bm4[g] : make_uint4(0u, 0u, 0u, 0u);
+      for (int st = warp; st < nsteps; st += kWarps) {
+        const int g = st * 32 + lane;
+        const int e0 = __shfl_sync(0xffffffffu, se0, st & 31), e1 = __shfl_sync(0xffffffffu, se1, st & 31);
+        const int run = st < 32 ? e0 : e1;  // the step's first rank
+        const uint4 v = g < nq ? bm4[g] : make_uint4(0u, 0u, 0u, 0u);
         const uint32_t words[4] = {v.x, v.y, v.z, v.w};
         const int tot = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
         int incl = tot;
@@ -657,7 +695,7 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
         // staging area first (when they fit), so that the stores to C.crd
         // are made by consecutive lanes at consecutive addresses.
         const bool staged = step_total <= kStageInts;  // warp-uniform
-        if (g < c1) {
+        if (g < nq) {
           if (((4 * g) & (kGroupWords - 1)) == 0) gbase[(4 * g) / kGroupWords] = (uint32_t)r;
           const int p1 = r + __popc(v.x), p2 = p1 + __popc(v.y), p3 = p2 + __popc(v.z);
           // the four 16-bit prefixes in one 8-byte store (4g is a multiple of 4)
@@ -682,7 +720,6 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
           for (int t = lane; t < step_total; t += 32) a.Ck[out + run + t] = stage[t];
           __syncwarp();
         }
-        run += step_total;
       }
       __syncthreads();
       // prefix of word w: the group's 32-bit base plus the 16-bit difference

@@ -74,7 +74,7 @@ struct SpgemmOpts {
   long long yield_ns = 0;
   // Tunables (the autotuner picks them per workload):
   int light_max = 512;        // rows with fewer products go to the warp-per-row kernel (power of two <= 512)
-  int long_min = 128;         // B-row slices this long are cut into pieces, shorter ones packed (<= 256)
+  int long_min = 64;          // B-row slices this long are cut into pieces, shorter ones packed (<= 256)
   bool wide_windows = false;  // numeric windows of 18432 ranks at 1 CTA/SM instead of 5120 at 2 CTAs/SM
   // Heavy rows' sums: 0 = FP64 reductions straight into C.vals (in L2), in
   // windows of 16384 output ranks for larger rows, three CTAs per SM; 1 =

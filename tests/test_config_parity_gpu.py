@@ -5,7 +5,8 @@
 * Banded 2^20 x 2^20, half-bandwidth 8, 50% fill: the whole product.
 * R-MAT 2^18, 16 edge draws a row (the timed product: 2.94e9 products, 1.28e9
   output nonzeros, C.pos near 2^30): random rows and the heaviest rows of the
-  device result against the oracle on the same rows.
+  device result against the oracle on the same rows, and every entry against
+  the coordinate workspace (the reference's summation order).
 * The 20M-nonzero Zipf tensor: MTTKRP (rank 32) on sampled output rows and
   TTM (rank 32) on sampled whole slices of the device result, against the
   oracle run on exactly the entries those outputs depend on.
@@ -20,7 +21,7 @@ import numpy as np
 import pytest
 
 import oracle
-from _check import abs_csr, assert_csr_close, assert_vals_close
+from _check import abs_csr, assert_csr_close, assert_csr_equal_structure, assert_vals_close
 from sparsews_gb300 import gen
 
 pytestmark = pytest.mark.gpu
@@ -78,6 +79,35 @@ def test_rmat18_config_sampled_and_heaviest_rows(spws_lib):
     ref = oracle.spgemm("hash", sub, A, w_cap=oracle.w_cap_default(len(A[1])))
     scale = oracle.spgemm("taco", abs_csr(sub), abs_csr(A))[2]
     assert_csr_close(got, ref, scale, "R-MAT 2^18 rows")
+
+
+def test_rmat18_config_every_entry_against_coordinate_workspace(spws_lib):
+    """Every entry of the timed product. The coordinate workspace sums each
+    entry's products in the reference's visiting order (bit-exact with the
+    oracle at every size the oracle runs), so it stands in for the oracle at
+    1.28e9 entries: the row-wise result must have its structure exactly and
+    its values within the tolerance, with S taken from |A|*|A| on the device
+    (same structure; no cancellation, so its rounding is far below RTOL)."""
+    import sparsews_gb300 as sp
+    A = gen.rmat(18, 16, seed=42)
+    dA = sp.DeviceCsr.upload(*A)
+    dAbs = sp.DeviceCsr.upload(*abs_csr(A))
+    dC, st = sp.spgemm_device(dA, dA)
+    dK, stk = sp.spgemm_device(dA, dA, accum_mode=1)
+    dS, _ = sp.spgemm_device(dAbs, dAbs)
+    dA.release()
+    dAbs.release()
+    assert st.nnz == stk.nnz == 1282240902
+    n = A[3]
+    step = 1 << 15
+    for r0 in range(0, n, step):
+        rows = np.arange(r0, min(n, r0 + step), dtype=np.int32)
+        got, ref, scale = dC.download_rows(rows), dK.download_rows(rows), dS.download_rows(rows)
+        what = f"R-MAT 2^18 rows {r0}..{rows[-1]}"
+        assert_csr_equal_structure(scale, ref, what + " (|A|*|A|)")
+        assert_csr_close(got, ref, scale[2], what)
+    for d in (dC, dK, dS):
+        d.release()
 
 
 @functools.lru_cache(maxsize=1)
