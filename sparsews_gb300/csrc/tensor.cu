@@ -32,6 +32,7 @@ namespace spws {
 namespace {
 
 constexpr int kPiece = 2048;  // leaves per warp work item
+constexpr int kLeafBatch = 4; // leaves whose factor rows a warp loads at once (full factors)
 constexpr int kJpl = 8;       // output columns per lane per pass (256 per warp)
 constexpr int kTileR = 32 * kJpl;
 
@@ -268,7 +269,43 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
   unsigned started = 0;
 #pragma unroll
   for (int u = 0; u < JPL; u++) acc[u] = 0.0;
-  for (long long qb = q0; qb < q1; qb += LW) {
+  // Factors with every entry present (direct output): no presence words to
+  // test, and the factor rows of kLeafBatch leaves are loaded before any is
+  // summed, so a warp waits on the L2 once per kLeafBatch leaves.
+  const bool full = JPL == 1 && direct.o0 != nullptr;
+  for (long long qb = q0; full && qb < q1; qb += LW) {
+    const long long q = qb + lane;
+    int32_t a0 = 0, a1 = 0;
+    double b = 0.0;
+    if (q < q1) {
+      a0 = r0[q];
+      if (MODE == 0) a1 = r1[q];
+      b = bv[q];
+    }
+    const int nb = (int)min((long long)LW, q1 - qb);
+    const int j = j0 + lane;
+    const bool in = j < R;
+    for (int t0 = 0; t0 < nb; t0 += kLeafBatch) {
+      double bb[kLeafBatch], d0[kLeafBatch], d1[kLeafBatch];
+#pragma unroll
+      for (int k = 0; k < kLeafBatch; k++) {
+        const int t = min(t0 + k, nb - 1);  // past the end: a repeat, loaded but not summed
+        const int32_t x0 = __shfl_sync(gm, a0, t, LW);
+        const int32_t x1 = MODE == 0 ? __shfl_sync(gm, a1, t, LW) : 0;
+        bb[k] = __shfl_sync(gm, b, t, LW);
+        d0[k] = in ? F0.dense[(int64_t)x0 * F0.R + j] : 0.0;
+        d1[k] = (MODE == 0 && in) ? F1.dense[(int64_t)x1 * F1.R + j] : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kLeafBatch; k++) {
+        if (t0 + k < nb) {
+          acc[0] = leaf_update<MODE, FMA>(acc[0], started & 1u, bb[k], d0[k], d1[k]);
+          started = 1u;
+        }
+      }
+    }
+  }
+  for (long long qb = q0; !full && qb < q1; qb += LW) {
     const long long q = qb + lane;
     int32_t a0 = -1, a1 = -1;
     double b = 0.0;
@@ -415,7 +452,41 @@ __global__ void k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const 
     cp++;
     ce = __shfl_sync(0xffffffffu, my_start, min(cp + 1, np));
   };
-  for (long long qb = L0; qb < L1; qb += 32) {
+  // Factors with every entry present (direct output): no presence words, and
+  // the factor rows of kLeafBatch leaves are loaded before any is summed.
+  const bool full = direct.o0 != nullptr;
+  for (long long qb = L0; full && qb < L1; qb += 32) {
+    const long long q = qb + lane;
+    int32_t a0 = 0, a1 = 0;
+    double b = 0.0;
+    if (q < L1) {
+      a0 = r0[q];
+      if (MODE == 0) a1 = r1[q];
+      b = bv[q];
+    }
+    const int nb = (int)min(32LL, L1 - qb);
+    for (int t0 = 0; t0 < nb; t0 += kLeafBatch) {
+      double bb[kLeafBatch], d0[kLeafBatch], d1[kLeafBatch];
+#pragma unroll
+      for (int k = 0; k < kLeafBatch; k++) {
+        const int t = min(t0 + k, nb - 1);  // past the end: a repeat, loaded but not summed
+        const int32_t x0 = __shfl_sync(0xffffffffu, a0, t);
+        const int32_t x1 = MODE == 0 ? __shfl_sync(0xffffffffu, a1, t) : 0;
+        bb[k] = __shfl_sync(0xffffffffu, b, t);
+        d0[k] = in ? F0.dense[(int64_t)x0 * F0.R + j] : 0.0;
+        d1[k] = (MODE == 0 && in) ? F1.dense[(int64_t)x1 * F1.R + j] : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kLeafBatch; k++) {
+        if (t0 + k < nb) {
+          while (qb + t0 + k >= ce) flush();  // the leaf starts the next piece
+          acc = leaf_update<MODE, FMA>(acc, started, bb[k], d0[k], d1[k]);
+          started = true;
+        }
+      }
+    }
+  }
+  for (long long qb = L0; !full && qb < L1; qb += 32) {
     const long long q = qb + lane;
     int32_t a0 = -1, a1 = -1;
     double b = 0.0;
@@ -448,6 +519,8 @@ __global__ void k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const 
   (void)mw;
 }
 
+constexpr int kCombineBatch = 16;  // pieces whose partials k_combine loads at once
+
 // Warp per segment: add the pieces' partials in piece order into the
 // segment's running values for this column tile (first present value
 // assigns, later ones add), and accumulate the presence mask.
@@ -466,16 +539,30 @@ __global__ void k_combine(int64_t nseg, int mode, const long long* __restrict__ 
   while (todo) {
     const int64_t s = base + (__ffs(todo) - 1);
     todo &= todo - 1u;
+    const long long p0 = poff[s], p1 = poff[s + 1];
     for (int u = 0; u < kJpl; u++) {
       const int j = j0 + lane + 32 * u;
       double v = 0.0;
       bool have = false;
-      for (long long pc = poff[s]; u < pw && pc < poff[s + 1]; pc++) {
-        const uint32_t m = pmask[pc * pw + u];
-        if ((m >> lane) & 1u) {
-          const double x = partial[pc * (int64_t)(32 * pw) + (j - j0)];
-          v = have ? __dadd_rn(v, x) : x;
-          have = true;
+      // kCombineBatch pieces' words and partials are loaded before any is
+      // added (every load is inside the partial and mask arrays), so a bucket
+      // of a thousand pieces waits on memory a few dozen times, not a
+      // thousand
+      for (long long pb = p0; u < pw && pb < p1; pb += kCombineBatch) {
+        uint32_t m[kCombineBatch];
+        double x[kCombineBatch];
+#pragma unroll
+        for (int k = 0; k < kCombineBatch; k++) {
+          const long long pc = pb + k;
+          m[k] = pc < p1 ? pmask[pc * pw + u] : 0u;
+          x[k] = pc < p1 ? partial[pc * (int64_t)(32 * pw) + (j - j0)] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < kCombineBatch; k++) {
+          if ((m[k] >> lane) & 1u) {
+            v = have ? __dadd_rn(v, x[k]) : x[k];
+            have = true;
+          }
         }
       }
       if (direct.o0) {
