@@ -156,6 +156,35 @@ __global__ void k_starts(int64_t n, const int32_t* __restrict__ head, const long
   if (head[p]) starts[hpos[p]] = p;
 }
 
+// first[v] (v <= nkeys): the first position of the sorted keys whose bucket
+// bits are at least v, by binary search.
+__global__ void k_key_first(int32_t nkeys, int64_t n, const unsigned long long* __restrict__ keys,
+                            unsigned long long mask, long long* __restrict__ first) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v > nkeys) return;
+  long long lo = 0, hi = n;
+  while (lo < hi) {
+    const long long m = (lo + hi) >> 1;
+    if ((long long)(keys[m] & mask) < v) lo = m + 1; else hi = m;
+  }
+  first[v] = lo;
+}
+
+// head[v] = 1 when bucket value v holds leaves.
+__global__ void k_key_heads(int32_t nkeys, const long long* __restrict__ first, int32_t* __restrict__ head) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nkeys) return;
+  head[v] = first[v + 1] > first[v] ? 1 : 0;
+}
+
+// starts[rank of v among the nonempty values] = first[v].
+__global__ void k_key_starts(int64_t nkeys, const int32_t* __restrict__ head, const long long* __restrict__ hpos,
+                             const long long* __restrict__ first, long long* __restrict__ starts) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nkeys) return;
+  if (head[v]) starts[hpos[v]] = first[v];
+}
+
 __global__ void k_piece_counts(int64_t nseg, const long long* __restrict__ starts, int32_t* __restrict__ pc) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
@@ -520,6 +549,24 @@ __global__ void k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const 
 }
 
 constexpr int kCombineBatch = 16;  // pieces whose partials k_combine loads at once
+constexpr int kBigSeg = 64;        // split buckets of more pieces are combined by k_combine_big
+
+// Writes a split bucket's combined value for column j0 + lane + 32u (called
+// by a whole warp): straight into the COO with direct output, else into the
+// segment values and, from lane 0, the column tile's presence word.
+__device__ __forceinline__ void combine_write(const DirectOut& direct, int mode, int64_t s, int32_t R, int32_t j0,
+                                              int u, int32_t mw, int32_t pw, double v, bool have,
+                                              double* __restrict__ segval, uint32_t* __restrict__ segmask) {
+  const int lane = threadIdx.x & 31;
+  const int j = j0 + lane + 32 * u;
+  if (direct.o0) {
+    if (j < R && u < pw) direct_write(direct, mode, s, R, j, v);
+    return;
+  }
+  if (j < R) segval[s * (int64_t)R + j] = v;
+  const unsigned m = __ballot_sync(0xffffffffu, have && j < R);
+  if (lane == 0 && (j0 / 32 + u) < mw) segmask[s * (int64_t)mw + j0 / 32 + u] = m;
+}
 
 // Warp per segment: add the pieces' partials in piece order into the
 // segment's running values for this column tile (first present value
@@ -534,7 +581,8 @@ __global__ void k_combine(int64_t nseg, int mode, const long long* __restrict__ 
   const int lane = threadIdx.x & 31;
   const int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
   const int64_t mine = base + lane;
-  const bool split = mine < nseg && poff[mine + 1] - poff[mine] > 1;
+  const long long np = mine < nseg ? poff[mine + 1] - poff[mine] : 0;
+  const bool split = np > 1 && np <= kBigSeg;  // larger ones: k_combine_big
   unsigned todo = __ballot_sync(0xffffffffu, split);
   while (todo) {
     const int64_t s = base + (__ffs(todo) - 1);
@@ -565,13 +613,66 @@ __global__ void k_combine(int64_t nseg, int mode, const long long* __restrict__ 
           }
         }
       }
-      if (direct.o0) {
-        if (j < R && u < pw) direct_write(direct, mode, s, R, j, v);
-        continue;
+      combine_write(direct, mode, s, R, j0, u, mw, pw, v, have, segval, segmask);
+    }
+  }
+}
+
+// Split buckets of more than kBigSeg pieces (Zipf-heavy buckets: thousands
+// of pieces), a CTA each: warp w sums the w-th eighth of the pieces in
+// order (loads batched as in k_combine), and warp 0 adds the eight partial
+// sums in warp order.
+__global__ void __launch_bounds__(256, 4) k_combine_big(int64_t nseg, int mode, const long long* __restrict__ poff,
+                                                     const double* __restrict__ partial,
+                                                     const uint32_t* __restrict__ pmask, int32_t R, int32_t j0,
+                                                     int32_t mw, int32_t pw, double* __restrict__ segval,
+                                                     uint32_t* __restrict__ segmask, DirectOut direct) {
+  __shared__ double sv[8][32];
+  __shared__ unsigned sh[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t s = blockIdx.x; s < nseg; s += gridDim.x) {
+    const long long p0 = poff[s], p1 = poff[s + 1];
+    if (p1 - p0 <= kBigSeg) continue;  // CTA-uniform
+    const long long per = (p1 - p0 + 7) / 8;
+    const long long a0 = min(p1, p0 + warp * per), a1 = min(p1, a0 + per);
+#pragma unroll 1
+    for (int u = 0; u < pw && u < kJpl; u++) {
+      const int j = j0 + lane + 32 * u;
+      double v = 0.0;
+      bool have = false;
+      for (long long pb = a0; pb < a1; pb += kCombineBatch) {
+        uint32_t m[kCombineBatch];
+        double x[kCombineBatch];
+#pragma unroll
+        for (int k = 0; k < kCombineBatch; k++) {
+          const long long pc = pb + k;
+          m[k] = pc < a1 ? pmask[pc * pw + u] : 0u;
+          x[k] = pc < a1 ? partial[pc * (int64_t)(32 * pw) + (j - j0)] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < kCombineBatch; k++) {
+          if ((m[k] >> lane) & 1u) {
+            v = have ? __dadd_rn(v, x[k]) : x[k];
+            have = true;
+          }
+        }
       }
-      if (j < R) segval[s * (int64_t)R + j] = v;
-      const unsigned m = __ballot_sync(0xffffffffu, have && j < R);
-      if (lane == 0 && (j0 / 32 + u) < mw) segmask[s * (int64_t)mw + j0 / 32 + u] = m;
+      sv[warp][lane] = v;
+      const unsigned hm = __ballot_sync(0xffffffffu, have);
+      if (lane == 0) sh[warp] = hm;
+      __syncthreads();
+      if (warp == 0) {
+        double t = 0.0;
+        bool h = false;
+        for (int w = 0; w < 8; w++) {
+          if ((sh[w] >> lane) & 1u) {
+            t = h ? __dadd_rn(t, sv[w][lane]) : sv[w][lane];
+            h = true;
+          }
+        }
+        combine_write(direct, mode, s, R, j0, u, mw, pw, t, h, segval, segmask);
+      }
+      __syncthreads();
     }
   }
 }
@@ -736,21 +837,40 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
   SPWS_TRY(alloc(r0, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
   SPWS_TRY(alloc(r1, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
   SPWS_TRY(alloc(bv, sizeof(double) * (size_t)std::max<int64_t>(nnz, 1), s));
-  SPWS_TRY(alloc(head, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1), s));
-  SPWS_TRY(alloc(hpos, sizeof(long long) * (size_t)std::max<int64_t>(nnz, 1), s));
+  // Bucket bounds. MTTKRP's bucket key is the leaf coordinate, below d2:
+  // when there are fewer key values than leaves, each value's first position
+  // is found by binary search in the sorted keys and the nonempty buckets
+  // are compacted (work and memory over d2, not over the leaves); otherwise
+  // (TTM's pairs) a head flag per leaf is scanned.
+  const bool by_value = mode == 0 && (int64_t)B.d2 < nnz;
+  const int64_t nh = by_value ? (int64_t)B.d2 : nnz;  // head flags
+  DevArr first;
+  SPWS_TRY(alloc(head, sizeof(int32_t) * (size_t)std::max<int64_t>(nh, 1), s));
+  SPWS_TRY(alloc(hpos, sizeof(long long) * (size_t)std::max<int64_t>(nh, 1), s));
   SPWS_TRY(alloc(starts, sizeof(long long) * ((size_t)nnz + 1), s));
+  if (by_value) SPWS_TRY(alloc(first, sizeof(long long) * ((size_t)B.d2 + 1), s));
   if (nnz > 0) {
     if (packed)
       k_unpack<<<gn, 256, 0, s>>>(nnz, mode, sk, perm, r1_bits, r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>());
     else
       k_gather<<<gn, 256, 0, s>>>(nnz, mode, perm, leaf_fib.as<int32_t>(), fib_root.as<int32_t>(), B.crd1, B.vals,
                                   r0.as<int32_t>(), r1.as<int32_t>(), bv.as<double>());
-    k_heads<<<gn, 256, 0, s>>>(nnz, sk, kmask, head.as<int32_t>());
-    count_launch(2);
+    if (by_value) {
+      const unsigned gk = (unsigned)((B.d2 + 1 + 255) / 256);
+      k_key_first<<<gk, 256, 0, s>>>(B.d2, nnz, sk, kmask, first.as<long long>());
+      k_key_heads<<<gk, 256, 0, s>>>(B.d2, first.as<long long>(), head.as<int32_t>());
+    } else {
+      k_heads<<<gn, 256, 0, s>>>(nnz, sk, kmask, head.as<int32_t>());
+    }
+    count_launch(by_value ? 3 : 2);
   }
-  SPWS_TRY(scan_i32_to_i64(head.as<int32_t>(), hpos.as<long long>(), nnz, tot.as<long long>(), s));
+  SPWS_TRY(scan_i32_to_i64(head.as<int32_t>(), hpos.as<long long>(), nh, tot.as<long long>(), s));
   if (nnz > 0) {
-    k_starts<<<gn, 256, 0, s>>>(nnz, head.as<int32_t>(), hpos.as<long long>(), starts.as<long long>());
+    if (by_value)
+      k_key_starts<<<(unsigned)((nh + 255) / 256), 256, 0, s>>>(nh, head.as<int32_t>(), hpos.as<long long>(),
+                                                               first.as<long long>(), starts.as<long long>());
+    else
+      k_starts<<<gn, 256, 0, s>>>(nnz, head.as<int32_t>(), hpos.as<long long>(), starts.as<long long>());
     count_launch(1);
   }
   // Do the factors hold every column of every row the tensor can reach?
@@ -817,6 +937,9 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
     SPWS_TRY(alloc(segval, sizeof(double) * (size_t)std::max<long long>(nseg, 1) * std::max(R, 1), s));
     SPWS_TRY(alloc(segmask, sizeof(uint32_t) * (size_t)std::max<long long>(nseg, 1) * mw, s));
   }
+  DeviceState* ds = nullptr;
+  SPWS_TRY(device_state(&ds));
+  const int sms = ds->sm_count;
   Factor f0{F0.dense, F0.mask, F0.rows, F0.R, F0.mw};
   Factor f1 = F1 ? Factor{F1->dense, F1->mask, F1->rows, F1->R, F1->mw} : f0;
   for (int32_t j0 = 0; j0 < R; j0 += kTileR) {
@@ -868,6 +991,14 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
       k_combine<<<(unsigned)((nseg + 255) / 256), 256, 0, s>>>(nseg, mode, poff.as<long long>(), partial.as<double>(),
                                                            pmask.as<uint32_t>(), R, j0, mw, pw, segval.as<double>(),
                                                            segmask.as<uint32_t>(), direct);
+      // a bucket of more than kBigSeg pieces makes npieces >= nseg + kBigSeg
+      // (every bucket has at least one piece)
+      if (npieces >= nseg + kBigSeg) {
+        k_combine_big<<<(unsigned)std::max(sms, 1) * 4, 256, 0, s>>>(
+            nseg, mode, poff.as<long long>(), partial.as<double>(), pmask.as<uint32_t>(), R, j0, mw, pw,
+            segval.as<double>(), segmask.as<uint32_t>(), direct);
+        count_launch(1);
+      }
       count_launch(2);
     }
   }

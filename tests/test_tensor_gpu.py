@@ -82,6 +82,24 @@ def test_mttkrp_against_oracle(spws_lib, R):
     assert_vals_close(gv, rv, scale, "mttkrp")
 
 
+def test_mttkrp_heavy_buckets_against_oracle(spws_lib):
+    """Zipf-heavy output rows: the heaviest bucket has more than 64 pieces of
+    2048 leaves (its partial sums combined by a whole CTA), the next ones
+    between 2 and 64 (combined by one warp each), the rest one piece."""
+    import sparsews_gb300 as sp
+    i0, i1, i2, tv = gen.tensor3((600, 2000, 1000), 400000, zipf_s=1.6, seed=91)
+    counts = np.sort(np.bincount(i0))[::-1]
+    assert counts[0] > 64 * 2048 and 2048 < counts[1] <= 64 * 2048
+    dims = (2000, 1000, 600)
+    Cf, Df = gen.dense_factor(2000, 32, seed=92), gen.dense_factor(1000, 32, seed=93)
+    Bc = (i1, i2, i0, tv)
+    (gi, gj), gv = sp.mttkrp(Bc, dims, Cf, Df)
+    (ri, rj), rv = oracle.mttkrp("hash", Bc, dims, Cf, Df, w_cap=BIG)
+    assert np.array_equal(gi, ri) and np.array_equal(gj, rj)
+    (_, _), scale = oracle.mttkrp("hash", (i1, i2, i0, np.abs(tv)), dims, abs_f(Cf), abs_f(Df), w_cap=BIG)
+    assert_vals_close(gv, rv, scale, "mttkrp, heavy buckets")
+
+
 def test_mttkrp_sparse_factors(spws_lib):
     """Factors with missing entries: products exist only where C(k,j) and
     D(l,j) both exist (the reference's co-iteration, hash_free.h:300-323)."""
