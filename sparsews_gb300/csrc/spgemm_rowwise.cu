@@ -503,6 +503,17 @@ __device__ __forceinline__ int claim(int* counter, int* s_idx, const PassArgs& a
   return *s_idx;
 }
 
+// The numeric pass claims its heavy rows interleaved from kOrderWays equal
+// parts of the cost order (claim c takes part c mod kOrderWays), so the CTAs
+// in flight hold a mix of the largest rows, whose C.vals ranges compete for
+// the L2, and smaller ones, instead of only the largest at first. A
+// bijection on [0, n): the last n mod kOrderWays claims take the last rows.
+constexpr int kOrderWays = 4;
+__device__ __forceinline__ int interleaved(int c, int n) {
+  const int m = n / kOrderWays;
+  return c < kOrderWays * m ? (c % kOrderWays) * m + c / kOrderWays : c;
+}
+
 __device__ __forceinline__ int words_in(long long wl, int32_t hi) {
   return (int)min((long long)kSpanWords, ((long long)hi - wl + 1 + 31) >> 5);
 }
@@ -581,7 +592,7 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
   for (;;) {
     const int idx = next;
     if (idx >= nwork) break;
-    const int32_t i = a.order[idx];
+    const int32_t i = a.order[interleaved(idx, nwork)];
     const RowInfo ri = a.info[i];
     const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
     const bool multi = (long long)ri.hi - ri.lo + 1 > kSpanBits;
@@ -620,7 +631,7 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
         }
         __syncthreads();
         if (next < nwork) {  // one 128-byte line per thread and step
-          const int32_t ni = a.order[next];
+          const int32_t ni = a.order[interleaved(next, nwork)];
           const RowInfo nr = a.info[ni];
           if ((long long)nr.hi - nr.lo + 1 <= kSpanBits) {
             const uint32_t* nsrc = a.bmstore + a.bmoff[ni];

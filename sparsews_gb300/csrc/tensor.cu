@@ -419,7 +419,7 @@ __global__ void k_pieces(int64_t npieces, const int32_t* __restrict__ pseg, cons
 // order as k_pieces; the bucket set-up that dominated a two-leaf piece is
 // paid once per G pieces.
 template <int MODE, bool FMA = false>
-__global__ void k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const int32_t* __restrict__ pseg,
+__global__ void __launch_bounds__(256, 4) k_pieces_grouped(int64_t npieces, int G, int64_t nleaves, const int32_t* __restrict__ pseg,
                                  const long long* __restrict__ pstart, const long long* __restrict__ starts,
                                  const int32_t* __restrict__ r0, const int32_t* __restrict__ r1,
                                  const double* __restrict__ bv, Factor F0, Factor F1, int32_t R, int32_t mw,
