@@ -508,7 +508,7 @@ __device__ __forceinline__ int claim(int* counter, int* s_idx, const PassArgs& a
 // in flight hold a mix of the largest rows, whose C.vals ranges compete for
 // the L2, and smaller ones, instead of only the largest at first. A
 // bijection on [0, n): the last n mod kOrderWays claims take the last rows.
-constexpr int kOrderWays = 4;
+constexpr int kOrderWays = 8;
 __device__ __forceinline__ int interleaved(int c, int n) {
   const int m = n / kOrderWays;
   return c < kOrderWays * m ? (c % kOrderWays) * m + c / kOrderWays : c;
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_symbolic(PassArgs a) {
       int c = 0;
       for (int w = threadIdx.x; w < nq; w += kThreads) {
         const uint4 v = bm4[w];
-        if (dst) dst[w] = v;
+        if (dst) __stcs(dst + w, v);  // read once, by the numeric pass: streamed past the L2's working set
         c += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
       }
       int t;
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(kThreads, L2W ? 3 : (ACC <= kAcc ? 2 : 1)) k_n
           const int g = st * 32 + lane;
           int c = 0;
           if (g < nq) {
-            const uint4 v = src[g];
+            const uint4 v = __ldcs(src + g);  // read once
             bm4[g] = v;
             c = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
           }

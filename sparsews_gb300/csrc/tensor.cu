@@ -960,7 +960,7 @@ int tensor_bucket(int mode, const Csf3Dev& B, const FactorDense& F0, const Facto
       };
       const bool grouped = direct_out && jpl <= 1 && npieces > 0 && nnz <= 8 * npieces;
       auto launch_grouped = [&](auto kernel) {  // tiny buckets: G pieces per warp
-        constexpr int G = 8;
+        constexpr int G = 31;  // lane k holds piece k, lane G the group end: at most 31
         const int64_t warps = (npieces + G - 1) / G;
         const unsigned gg = (unsigned)((warps + 7) / 8);
         kernel<<<gg, 256, 0, s>>>(npieces, G, nnz, pseg.as<int32_t>(), pstart.as<long long>(), starts.as<long long>(),
