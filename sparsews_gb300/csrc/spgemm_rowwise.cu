@@ -503,7 +503,7 @@ __device__ __forceinline__ int claim(int* counter, int* s_idx, const PassArgs& a
   return *s_idx;
 }
 
-// The numeric pass claims its heavy rows interleaved from kOrderWays equal
+// The heavy-row passes claim their rows interleaved from kOrderWays equal
 // parts of the cost order (claim c takes part c mod kOrderWays), so the CTAs
 // in flight hold a mix of the largest rows, whose C.vals ranges compete for
 // the L2, and smaller ones, instead of only the largest at first. A
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_symbolic(PassArgs a) {
   for (;;) {
     const int idx = claim(a.counter, &s_idx, a, t0);
     if (idx >= nwork) break;
-    const int32_t i = a.order[idx];
+    const int32_t i = a.order[interleaved(idx, nwork)];
     const RowInfo ri = a.info[i];
     const int32_t q0 = a.Ap[i], q1 = a.Ap[i + 1];
     const bool multi = (long long)ri.hi - ri.lo + 1 > kSpanBits;
