@@ -162,12 +162,12 @@ int spws_batch_release(spws_batch* batch);
  *                CTA per SM; 0 = windows of 5120 ranks with two CTAs per SM.
  *  heavy_sums:   how the 512-thread kernel sums a heavy row: 0 (default) =
  *                FP64 reductions straight into C.vals, which the L2
- *                executes: rows of up to 16384 output entries in one pass,
- *                larger ones in windows of 16384 ranks (so the CTAs' live
+ *                executes: rows of up to 20480 output entries in one pass,
+ *                larger ones in windows of 20480 ranks (so the CTAs' live
  *                output ranges stay in L2), three CTAs per SM, wide_windows
  *                unused; 1 = shared-memory windows of output ranks, written
  *                out window by window; 2 = shared-memory windows, with rows
- *                of up to 16384 output entries summed in C.vals in one pass. */
+ *                of up to 20480 output entries summed in C.vals in one pass. */
 typedef struct spws_tuning {
   int32_t light_max;
   int32_t long_min;
@@ -236,7 +236,7 @@ int spws_measure_fp64(double* gflops);
 
 /* Rate of FP64 reductions (red.global.add.f64) into an L2-resident range, in
  * G reductions/s: three 512-thread CTAs per SM, each adding at scattered
- * offsets of its own 128 KB window (the numeric pass's pattern for heavy
+ * offsets of its own 160 KB window (the numeric pass's pattern for heavy
  * rows). The reduction term of the row-wise roofline. */
 int spws_measure_l2_red(double* gops);
 

@@ -269,18 +269,17 @@ __global__ void k_fp64_fma(int iters, double* sink) {
 }
 
 // FP64 reductions into an L2-resident range, in the numeric pass's pattern:
-// each CTA adds into its own window of kRedWindow doubles (128 KB, the heavy
+// each CTA adds into its own window of kRedWindow doubles (160 KB, the heavy
 // rows' window) at scattered offsets, one reduction per thread and step.
-constexpr int kRedWindow = 16384;
+constexpr int kRedWindow = 20480;
 __global__ void k_l2_red(int iters, double* win) {
   double* w = win + (size_t)blockIdx.x * kRedWindow;
   unsigned h = threadIdx.x * 2654435761u + blockIdx.x * 40503u;
   for (int i = 0; i < iters; i++) {
     h = h * 1664525u + 1013904223u;  // a linear congruential walk over the window
-    atomicAdd(w + (h >> 18), 1.0);     // top 14 bits: an offset below kRedWindow
+    atomicAdd(w + (int)(((unsigned long long)h * kRedWindow) >> 32), 1.0);  // an offset below kRedWindow
   }
 }
-static_assert(kRedWindow == 1 << 14, "the offset takes the top 14 bits of the walk");
 
 }  // namespace
 }  // namespace spws

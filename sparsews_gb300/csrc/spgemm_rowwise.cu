@@ -234,7 +234,7 @@ __device__ __forceinline__ int claim_or_yield(int* counter, const PassArgs& a, u
 constexpr int kPieceLen = 256;   // B entries per warp work piece of a long slice
 constexpr int kLongMin = 64;     // default: slices this long are cut into pieces; shorter ones are packed
 constexpr int kLongMinMax = 256; // packed stream length < 512 * 256 fits the 17-bit field of fill_batch
-constexpr int kL2RankMax = 16384; // default PassArgs::l2_rank_max: 128 KB of C.vals per CTA in L2
+constexpr int kL2RankMax = 20480; // default PassArgs::l2_rank_max: 160 KB of C.vals per CTA in L2
 static_assert(kL2RankMax < 65536, "L2-pass ranks are taken from the 16-bit word prefixes");
 static_assert(kThreads * (kLongMinMax - 1) < (1 << 17), "short slices (< long_min entries) fill at most 17 bits");
 constexpr int kChunkLen = 128;   // packed entries per warp work item (4 rounds of 32 lanes)

@@ -77,9 +77,9 @@ struct SpgemmOpts {
   int long_min = 64;          // B-row slices this long are cut into pieces, shorter ones packed (<= 256)
   bool wide_windows = false;  // numeric windows of 18432 ranks at 1 CTA/SM instead of 5120 at 2 CTAs/SM
   // Heavy rows' sums: 0 = FP64 reductions straight into C.vals (in L2), in
-  // windows of 16384 output ranks for larger rows, three CTAs per SM; 1 =
+  // windows of 20480 output ranks for larger rows, three CTAs per SM; 1 =
   // shared-memory rank windows (wide_windows picks their width); 2 = shared
-  // windows, with rows of at most 16384 outputs in C.vals in one pass.
+  // windows, with rows of at most 20480 outputs in C.vals in one pass.
   int heavy_sums = 0;
   // Per A row, an amount subtracted from every column written for that row
   // (the batched form writes each instance's own columns); nullptr: none.

@@ -41,7 +41,7 @@ def test_every_candidate_tuning_matches_oracle(spws_lib):
         C, st = sp.spgemm_device(d, d, tuning=sp.Tuning(lm, ln, w, h))
         got = C.download()
         C.release()
-        assert st.chunk_width == (16384 if h == 0 else (18432 if w else 5120))
+        assert st.chunk_width == (20480 if h == 0 else (18432 if w else 5120))
         assert_csr_equal_structure(got, ref, f"tuning {lm},{ln},{w},{h}")
         assert_csr_close(got, ref, scale, f"tuning {lm},{ln},{w},{h}")
 
