@@ -1527,7 +1527,7 @@ def main():
                     help="batched workload: output bound of one wave (GB; 4096 instances hold ~217 GB in all)")
     ap.add_argument("--plain-sample", type=int, default=512, help="batched workload: one-at-a-time ABI sample")
     ap.add_argument("--scale", type=int, default=None, help="R-MAT scale (default 18); smaller for profiling")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-products", type=int, default=60_000_000, help="products in the CPU-baseline sample")
     ap.add_argument("--cpu-step-products", type=int, default=100_000_000,
                     help="products per step of the reference arm (all cores)")
