@@ -30,8 +30,11 @@ static_assert(kBins == kSortThreads, "one bin per thread");
 // Both kernels load a thread's kRounds items of the tile up front (all loads
 // in flight at once) before any shared-memory work, so a CTA waits for DRAM
 // once per tile rather than once per round.
-__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long* __restrict__ keys, int64_t n,
-                                                             int shift, int64_t ntiles, int* __restrict__ hist) {
+// K: the key type (64-bit keys, or 32-bit ones where the key fits them: 4
+// bytes less per item to move).
+template <typename K>
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const K* __restrict__ keys, int64_t n, int shift,
+                                                             int64_t ntiles, int* __restrict__ hist) {
   __shared__ int h[kBins];
   h[threadIdx.x] = 0;
   const int64_t base = (int64_t)blockIdx.x * kTile + threadIdx.x;
@@ -62,29 +65,33 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long
 // three CTAs fit an SM (75 KB of shared memory each).
 constexpr int kWarpItems = kTile / kSortWarps;  // 512
 constexpr int kWarpRounds = kWarpItems / 32;   // 16
-constexpr size_t kScatterSmem = 2 * sizeof(unsigned long long) * kTile;
+template <typename K>
+constexpr size_t scatter_smem() {
+  return (sizeof(K) + sizeof(unsigned long long)) * kTile;
+}
 
-__global__ void __launch_bounds__(kSortThreads, 3) k_radix_scatter(const unsigned long long* __restrict__ kin,
+template <typename K>
+__global__ void __launch_bounds__(kSortThreads, 3) k_radix_scatter(const K* __restrict__ kin,
                                                                    const unsigned long long* __restrict__ vin,
-                                                                   unsigned long long* __restrict__ kout,
+                                                                   K* __restrict__ kout,
                                                                    unsigned long long* __restrict__ vout, int64_t n,
                                                                    int shift, int64_t ntiles,
                                                                    const long long* __restrict__ offs,
                                                                    const int* __restrict__ hist) {
-  extern __shared__ unsigned long long stage[];  // keys [kTile], then payloads [kTile]
-  __shared__ long long dbase[kBins];             // digit d: output offset minus its tile-local start
-  __shared__ int wcnt[kSortWarps][kBins];        // per warp and digit: count, then first slot
+  extern __shared__ __align__(16) unsigned char stage[];  // payloads [kTile], then keys [kTile]
+  __shared__ long long dbase[kBins];                      // digit d: output offset minus its tile-local start
+  __shared__ int wcnt[kSortWarps][kBins];                 // per warp and digit: count, then first slot
   __shared__ int wsum[kSortWarps];
-  unsigned long long* sk = stage;
-  unsigned long long* sv = stage + kTile;
+  unsigned long long* sv = reinterpret_cast<unsigned long long*>(stage);
+  K* sk = reinterpret_cast<K*>(stage + sizeof(unsigned long long) * kTile);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t tile0 = (int64_t)blockIdx.x * kTile;
   const int64_t w0 = tile0 + (int64_t)warp * kWarpItems + lane;
-  unsigned long long kr[kWarpRounds];
+  K kr[kWarpRounds];
 #pragma unroll
   for (int r = 0; r < kWarpRounds; r++) {
     const int64_t idx = w0 + 32 * r;
-    kr[r] = idx < n ? kin[idx] : 0ull;
+    kr[r] = idx < n ? kin[idx] : K(0);
   }
   for (int d = lane; d < kBins; d += 32) wcnt[warp][d] = 0;
   __syncwarp();
@@ -148,7 +155,7 @@ __global__ void __launch_bounds__(kSortThreads, 3) k_radix_scatter(const unsigne
   __syncthreads();
   const int count = (int)(n - tile0 < kTile ? n - tile0 : kTile);
   for (int j = threadIdx.x; j < count; j += kSortThreads) {
-    const unsigned long long k = sk[j];
+    const K k = sk[j];
     const int d = (int)((k >> shift) & (kBins - 1));
     const long long p = dbase[d] + j;
     kout[p] = k;
@@ -265,9 +272,11 @@ int scan_i64(const long long* in, long long* out, int64_t n, long long* total_de
   return scan64_impl<long long>(in, out, n, total_dev, nullptr, s);
 }
 
-int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigned long long* keys_tmp,
-                     unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s,
-                     int begin_bit) {
+namespace {
+
+template <typename K>
+int radix_sort_impl(K* keys, unsigned long long* vals, K* keys_tmp, unsigned long long* vals_tmp, int64_t n,
+                    int key_bits, bool* result_in_tmp, cudaStream_t s, int begin_bit) {
   *result_in_tmp = false;
   if (n <= 1 || key_bits <= begin_bit) return SPWS_OK;
   {  // the scatter's staging exceeds the default 48 KB: opt in once per device
@@ -277,8 +286,8 @@ int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigne
     SPWS_CUDA(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> g(mu);
     if (dev >= 0 && dev < 64 && !smem_set[dev]) {
-      SPWS_CUDA(cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kScatterSmem));
+      SPWS_CUDA(cudaFuncSetAttribute(k_radix_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)scatter_smem<K>()));
       smem_set[dev] = true;
     }
   }
@@ -287,12 +296,13 @@ int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigne
   long long* offs = nullptr;
   SPWS_TRY(dalloc((void**)&hist, sizeof(int) * kBins * ntiles, s));
   SPWS_TRY(dalloc((void**)&offs, sizeof(long long) * kBins * ntiles, s));
-  unsigned long long *ka = keys, *va = vals, *kb = keys_tmp, *vb = vals_tmp;
+  K *ka = keys, *kb = keys_tmp;
+  unsigned long long *va = vals, *vb = vals_tmp;
   for (int shift = begin_bit; shift < key_bits; shift += kRadixBits) {
-    k_radix_hist<<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, hist);
+    k_radix_hist<K><<<(unsigned)ntiles, kSortThreads, 0, s>>>(ka, n, shift, ntiles, hist);
     SPWS_TRY(scan_i32_to_i64(hist, offs, (int64_t)kBins * ntiles, nullptr, s));
-    k_radix_scatter<<<(unsigned)ntiles, kSortThreads, kScatterSmem, s>>>(ka, va, kb, vb, n, shift, ntiles, offs,
-                                                                           hist);
+    k_radix_scatter<K><<<(unsigned)ntiles, kSortThreads, scatter_smem<K>(), s>>>(ka, va, kb, vb, n, shift, ntiles,
+                                                                              offs, hist);
     count_launch(2);
     SPWS_CUDA(cudaGetLastError());
     std::swap(ka, kb);
@@ -302,6 +312,23 @@ int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigne
   dfree(hist, s);
   dfree(offs, s);
   return SPWS_OK;
+}
+
+}  // namespace
+
+int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigned long long* keys_tmp,
+                     unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s,
+                     int begin_bit) {
+  return radix_sort_impl(keys, vals, keys_tmp, vals_tmp, n, key_bits, result_in_tmp, s, begin_bit);
+}
+
+int radix_sort_pairs(uint32_t* keys, unsigned long long* vals, uint32_t* keys_tmp, unsigned long long* vals_tmp,
+                     int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s, int begin_bit) {
+  if (key_bits > 32) {
+    set_error("radix_sort_pairs: 32-bit keys hold at most 32 key bits");
+    return SPWS_ERR_INVALID;
+  }
+  return radix_sort_impl(keys, vals, keys_tmp, vals_tmp, n, key_bits, result_in_tmp, s, begin_bit);
 }
 
 }  // namespace spws

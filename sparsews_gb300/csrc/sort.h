@@ -16,4 +16,7 @@ int scan_i64(const long long* in, long long* out, int64_t n, long long* total_de
 int radix_sort_pairs(unsigned long long* keys, unsigned long long* vals, unsigned long long* keys_tmp,
                      unsigned long long* vals_tmp, int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s,
                      int begin_bit = 0);
+// The same with 32-bit keys (key_bits <= 32): 12 bytes an item instead of 16.
+int radix_sort_pairs(uint32_t* keys, unsigned long long* vals, uint32_t* keys_tmp, unsigned long long* vals_tmp,
+                     int64_t n, int key_bits, bool* result_in_tmp, cudaStream_t s, int begin_bit = 0);
 }  // namespace spws

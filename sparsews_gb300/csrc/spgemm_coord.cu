@@ -54,11 +54,12 @@ __global__ void k_entry_products(int64_t nnzA, const int32_t* __restrict__ Aj, c
 // the entries' products as one flat stream at the group's offset (eoff: each
 // entry's product offset over the whole matrix, base: the chunk's). The
 // stream is in (row, j, k) order, as the reference's loop visits it.
+template <typename K>
 __global__ void k_expand(int32_t r0, int32_t r1, int64_t q0, int64_t q1, const int32_t* __restrict__ Ap,
                          const int32_t* __restrict__ Aj, const double* __restrict__ Av,
                          const int32_t* __restrict__ Bp, const int32_t* __restrict__ Bk,
                          const double* __restrict__ Bv, int32_t ncols, const long long* __restrict__ eoff,
-                         long long base, unsigned long long* __restrict__ keys, unsigned long long* __restrict__ vals) {
+                         long long base, K* __restrict__ keys, unsigned long long* __restrict__ vals) {
   const int lane = threadIdx.x & 31;
   const int64_t qg = q0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
   if (qg >= q1) return;
@@ -102,13 +103,14 @@ __global__ void k_expand(int32_t r0, int32_t r1, int64_t q0, int64_t q1, const i
     const unsigned long long o_key = __shfl_sync(0xffffffffu, rowkey, owner);
     if (f < total) {
       const int32_t p = o_s + (f - o_excl);
-      keys[out + f] = o_key + (unsigned long long)Bk[p];
+      keys[out + f] = (K)(o_key + (unsigned long long)Bk[p]);
       vals[out + f] = __double_as_longlong(__dmul_rn(o_a, Bv[p]));
     }
   }
 }
 
-__global__ void k_heads(int64_t n, const unsigned long long* __restrict__ keys, int32_t* __restrict__ head) {
+template <typename K>
+__global__ void k_heads(int64_t n, const K* __restrict__ keys, int32_t* __restrict__ head) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   head[p] = (p == 0 || keys[p] != keys[p - 1]) ? 1 : 0;
@@ -126,8 +128,9 @@ __global__ void k_run_starts(int64_t n, const int32_t* __restrict__ head, const 
 // a row records its index in first[row], and the row's count is taken from
 // that by k_row_counts (no per-run atomic on a shared counter: the runs of a
 // heavy row would all serialise on it).
+template <typename K>
 __global__ void k_reduce_runs(int64_t nruns, int64_t n, const long long* __restrict__ starts,
-                              const unsigned long long* __restrict__ keys, const unsigned long long* __restrict__ vals,
+                              const K* __restrict__ keys, const unsigned long long* __restrict__ vals,
                               int32_t ncols, int32_t* __restrict__ out_crd, double* __restrict__ out_val,
                               long long* __restrict__ first) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -136,21 +139,22 @@ __global__ void k_reduce_runs(int64_t nruns, int64_t n, const long long* __restr
   const long long e = r + 1 < nruns ? starts[r + 1] : n;
   double v = __longlong_as_double((long long)vals[s]);
   for (long long q = s + 1; q < e; q++) v = __dadd_rn(v, __longlong_as_double((long long)vals[q]));
-  const unsigned long long k = keys[s];
-  const unsigned long long row = k / (unsigned long long)ncols;
-  out_crd[r] = (int32_t)(k - row * (unsigned long long)ncols);
+  const K k = keys[s];
+  const K row = k / (K)ncols;
+  out_crd[r] = (int32_t)(k - row * (K)ncols);
   out_val[r] = v;
-  if (r == 0 || keys[starts[r - 1]] / (unsigned long long)ncols != row) first[row] = r;
+  if (r == 0 || keys[starts[r - 1]] / (K)ncols != row) first[row] = r;
 }
 
 // The last run of each row writes the row's output count.
-__global__ void k_row_counts(int64_t nruns, const long long* __restrict__ starts,
-                             const unsigned long long* __restrict__ keys, int32_t ncols, int32_t r0,
-                             const long long* __restrict__ first, int32_t* __restrict__ rowcnt) {
+template <typename K>
+__global__ void k_row_counts(int64_t nruns, const long long* __restrict__ starts, const K* __restrict__ keys,
+                             int32_t ncols, int32_t r0, const long long* __restrict__ first,
+                             int32_t* __restrict__ rowcnt) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nruns) return;
-  const unsigned long long row = keys[starts[r]] / (unsigned long long)ncols;
-  if (r + 1 == nruns || keys[starts[r + 1]] / (unsigned long long)ncols != row)
+  const K row = keys[starts[r]] / (K)ncols;
+  if (r + 1 == nruns || keys[starts[r + 1]] / (K)ncols != row)
     rowcnt[r0 + (int32_t)row] = (int32_t)(r + 1 - first[row]);
 }
 
@@ -158,6 +162,96 @@ int bits_for(unsigned long long max_key_exclusive) {
   int b = 0;
   while (b < 64 && (1ull << b) < max_key_exclusive) b++;
   return b;
+}
+
+// One chunk's output entries (C.crd, C.vals pieces, concatenated at the end).
+struct Part {
+  int32_t* crd;
+  double* val;
+  long long n;
+};
+
+constexpr unsigned long long kMinRows32 = 1024;  // 32-bit keys when a chunk may hold this many rows
+
+// Expand, sort and reduce every chunk [cuts[c], cuts[c + 1]) of rows with K
+// keys; the row counts go to rowcnt, the entries to `parts`.
+template <typename K>
+int coord_chunks(const CsrView& A, const CsrView& B, const std::vector<int32_t>& cuts,
+                 const std::vector<long long>& hoff, const std::vector<int32_t>& hApos, const long long* eoff,
+                 int32_t* rowcnt, long long* tot, std::vector<Part>* parts, long long* nnz_out, cudaStream_t s) {
+  const int32_t ncols = B.ncols;
+  long long max_chunk = 0;
+  int32_t max_rows = 1;
+  for (size_t c = 0; c + 1 < cuts.size(); c++) {
+    max_chunk = std::max(max_chunk, hoff[cuts[c + 1]] - hoff[cuts[c]]);
+    max_rows = std::max(max_rows, cuts[c + 1] - cuts[c]);
+  }
+  const size_t cap = (size_t)std::max<long long>(max_chunk, 1);
+  K *k0 = nullptr, *k1 = nullptr;
+  unsigned long long *v0 = nullptr, *v1 = nullptr;
+  int32_t* head = nullptr;
+  long long *hpos = nullptr, *starts = nullptr;
+  long long* first = nullptr;  // per row of a chunk: its first run
+  int rc = SPWS_OK;
+  auto release = [&]() {
+    dfree(k0, s); dfree(v0, s); dfree(k1, s); dfree(v1, s);
+    dfree(head, s); dfree(hpos, s); dfree(starts, s); dfree(first, s);
+  };
+  if ((rc = dalloc((void**)&k0, sizeof(K) * cap, s)) != SPWS_OK ||
+      (rc = dalloc((void**)&v0, sizeof(unsigned long long) * cap, s)) != SPWS_OK ||
+      (rc = dalloc((void**)&k1, sizeof(K) * cap, s)) != SPWS_OK ||
+      (rc = dalloc((void**)&v1, sizeof(unsigned long long) * cap, s)) != SPWS_OK ||
+      (rc = dalloc((void**)&head, sizeof(int32_t) * cap, s)) != SPWS_OK ||
+      (rc = dalloc((void**)&hpos, sizeof(long long) * cap, s)) != SPWS_OK ||
+      (rc = dalloc((void**)&starts, sizeof(long long) * cap, s)) != SPWS_OK ||
+      (rc = dalloc((void**)&first, sizeof(long long) * (size_t)max_rows, s)) != SPWS_OK) {
+    release();
+    return rc;
+  }
+  long long nnz = 0;
+  for (size_t c = 0; c + 1 < cuts.size() && rc == SPWS_OK; c++) {
+    const int32_t r0 = cuts[c], r1 = cuts[c + 1];
+    const long long n = hoff[r1] - hoff[r0];
+    if (n == 0) continue;
+    const int64_t q0 = hApos[r0], q1 = hApos[r1];  // the chunk's A entries
+    const int64_t groups = (q1 - q0 + 31) / 32;
+    k_expand<K><<<(unsigned)((groups + 7) / 8), 256, 0, s>>>(r0, r1, q0, q1, A.pos, A.crd, A.vals, B.pos, B.crd,
+                                                            B.vals, ncols, eoff, hoff[r0], k0, v0);
+    count_launch(1);
+    bool in_tmp = false;
+    const int bits = bits_for((unsigned long long)(r1 - r0) * (unsigned long long)std::max(ncols, 1));
+    if ((rc = radix_sort_pairs(k0, v0, k1, v1, n, bits, &in_tmp, s)) != SPWS_OK) break;
+    const K* ks = in_tmp ? k1 : k0;
+    const unsigned long long* vs = in_tmp ? v1 : v0;
+    k_heads<K><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, ks, head);
+    count_launch(1);
+    if ((rc = scan_i32_to_i64(head, hpos, n, tot, s)) != SPWS_OK) break;
+    k_run_starts<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, head, hpos, starts);
+    count_launch(1);
+    long long nruns = 0;
+    Readback rb(s);
+    if ((rc = rb.get(&nruns, tot, sizeof(long long))) != SPWS_OK || (rc = rb.wait()) != SPWS_OK) break;
+    Part pt{nullptr, nullptr, nruns};
+    if ((rc = dalloc((void**)&pt.crd, sizeof(int32_t) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
+    if ((rc = dalloc((void**)&pt.val, sizeof(double) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) {
+      dfree(pt.crd, s);
+      break;
+    }
+    // first run of each row of the chunk (rows without products keep the count 0 they started with)
+    k_reduce_runs<K><<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, n, starts, ks, vs, ncols, pt.crd,
+                                                                     pt.val, first);
+    k_row_counts<K><<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, starts, ks, ncols, r0, first, rowcnt);
+    count_launch(2);
+    if (cudaGetLastError() != cudaSuccess) {
+      set_error("coordinate workspace: kernel launch failed");
+      rc = SPWS_ERR_CUDA;
+    }
+    parts->push_back(pt);
+    nnz += nruns;
+  }
+  release();
+  *nnz_out = nnz;
+  return rc;
 }
 
 }  // namespace
@@ -208,81 +302,29 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
   SPWS_CUDA(cudaStreamSynchronize(s));
   const long long total_products = hoff[nA];
 
+  // Keys (row - r0) * ncols + col fit 32 bits when a chunk holds at most
+  // 2^32 / ncols rows; with narrow enough B (at least kMinRows32 rows a chunk)
+  // chunks are cut to that too, and the sort moves 12 bytes an item instead
+  // of 16.
+  const bool k32 = (unsigned long long)std::max(ncols, 1) * kMinRows32 <= (1ull << 32);
+  const int32_t row_cap =
+      k32 ? (int32_t)std::min<unsigned long long>((1ull << 32) / (unsigned long long)std::max(ncols, 1), INT32_MAX)
+          : INT32_MAX;
   // chunk boundaries: consecutive rows whose products fit the budget (a row
-  // larger than the budget forms a chunk of its own)
+  // larger than the budget forms a chunk of its own), at most row_cap rows
   std::vector<int32_t> cuts{0};
   while (cuts.back() < nA) {
     const int32_t r0 = cuts.back();
     const long long lim = hoff[r0] + kChunkProducts;
     int32_t r1 = (int32_t)(std::upper_bound(hoff.begin() + r0 + 1, hoff.end(), lim) - hoff.begin()) - 1;
     if (r1 <= r0) r1 = r0 + 1;
+    r1 = (int32_t)std::min<long long>((long long)r1, (long long)r0 + row_cap);
     cuts.push_back(std::min(r1, nA));
   }
-  long long max_chunk = 0;
-  int32_t max_rows = 1;
-  for (size_t c = 0; c + 1 < cuts.size(); c++) {
-    max_chunk = std::max(max_chunk, hoff[cuts[c + 1]] - hoff[cuts[c]]);
-    max_rows = std::max(max_rows, cuts[c + 1] - cuts[c]);
-  }
-  const size_t cap = (size_t)std::max<long long>(max_chunk, 1);
-
-  unsigned long long *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr;
-  int32_t* head = nullptr;
-  long long *hpos = nullptr, *starts = nullptr;
-  SPWS_TRY(dalloc((void**)&k0, sizeof(unsigned long long) * cap, s));
-  SPWS_TRY(dalloc((void**)&v0, sizeof(unsigned long long) * cap, s));
-  SPWS_TRY(dalloc((void**)&k1, sizeof(unsigned long long) * cap, s));
-  SPWS_TRY(dalloc((void**)&v1, sizeof(unsigned long long) * cap, s));
-  SPWS_TRY(dalloc((void**)&head, sizeof(int32_t) * cap, s));
-  SPWS_TRY(dalloc((void**)&hpos, sizeof(long long) * cap, s));
-  SPWS_TRY(dalloc((void**)&starts, sizeof(long long) * cap, s));
-  long long* first = nullptr;  // per row of a chunk: its first run
-  SPWS_TRY(dalloc((void**)&first, sizeof(long long) * (size_t)max_rows, s));
-
-  struct Part {
-    int32_t* crd;
-    double* val;
-    long long n;
-  };
   std::vector<Part> parts;
   long long nnz = 0;
-  int rc = SPWS_OK;
-  for (size_t c = 0; c + 1 < cuts.size() && rc == SPWS_OK; c++) {
-    const int32_t r0 = cuts[c], r1 = cuts[c + 1];
-    const long long n = hoff[r1] - hoff[r0];
-    if (n == 0) continue;
-    const int64_t q0 = hApos[r0], q1 = hApos[r1];  // the chunk's A entries
-    const int64_t groups = (q1 - q0 + 31) / 32;
-    k_expand<<<(unsigned)((groups + 7) / 8), 256, 0, s>>>(r0, r1, q0, q1, A.pos, A.crd, A.vals, B.pos, B.crd, B.vals,
-                                                         ncols, eoff, hoff[r0], k0, v0);
-    count_launch(1);
-    bool in_tmp = false;
-    const int bits = bits_for((unsigned long long)(r1 - r0) * (unsigned long long)std::max(ncols, 1));
-    if ((rc = radix_sort_pairs(k0, v0, k1, v1, n, bits, &in_tmp, s)) != SPWS_OK) break;
-    const unsigned long long* ks = in_tmp ? k1 : k0;
-    const unsigned long long* vs = in_tmp ? v1 : v0;
-    k_heads<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, ks, head);
-    count_launch(1);
-    if ((rc = scan_i32_to_i64(head, hpos, n, tot, s)) != SPWS_OK) break;
-    k_run_starts<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, head, hpos, starts);
-    count_launch(1);
-    long long nruns = 0;
-    Readback rb(s);
-    if ((rc = rb.get(&nruns, tot, sizeof(long long))) != SPWS_OK || (rc = rb.wait()) != SPWS_OK) break;
-    Part pt{nullptr, nullptr, nruns};
-    if ((rc = dalloc((void**)&pt.crd, sizeof(int32_t) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
-    if ((rc = dalloc((void**)&pt.val, sizeof(double) * (size_t)std::max<long long>(nruns, 1), s)) != SPWS_OK) break;
-    // first run of each row of the chunk (rows without products keep the count 0 they started with)
-    k_reduce_runs<<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, n, starts, ks, vs, ncols, pt.crd, pt.val,
-                                                                  first);
-    k_row_counts<<<(unsigned)((nruns + 255) / 256), 256, 0, s>>>(nruns, starts, ks, ncols, r0, first, rowcnt);
-    count_launch(2);
-    SPWS_CUDA(cudaGetLastError());
-    parts.push_back(pt);
-    nnz += nruns;
-  }
-  dfree(k0, s); dfree(v0, s); dfree(k1, s); dfree(v1, s);
-  dfree(head, s); dfree(hpos, s); dfree(starts, s); dfree(first, s);
+  int rc = k32 ? coord_chunks<uint32_t>(A, B, cuts, hoff, hApos, eoff, rowcnt, tot, &parts, &nnz, s)
+               : coord_chunks<unsigned long long>(A, B, cuts, hoff, hApos, eoff, rowcnt, tot, &parts, &nnz, s);
   if (rc == SPWS_OK && nnz > INT32_MAX) {
     set_error("output has more than INT32_MAX nonzeros");
     rc = SPWS_ERR_CAPACITY;
