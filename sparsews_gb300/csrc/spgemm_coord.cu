@@ -171,8 +171,6 @@ struct Part {
   long long n;
 };
 
-constexpr unsigned long long kMinRows32 = 1024;  // 32-bit keys when a chunk may hold this many rows
-
 // Expand, sort and reduce every chunk [cuts[c], cuts[c + 1]) of rows with K
 // keys; the row counts go to rowcnt, the entries to `parts`.
 template <typename K>
@@ -302,24 +300,33 @@ int spgemm_coord(const CsrView& A, const CsrView& B, spws_csr_dev* C, spws_spgem
   SPWS_CUDA(cudaStreamSynchronize(s));
   const long long total_products = hoff[nA];
 
-  // Keys (row - r0) * ncols + col fit 32 bits when a chunk holds at most
-  // 2^32 / ncols rows; with narrow enough B (at least kMinRows32 rows a chunk)
-  // chunks are cut to that too, and the sort moves 12 bytes an item instead
-  // of 16.
-  const bool k32 = (unsigned long long)std::max(ncols, 1) * kMinRows32 <= (1ull << 32);
-  const int32_t row_cap =
-      k32 ? (int32_t)std::min<unsigned long long>((1ull << 32) / (unsigned long long)std::max(ncols, 1), INT32_MAX)
-          : INT32_MAX;
   // chunk boundaries: consecutive rows whose products fit the budget (a row
   // larger than the budget forms a chunk of its own), at most row_cap rows
-  std::vector<int32_t> cuts{0};
-  while (cuts.back() < nA) {
-    const int32_t r0 = cuts.back();
-    const long long lim = hoff[r0] + kChunkProducts;
-    int32_t r1 = (int32_t)(std::upper_bound(hoff.begin() + r0 + 1, hoff.end(), lim) - hoff.begin()) - 1;
-    if (r1 <= r0) r1 = r0 + 1;
-    r1 = (int32_t)std::min<long long>((long long)r1, (long long)r0 + row_cap);
-    cuts.push_back(std::min(r1, nA));
+  auto cut = [&](long long row_cap) {
+    std::vector<int32_t> cuts{0};
+    while (cuts.back() < nA) {
+      const int32_t r0 = cuts.back();
+      const long long lim = hoff[r0] + kChunkProducts;
+      int32_t r1 = (int32_t)(std::upper_bound(hoff.begin() + r0 + 1, hoff.end(), lim) - hoff.begin()) - 1;
+      if (r1 <= r0) r1 = r0 + 1;
+      r1 = (int32_t)std::min<long long>((long long)r1, (long long)r0 + row_cap);
+      cuts.push_back(std::min(r1, nA));
+    }
+    return cuts;
+  };
+  // Keys (row - r0) * ncols + col fit 32 bits when a chunk holds at most
+  // 2^32 / ncols rows. Chunks cut to that as well move 12 bytes an item per
+  // sort pass instead of 16; taken unless the cap multiplies the chunks
+  // (each costs a few launches and a host read).
+  std::vector<int32_t> cuts = cut(INT32_MAX);
+  bool k32 = false;
+  {
+    const long long cap32 = (long long)((1ull << 32) / (unsigned long long)std::max(ncols, 1));
+    std::vector<int32_t> c32 = cut(cap32);
+    if (c32.size() - 1 <= 2 * (cuts.size() - 1) + 8) {
+      cuts.swap(c32);
+      k32 = true;
+    }
   }
   std::vector<Part> parts;
   long long nnz = 0;
