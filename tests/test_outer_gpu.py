@@ -60,6 +60,29 @@ def test_coord_against_oracle(spws_lib, case):
     assert np.array_equal(got_t[2], ref[2])
 
 
+def _random_csr(nrows, ncols, per_row, seed):
+    rng = np.random.default_rng(seed)
+    rows = [np.unique(rng.integers(0, ncols, per_row)) for _ in range(nrows)]
+    pos = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+    crd = np.concatenate(rows).astype(np.int32)
+    return pos, crd, rng.uniform(-1.0, 1.0, len(crd)), nrows, ncols
+
+
+@pytest.mark.parametrize("ncols_log2", [22, 26])
+def test_coord_wide_outputs(spws_lib, ncols_log2):
+    """Wide outputs: with 2^22 columns the chunks are capped at 1024 rows for
+    32-bit sort keys (three chunks here); with 2^26 the cap would cut the
+    product into 47 chunks, so the sort keeps 64-bit keys. Bit-exact with
+    the oracle's visiting-order sums either way."""
+    import sparsews_gb300 as sp
+    A = _random_csr(3000, 500, 12, seed=65)
+    B = _random_csr(500, 1 << ncols_log2, 20, seed=66)
+    got = sp.spgemm(A, B, method="coord")
+    ref = oracle.spgemm("hash", A, B, w_cap=1 << 24)
+    assert_csr_equal_structure(got, ref, f"2^{ncols_log2} columns")
+    assert np.array_equal(got[2], ref[2])
+
+
 def test_outer_against_oracle_rmat(spws_lib):
     import sparsews_gb300 as sp
     A = gen.rmat(12, 10, seed=64)
