@@ -95,3 +95,82 @@ def test_injection_disarms_after_one_failure(spws_lib):
     assert_csr_close(got, oracle.spgemm("hash", A, A), oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2], "after")
     L.spws_inject_alloc_failure(0)
     assert np.all(np.diff(got[0]) >= 0)
+
+
+def test_batched_fails_cleanly_at_every_allocation(spws_lib):
+    """The batched form: each of its allocations refused in turn gives
+    SPWS_ERR_NOMEM (or, for an optional buffer, a correct result), and the
+    next batch matches the oracle."""
+    import sparsews_gb300 as sp
+    L = sp.lib()
+    insts = [gen.er(3000, 8, seed=71), gen.rmat(11, 8, seed=72), gen.er(700, 5, seed=73)]
+    dev = [sp.DeviceCsr.upload(*A) for A in insts]
+    refs = [(oracle.spgemm("hash", A, A), oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2]) for A in insts]
+
+    def check_all(batch, what):
+        for i, (ref, scale) in enumerate(refs):
+            assert_csr_close(batch.download(i), ref, scale, f"{what}, instance {i}")
+
+    def ok():
+        b = sp.spgemm_batched(dev, dev)
+        check_all(b, "plain batch")
+        b.release()
+
+    n = _allocs_of(L, ok)
+    assert n >= 3
+    failed = 0
+    for k in range(1, n + 1):
+        L.spws_inject_alloc_failure(k)
+        try:
+            b = sp.spgemm_batched(dev, dev)
+        except sp.SpwsError as e:
+            assert e.status == NOMEM, (k, e.status)
+            failed += 1
+        else:
+            check_all(b, f"allocation {k} refused")
+            b.release()
+        finally:
+            L.spws_inject_alloc_failure(0)
+        ok()
+    assert failed >= 1
+    for d in dev:
+        d.release()
+
+
+def test_served_request_fails_cleanly_and_server_continues(spws_lib):
+    """A served request whose allocation is refused finishes with
+    SPWS_ERR_NOMEM (reported through its ticket); the server keeps serving."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import served
+    L = sp.lib()
+    A = gen.rmat(11, 8, seed=74)
+    ref = oracle.spgemm("hash", A, A)
+    scale = oracle.spgemm("taco", abs_csr(A), abs_csr(A))[2]
+    dA = sp.DeviceCsr.upload(*A)
+    srv = served.Server(workers=2)
+    try:
+        t = srv.submit_spgemm(dA, dA)
+        srv.wait(t)
+        assert_csr_close(srv.result_csr(t).download(), ref, scale, "served")
+        srv.release(t)
+        nomem = 0
+        for k in range(1, 4):
+            L.spws_inject_alloc_failure(k)
+            t = srv.submit_spgemm(dA, dA)
+            info = srv.wait(t, raise_on_error=False)
+            L.spws_inject_alloc_failure(0)
+            assert info.status in (0, NOMEM), (k, info.status)
+            if info.status == NOMEM:
+                nomem += 1
+            else:
+                assert_csr_close(srv.result_csr(t).download(), ref, scale, f"served, allocation {k} refused")
+            srv.release(t)
+            t = srv.submit_spgemm(dA, dA)  # the server keeps working
+            srv.wait(t)
+            assert_csr_close(srv.result_csr(t).download(), ref, scale, f"served after failure {k}")
+            srv.release(t)
+        assert nomem >= 1
+    finally:
+        L.spws_inject_alloc_failure(0)
+        srv.close()
+        dA.release()
