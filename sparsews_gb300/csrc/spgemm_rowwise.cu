@@ -519,7 +519,7 @@ __device__ __forceinline__ int words_in(long long wl, int32_t hi) {
 }
 
 // Symbolic pass: per row, the number of distinct output columns.
-__global__ void __launch_bounds__(kThreads, 3) k_symbolic(PassArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) k_symbolic(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   uint32_t* bm = reinterpret_cast<uint32_t*>(smem);  // kSpanWords
   Batch& b = *reinterpret_cast<Batch*>(smem + sizeof(uint32_t) * kSpanWords);
