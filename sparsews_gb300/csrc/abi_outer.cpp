@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "abi_util.h"
 #include "convert.h"
@@ -64,11 +65,49 @@ int up(const T* h, size_t n, DevBuf* b, cudaStream_t s) {
 // outer_mode 1 = DCSC (outer level over columns), 0 = DCSR. With transposed
 // set, a DCSC's arrays are read as the DCSR of its transpose (no sort), so
 // the result is the CSR of the transpose.
+// A dense outer level instead (the CSC / CSR layout of
+// utils/dataloader.h:374-399: indices[0][0] = {dim}, positions over every
+// outer index) is read as a compressed one whose outer coordinates are
+// 0 .. dim-1, so the DCSC x DCSR entry points also take the CSC x CSR
+// operands of the reference's benchmark/CSC_CSR_T drivers. The two layouts
+// are told apart by indices[0][0][0]: a compressed level's positions start
+// at 0, a dense level stores its dimension there (mode_types is not read:
+// the reference's builders leave it unset).
 int cc_to_dev_csr(const taco_tensor_t* t, const char* what, int outer_mode, DevCsr* out, cudaStream_t s,
                   bool transposed = false) {
   int32_t nq;
   int64_t nnz;
-  SPWS_TRY(check_cc(t, what, outer_mode, &nq, &nnz));
+  if (!t || t->order != 2 || !t->dimensions || !t->indices || !t->indices[0] || !t->indices[0][0] ||
+      !t->indices[1] || !t->indices[1][0]) {
+    set_error(std::string(what) + ": expected an order-2 tensor with a compressed inner level");
+    return SPWS_ERR_INVALID;
+  }
+  const bool dense_outer = t->indices[0][0][0] != 0 || t->dimensions[outer_mode] == 0;
+  std::vector<int32_t> iota;
+  if (dense_outer) {
+    if (t->indices[0][0][0] != t->dimensions[outer_mode]) {
+      set_error(std::string(what) + ": outer level is neither compressed (positions from 0) nor dense (its dimension)");
+      return SPWS_ERR_INVALID;
+    }
+    if (t->mode_ordering && t->mode_ordering[0] != outer_mode) {
+      set_error(std::string(what) + ": unexpected mode ordering");
+      return SPWS_ERR_INVALID;
+    }
+    nq = t->dimensions[outer_mode];
+    if (nq < 0) {
+      set_error(std::string(what) + ": negative dimension");
+      return SPWS_ERR_INVALID;
+    }
+    nnz = t->indices[1][0][nq];
+    if (nnz < 0 || (nnz > 0 && (!t->indices[1][1] || !t->vals))) {
+      set_error(std::string(what) + ": missing crd/vals arrays");
+      return SPWS_ERR_INVALID;
+    }
+    iota.resize((size_t)nq);
+    for (int32_t q = 0; q < nq; q++) iota[(size_t)q] = q;
+  } else {
+    SPWS_TRY(check_cc(t, what, outer_mode, &nq, &nnz));
+  }
   const int32_t nrows = t->dimensions[0], ncols = t->dimensions[1];
   if (nrows < 0 || ncols < 0) {
     set_error(std::string(what) + ": negative dimension");
@@ -77,7 +116,7 @@ int cc_to_dev_csr(const taco_tensor_t* t, const char* what, int outer_mode, DevC
   const int32_t outer_dim = outer_mode == 1 ? ncols : nrows;
   const int32_t inner_dim = outer_mode == 1 ? nrows : ncols;
   DevBuf oc, pos, ic, vals;
-  SPWS_TRY(up(t->indices[0][1], (size_t)nq, &oc, s));
+  SPWS_TRY(up(dense_outer ? iota.data() : t->indices[0][1], (size_t)nq, &oc, s));
   SPWS_TRY(up(t->indices[1][0], (size_t)nq + 1, &pos, s));
   SPWS_TRY(up(t->indices[1][1], (size_t)nnz, &ic, s));
   SPWS_TRY(up(t->vals, (size_t)nnz, &vals, s));

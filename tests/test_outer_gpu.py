@@ -146,6 +146,41 @@ def test_outer_transposed_golden_and_oracle(spws_lib, method):
     assert_csr_equal_structure(got, fused, "DCSC x DCSR vs CSC x CSR")
 
 
+@pytest.mark.parametrize("method", ["hash", "bucket", "coord"])
+def test_outer_entries_take_dense_outer_operands(spws_lib, method):
+    """The DCSC x DCSR entry points also take dense-outer CSC x CSR operands
+    (utils/dataloader.h:374-399: indices[0][0] = {dim}, as the reference's
+    benchmark/CSC_CSR_T drivers build them), empty columns included: the
+    same results as with compressed outer levels."""
+    import sparsews_gb300 as sp
+    from sparsews_gb300 import taco
+    L = sp.lib()
+    A, B = gen.rmat(10, 6, seed=81), gen.rmat(10, 5, seed=82)
+    ap, ac, av, an, am = A
+    bp, bc, bv, bn, bm = B
+    tp, tc, tv = sp._csr_transpose_np(ap, ac, av, an, am)
+    assert (np.diff(tp) == 0).any()  # some columns of A are empty
+    Acsc, Bcsr = taco.csc(tp, tc, tv, an, am), taco.csr(bp, bc, bv, bn, bm)
+    sT = oracle.spgemm_outer_t(abs_csr(A), abs_csr(B), w_cap=1 << 22)[2]
+    Ct = taco.init_dc(bm, an)
+    fn = {"hash": L.spws_dcsc_dcsr_t_hash_compute, "bucket": L.spws_dcsc_dcsr_t_bucket_compute,
+          "coord": L.spws_dcsc_dcsr_t_coord_compute}[method]
+    sp.check(fn(Ct.ptr(), Acsc.ptr(), Bcsr.ptr(), 0))
+    got_t = taco.take_csr(Ct, bm, L.spws_free)
+    ref_t = sp.spgemm_outer_t(A, B, method)
+    assert_csr_close(got_t, ref_t, sT, f"transposed, dense outer, {method}")
+    s = oracle.spgemm("taco", abs_csr(A), abs_csr(B))[2]
+    Cn = taco.init_dc(an, bm)
+    fn = {"hash": L.spws_dcsc_dcsr_hash_compute, "bucket": L.spws_dcsc_dcsr_bucket_compute,
+          "coord": L.spws_dcsc_dcsr_coord_compute}[method]
+    sp.check(fn(Cn.ptr(), Acsc.ptr(), Bcsr.ptr(), 0))
+    got = taco.take_csr(Cn, an, L.spws_free)
+    ref = sp.spgemm_outer(A, B, method)
+    assert_csr_close(got, ref, s, f"dense outer, {method}")
+    if method == "coord":  # visiting-order sums: bit-exact both ways
+        assert np.array_equal(got_t[2], ref_t[2]) and np.array_equal(got[2], ref[2])
+
+
 def test_transposed_nofuse_golden(spws_lib):
     """The non-fused form against the reference's own outputs
     (evaluate/CSC_CSR_T_hash_record_nofuse.h): C_noT = A*B and C = C_noT^T."""
